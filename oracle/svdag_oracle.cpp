@@ -1,0 +1,658 @@
+// CPU oracle: a restatement of the reference SymVox / SVDAG-Compression
+// build path.  TEST INFRASTRUCTURE ONLY (see svdag_oracle.h): it is the
+// checker the CUDA path is compared against, never part of the product.
+//
+// Each function cites the reference lines it restates (paths relative to the
+// reference project).  The data structures follow the reference's own
+// (ordered maps, explicit DFS stack) so that its CPU timing is representative
+// of the reference when it is used as the CPU baseline.
+//
+// Build with -ffp-contract=off: the fp64 triangle/box test must not be fused.
+#include "svdag_oracle.h"
+
+#include <omp.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <set>
+#include <stack>
+#include <utility>
+#include <vector>
+
+namespace {
+
+const uint32_t kNull = 0xFFFFFFFEu;  // Octree::nullNode (src/symvox/octree.cpp:22)
+
+// GeomOctree::Node (src/symvox/octree.hpp:57-85, src/symvox/geom_octree.hpp:59-96)
+struct Node {
+  uint8_t mask;
+  uint8_t mir[3];
+  uint8_t inv;
+  uint32_t ch[8];
+  uint32_t clev[8];
+  Node() : mask(0), inv(0) {
+    mir[0] = mir[1] = mir[2] = 0;
+    for (int c = 0; c < 8; ++c) { ch[c] = kNull; clev[c] = 0xFFFFFFFFu; }
+  }
+  bool has_ptr(int c) const { return ch[c] != kNull; }
+  bool has_child(int c) const { return (mask >> c) & 1u; }
+};
+
+// Node::operator== / operator< (src/symvox/octree_node.cpp:39-86): the key is
+// (childrenBitmask, children[0..7], childrenMirroredBitmask[0..2]).
+inline bool key_eq(const Node& a, const Node& b) {
+  if (a.mask != b.mask) return false;
+  for (int c = 0; c < 8; ++c) if (a.ch[c] != b.ch[c]) return false;
+  return a.mir[0] == b.mir[0] && a.mir[1] == b.mir[1] && a.mir[2] == b.mir[2];
+}
+struct KeyLess {
+  bool operator()(const Node& a, const Node& b) const {
+    if (a.mask != b.mask) return a.mask < b.mask;
+    for (int c = 0; c < 8; ++c) if (a.ch[c] != b.ch[c]) return a.ch[c] < b.ch[c];
+    for (int k = 0; k < 3; ++k) if (a.mir[k] != b.mir[k]) return a.mir[k] < b.mir[k];
+    return false;
+  }
+};
+
+// Node::mirror (src/symvox/octree_node.cpp:88-195): child index 4x+2y+z, an
+// x mirror swaps c <-> c^4, y swaps c <-> c^2, z swaps c <-> c^1, for the
+// mask, the three mirror masks and the child pointers; then the mirror bit of
+// every mirrored axis is toggled for each child that has a pointer.  The
+// result's invariant mask is 0 (the reference builds it in a fresh Node).
+inline uint8_t permute_bits(uint8_t m, int flip) {
+  uint8_t r = 0;
+  for (int c = 0; c < 8; ++c) if ((m >> c) & 1u) r |= uint8_t(1u << (c ^ flip));
+  return r;
+}
+Node mirror(const Node& n, bool x, bool y, bool z) {
+  int flip = (x ? 4 : 0) | (y ? 2 : 0) | (z ? 1 : 0);
+  Node r;
+  if (flip == 0) return n;
+  r.mask = permute_bits(n.mask, flip);
+  for (int k = 0; k < 3; ++k) r.mir[k] = permute_bits(n.mir[k], flip);
+  for (int c = 0; c < 8; ++c) r.ch[c] = n.ch[c ^ flip];
+  r.inv = 0;
+  for (int c = 0; c < 8; ++c) {
+    if (r.has_ptr(c)) {
+      if (x) r.mir[0] ^= uint8_t(1u << c);
+      if (y) r.mir[1] ^= uint8_t(1u << c);
+      if (z) r.mir[2] ^= uint8_t(1u << c);
+    }
+  }
+  return r;
+}
+
+inline unsigned popc8(uint8_t m) { return unsigned(__builtin_popcount(m)); }
+
+// ---------------------------------------------------------------------------
+// Triangle / box overlap, fp64 (src/symvox/test_triangle_box.cpp:38-184).
+// Every operation below is one IEEE double operation in the reference's order.
+
+bool plane_box_overlap(const double n[3], const double v[3], double maxbox) {
+  double vmin[3], vmax[3];
+  for (int q = 0; q < 3; ++q) {
+    if (n[q] > 0.0) { vmin[q] = -maxbox - v[q]; vmax[q] = maxbox - v[q]; }
+    else            { vmin[q] = maxbox - v[q];  vmax[q] = -maxbox - v[q]; }
+  }
+  double d = n[0] * vmin[0];
+  d = d + n[1] * vmin[1];
+  d = d + n[2] * vmin[2];
+  if (d > 0.0) return false;
+  double e = n[0] * vmax[0];
+  e = e + n[1] * vmax[1];
+  e = e + n[2] * vmax[2];
+  if (e >= 0.0) return true;
+  return false;
+}
+
+inline bool axis_reject(double pa, double pb, double fa, double fb, double h, bool b_first) {
+  double mn, mx;
+  // Z12 orders its pair as (p2 < p1); the other macros as (first < second).
+  if (b_first) { if (pb < pa) { mn = pb; mx = pa; } else { mn = pa; mx = pb; } }
+  else         { if (pa < pb) { mn = pa; mx = pb; } else { mn = pb; mx = pa; } }
+  double rad = (fa + fb) * h;
+  return (mn > rad || mx < -rad);
+}
+
+bool tri_box(const double c[3], double h, const float* t) {
+  double v0[3], v1[3], v2[3], e0[3], e1[3], e2[3];
+  for (int k = 0; k < 3; ++k) {
+    v0[k] = double(t[k]) - c[k];
+    v1[k] = double(t[3 + k]) - c[k];
+    v2[k] = double(t[6 + k]) - c[k];
+  }
+  for (int k = 0; k < 3; ++k) { e0[k] = v1[k] - v0[k]; e1[k] = v2[k] - v1[k]; e2[k] = v0[k] - v2[k]; }
+  const int X = 0, Y = 1, Z = 2;
+  double fex, fey, fez, a, b;
+  // edge 0: X01, Y02, Z12
+  fex = std::fabs(e0[X]); fey = std::fabs(e0[Y]); fez = std::fabs(e0[Z]);
+  a = e0[Z]; b = e0[Y];
+  if (axis_reject(a * v0[Y] - b * v0[Z], a * v2[Y] - b * v2[Z], fez, fey, h, false)) return false;
+  a = e0[Z]; b = e0[X];
+  if (axis_reject(-a * v0[X] + b * v0[Z], -a * v2[X] + b * v2[Z], fez, fex, h, false)) return false;
+  a = e0[Y]; b = e0[X];
+  if (axis_reject(a * v1[X] - b * v1[Y], a * v2[X] - b * v2[Y], fey, fex, h, true)) return false;
+  // edge 1: X01, Y02, Z0
+  fex = std::fabs(e1[X]); fey = std::fabs(e1[Y]); fez = std::fabs(e1[Z]);
+  a = e1[Z]; b = e1[Y];
+  if (axis_reject(a * v0[Y] - b * v0[Z], a * v2[Y] - b * v2[Z], fez, fey, h, false)) return false;
+  a = e1[Z]; b = e1[X];
+  if (axis_reject(-a * v0[X] + b * v0[Z], -a * v2[X] + b * v2[Z], fez, fex, h, false)) return false;
+  a = e1[Y]; b = e1[X];
+  if (axis_reject(a * v0[X] - b * v0[Y], a * v1[X] - b * v1[Y], fey, fex, h, false)) return false;
+  // edge 2: X2, Y1, Z12
+  fex = std::fabs(e2[X]); fey = std::fabs(e2[Y]); fez = std::fabs(e2[Z]);
+  a = e2[Z]; b = e2[Y];
+  if (axis_reject(a * v0[Y] - b * v0[Z], a * v1[Y] - b * v1[Z], fez, fey, h, false)) return false;
+  a = e2[Z]; b = e2[X];
+  if (axis_reject(-a * v0[X] + b * v0[Z], -a * v1[X] + b * v1[Z], fez, fex, h, false)) return false;
+  a = e2[Y]; b = e2[X];
+  if (axis_reject(a * v1[X] - b * v1[Y], a * v2[X] - b * v2[Y], fey, fex, h, true)) return false;
+  // bounding-box overlap per axis (FINDMINMAX)
+  for (int k = 0; k < 3; ++k) {
+    double mn = v0[k], mx = v0[k];
+    if (v1[k] < mn) mn = v1[k];
+    if (v1[k] > mx) mx = v1[k];
+    if (v2[k] < mn) mn = v2[k];
+    if (v2[k] > mx) mx = v2[k];
+    if (mn > h || mx < -h) return false;
+  }
+  // plane of the triangle: normal = e0 x e1
+  double nrm[3] = {e0[1] * e1[2] - e0[2] * e1[1], e0[2] * e1[0] - e0[0] * e1[2], e0[0] * e1[1] - e0[1] * e1[0]};
+  return plane_box_overlap(nrm, v0, h);
+}
+
+}  // namespace
+
+struct ora_octree {
+  std::vector<std::vector<Node>> d;
+  uint32_t levels = 0;
+  int state = 0;  // 0 empty, 1 SVO, 2 DAG, 3 SDAG
+  float bbox[6] = {0, 0, 0, 0, 0, 0};
+  double root_side = 0;
+  uint64_t n_voxels = 0, n_nodes = 0;
+  ora_stats st{};
+};
+
+namespace {
+
+// Octree::resizeSceneBbox / buildSVO prologue (src/symvox/octree.hpp:101-105,
+// src/symvox/geom_octree.cpp:176-184): float box, root side = largest float side.
+void set_box(ora_octree* o, const double bb[6]) {
+  for (int k = 0; k < 6; ++k) o->bbox[k] = float(bb[k]);
+  float s[3];
+  for (int k = 0; k < 3; ++k) s[k] = ((o->bbox[3 + k] - o->bbox[k]) * 0.5f) * 2.0f;
+  o->root_side = double(std::max(std::max(s[0], s[1]), s[2]));
+}
+
+// GeomOctree::cleanEmptyNodes (src/symvox/geom_octree.cpp:437-456)
+void clean_empty(ora_octree* o) {
+  for (int lev = int(o->levels) - 1; lev > 0; --lev) {
+    std::vector<char> empty(o->d[lev].size());
+    for (size_t i = 0; i < o->d[lev].size(); ++i) empty[i] = (o->d[lev][i].mask == 0);
+    for (auto& p : o->d[lev - 1]) {
+      for (int j = 0; j < 8; ++j) {
+        if (p.ch[j] != kNull && p.ch[j] < empty.size() && empty[p.ch[j]]) {
+          p.mask &= uint8_t(~(1u << j));
+          p.ch[j] = kNull;
+        }
+      }
+    }
+  }
+}
+
+// GeomOctree::buildSVO (src/symvox/geom_octree.cpp:171-280)
+void build_svo(ora_octree* o, const float* tris, uint64_t n_tris, const double bb[6], uint32_t levels) {
+  set_box(o, bb);
+  o->levels = levels;
+  o->d.assign(levels, std::vector<Node>());
+  o->d[0].push_back(Node());
+  o->n_nodes = 0;
+  o->n_voxels = 0;
+  double root_c[3];
+  for (int k = 0; k < 3; ++k) root_c[k] = (bb[k] + bb[3 + k]) * 0.5;
+  struct Item { uint32_t id; uint32_t lev; double c[3]; };
+  std::stack<Item> st;
+  for (uint64_t t = 0; t < n_tris; ++t) {
+    const float* tri = tris + 9 * t;
+    Item root{0, 0, {root_c[0], root_c[1], root_c[2]}};
+    st.push(root);
+    while (!st.empty()) {
+      Item it = st.top();
+      st.pop();
+      double k = o->root_side / double(1u << (it.lev + 2));  // getHalfSideD(lev+1)
+      for (int i = 7; i >= 0; --i) {
+        double cc[3] = {it.c[0] + ((i & 4) ? k : -k), it.c[1] + ((i & 2) ? k : -k), it.c[2] + ((i & 1) ? k : -k)};
+        if (!tri_box(cc, k, tri)) continue;
+        Node& node = o->d[it.lev][it.id];
+        node.mask |= uint8_t(1u << i);
+        if (node.ch[i] == kNull && it.lev < levels - 1) {
+          node.ch[i] = uint32_t(o->d[it.lev + 1].size());
+          o->d[it.lev + 1].emplace_back();
+          o->n_nodes++;
+        }
+        if (it.lev + 1 < levels) {
+          Item nx{o->d[it.lev][it.id].ch[i], it.lev + 1, {cc[0], cc[1], cc[2]}};
+          st.push(nx);
+        }
+      }
+    }
+  }
+  clean_empty(o);
+  for (const auto& n : o->d[levels - 1]) o->n_voxels += popc8(n.mask);
+  o->state = 1;
+  o->st.n_nodes_svo = o->n_nodes;
+  o->st.n_nodes_last_lev_svo = o->d[levels - 1].size();
+  o->st.n_total_voxels = o->n_voxels;
+}
+
+// GeomOctree::toDAG (src/symvox/geom_octree.cpp:462-548)
+int to_dag(ora_octree* o) {
+  if (o->state != 1 && o->state != 2) return -1;
+  o->n_nodes = 1;
+  std::map<Node, uint32_t, KeyLess> seen;
+  for (uint32_t lev = o->levels - 1; lev > 0; --lev) {
+    std::vector<Node>& L = o->d[lev];
+    std::vector<uint32_t> corr(L.size(), 0);
+    std::vector<Node> uniq;
+    seen.clear();
+    for (size_t i = 0; i < L.size(); ++i) {
+      const Node& n = L[i];
+      if (n.mask == 0) continue;
+      auto it = seen.find(n);
+      if (it != seen.end()) {
+        corr[i] = it->second;
+      } else {
+        uint32_t id = uint32_t(uniq.size());
+        seen.emplace(n, id);
+        corr[i] = id;
+        uniq.push_back(n);
+      }
+    }
+    L.swap(uniq);
+    o->n_nodes += L.size();
+    for (auto& p : o->d[lev - 1])
+      for (int j = 0; j < 8; ++j)
+        if (p.has_child(j)) p.ch[j] = corr[p.ch[j]];
+  }
+  o->state = 2;
+  o->st.n_nodes_dag = o->n_nodes;
+  return 0;
+}
+
+// GeomOctree::invertInvs (src/symvox/geom_octree.cpp:822-831)
+void invert_invs(const ora_octree* o, Node& n, uint32_t lev, bool x, bool y, bool z) {
+  for (int i = 0; i < 8; ++i) {
+    if (!n.has_ptr(i)) continue;
+    const Node& c = o->d[lev + 1][n.ch[i]];
+    if (x && (c.inv & 1u)) n.mir[0] &= uint8_t(~(1u << i));
+    if (y && (c.inv & 2u)) n.mir[1] &= uint8_t(~(1u << i));
+    if (z && (c.inv & 4u)) n.mir[2] &= uint8_t(~(1u << i));
+  }
+}
+
+// GeomOctree::toSDAG(false, false) (src/symvox/geom_octree.cpp:551-697)
+int to_sdag(ora_octree* o) {
+  if (o->state != 1 && o->state != 2) return -1;
+  struct Corr { uint8_t m; uint32_t id; };
+  std::map<Node, uint32_t, KeyLess> seen;
+  o->n_nodes = 0;
+  // lookup order: identity, X, Y, Z, XY, XZ, YZ, XYZ (geom_octree.cpp:630-658)
+  static const int axes[8] = {0, 4, 2, 1, 6, 5, 3, 7};
+  for (uint32_t lev = o->levels - 1; lev > 0; --lev) {
+    std::vector<Node>& L = o->d[lev];
+    std::vector<Corr> corr(L.size(), Corr{0, 0});
+    std::vector<Node> uniq;
+    seen.clear();
+    for (size_t i = 0; i < L.size(); ++i) {
+      Node n = L[i];
+      if (n.mask == 0) continue;
+      if (key_eq(n, mirror(n, true, false, false))) n.inv |= 1u;
+      if (key_eq(n, mirror(n, false, true, false))) n.inv |= 2u;
+      if (key_eq(n, mirror(n, false, false, true))) n.inv |= 4u;
+      Node var[8];
+      var[0] = n;
+      for (int k = 1; k < 8; ++k) {
+        int a = axes[k];
+        var[k] = mirror(n, a & 4, a & 2, a & 1);
+        if (lev < o->levels - 1) invert_invs(o, var[k], lev, a & 4, a & 2, a & 1);
+      }
+      bool found = false;
+      for (int k = 0; k < 8 && !found; ++k) {
+        auto it = seen.find(var[k]);
+        if (it != seen.end()) {
+          // bit0 = X, bit1 = Y, bit2 = Z
+          int a = axes[k];
+          corr[i] = Corr{uint8_t(((a & 4) ? 1 : 0) | ((a & 2) ? 2 : 0) | ((a & 1) ? 4 : 0)), it->second};
+          found = true;
+        }
+      }
+      if (!found) {
+        uint32_t id = uint32_t(uniq.size());
+        seen.emplace(n, id);
+        corr[i] = Corr{0, id};
+        uniq.push_back(n);
+      }
+    }
+    L.swap(uniq);
+    o->n_nodes += L.size();
+    for (auto& p : o->d[lev - 1]) {
+      for (int j = 0; j < 8; ++j) {
+        if (!p.has_ptr(j)) continue;
+        Corr cr = corr[p.ch[j]];
+        p.ch[j] = cr.id;
+        if (cr.m & 1) p.mir[0] |= uint8_t(1u << j);
+        if (cr.m & 2) p.mir[1] |= uint8_t(1u << j);
+        if (cr.m & 4) p.mir[2] |= uint8_t(1u << j);
+      }
+    }
+  }
+  o->st.n_nodes_sdag = o->n_nodes;
+  o->state = 3;
+  return 0;
+}
+
+// GeomOctree::initChildLevels (src/symvox/geom_octree_extension.cpp:21-30)
+void init_child_levels(ora_octree* o) {
+  for (uint32_t lev = 0; lev < o->levels; ++lev)
+    for (auto& n : o->d[lev])
+      for (int c = 0; c < 8; ++c) n.clev[c] = lev + 1;
+}
+
+// Truncated-subtree equality "A equals the top of B" with correspondences of
+// visited nodes (src/symvox/geom_octree_extension.cpp:238-290).  The map
+// assignment overwrites, so a node reached twice keeps its last visit.
+bool compare_subtrees(const ora_octree* o, uint32_t levA, uint32_t levB, const Node& a, const Node& b,
+                      std::vector<std::map<uint32_t, std::pair<uint32_t, uint32_t>>>& visited) {
+  if (a.mask != 0 && b.mask == 0) return false;
+  if (levA == o->levels - 1) return a.mask == b.mask;
+  for (int i = 0; i < 8; ++i) {
+    if (a.has_child(i) != b.has_child(i)) return false;
+    if (!a.has_child(i)) continue;
+    const Node& ca = o->d[levA + 1][a.ch[i]];
+    const Node& cb = o->d[levB + 1][b.ch[i]];
+    visited[levA + 1][a.ch[i]] = std::make_pair(levB + 1, b.ch[i]);
+    if (!compare_subtrees(o, levA + 1, levB + 1, ca, cb, visited)) return false;
+  }
+  return true;
+}
+
+inline uint64_t mix64(uint64_t x) {
+  x ^= x >> 31; x *= 0x7FB5D329728EA185ull;
+  x ^= x >> 27; x *= 0x81DADEF4BC2DD44Dull;
+  x ^= x >> 33;
+  return x;
+}
+
+// Depth-d structural fingerprint of every node at levels 1..levels-1: equal
+// for nodes whose top d levels of masks agree.  Used only to shortlist
+// candidates; equality is decided by compare_subtrees, exactly as the
+// reference's hash multimap is only a shortlist (geom_octree_extension.cpp:34-74,
+// 105-142, 1343-1348).
+void depth_hashes(const ora_octree* o, uint32_t depth, std::vector<std::vector<uint64_t>>& h) {
+  std::vector<std::vector<uint64_t>> prev(o->levels), cur(o->levels);
+  for (uint32_t l = 0; l < o->levels; ++l) {
+    prev[l].resize(o->d[l].size());
+    for (size_t i = 0; i < o->d[l].size(); ++i) prev[l][i] = o->d[l][i].mask;
+  }
+  for (uint32_t dd = 1; dd <= depth; ++dd) {
+    for (uint32_t l = 0; l < o->levels; ++l) {
+      cur[l].assign(o->d[l].size(), 0);
+      for (size_t i = 0; i < o->d[l].size(); ++i) {
+        const Node& n = o->d[l][i];
+        uint64_t x = mix64(0x1234567ull + n.mask);
+        for (int c = 0; c < 8; ++c) {
+          uint64_t v = 0x9E3779B97F4A7C15ull * uint64_t(c + 1);
+          if (n.has_ptr(c) && l + 1 < o->levels) v ^= prev[n.clev[c]][n.ch[c]];
+          x = mix64(x ^ v);
+        }
+        cur[l][i] = x;
+      }
+    }
+    prev.swap(cur);
+  }
+  h.swap(prev);
+}
+
+// GeomOctree::mergeAcrossAllLevels (src/symvox/geom_octree_extension.cpp:1192-1544)
+int merge_across_levels(ora_octree* o, uint64_t* n_missing) {
+  const uint32_t L = o->levels;
+  std::vector<std::multimap<uint64_t, uint32_t>> cand(L);
+  std::vector<std::vector<uint64_t>> h;
+  uint32_t cur_depth = L / 2;
+  auto rebuild = [&](uint32_t depth) {
+    depth_hashes(o, depth, h);
+    for (uint32_t l = 0; l < L; ++l) cand[l].clear();
+    // levels 1..L-1 only (buildMultiMap default range, geom_octree.hpp:146-148)
+    for (uint32_t l = 1; l < L; ++l)
+      for (uint32_t i = 0; i < o->d[l].size(); ++i) cand[l].insert(std::make_pair(h[l][i], i));
+  };
+  rebuild(cur_depth);
+
+  std::set<uint32_t> check, next;
+  for (uint32_t i = 0; i < o->d[1].size(); ++i) check.insert(i);
+  std::vector<std::map<uint32_t, std::pair<uint32_t, uint32_t>>> corr(L), visited(L);
+  for (uint32_t levA = 1; levA < L; ++levA) {
+    uint32_t max_depth = L - levA - 1;
+    if (max_depth < cur_depth) {
+      cur_depth = max_depth;
+      rebuild(cur_depth);
+    }
+    for (uint32_t idA : check) {
+      const Node& a = o->d[levA][idA];
+      uint64_t key = h[levA][idA];
+      bool found = false;
+      for (uint32_t levB = 0; levB < levA && !found; ++levB) {
+        auto rng = cand[levB].equal_range(key);
+        for (auto it = rng.first; it != rng.second; ++it) {
+          uint32_t j = it->second;
+          for (uint32_t l = 0; l < L; ++l) visited[l].clear();
+          if (compare_subtrees(o, levA, levB, a, o->d[levB][j], visited)) {
+            corr[levA][idA] = std::make_pair(levB, j);
+            for (uint32_t l = 0; l < L; ++l) corr[l].insert(visited[l].begin(), visited[l].end());
+            found = true;
+            break;
+          }
+        }
+      }
+      if (!found)
+        for (int i = 0; i < 8; ++i)
+          if (a.has_child(i)) next.insert(a.ch[i]);
+    }
+    check.clear();
+    check.swap(next);
+  }
+
+  uint64_t removed_total = 0, missing = 0;
+  for (uint32_t l = 0; l < L; ++l) removed_total += corr[l].size();
+  o->n_nodes = 1;
+  for (uint32_t lev = L - 1; lev > 0; --lev) {
+    std::vector<Node>& Lv = o->d[lev];
+    std::vector<uint32_t> newidx(Lv.size(), 0xFFFFFFFFu);
+    std::vector<Node> keep;
+    for (uint32_t i = 0; i < Lv.size(); ++i) {
+      if (corr[lev].count(i) == 0) { newidx[i] = uint32_t(keep.size()); keep.push_back(Lv[i]); }
+    }
+    Lv.swap(keep);
+    o->n_nodes += Lv.size();
+    for (auto& p : o->d[lev - 1]) {
+      for (int j = 0; j < 8; ++j) {
+        if (!p.has_child(j)) continue;
+        auto it = corr[lev].find(p.ch[j]);
+        if (it != corr[lev].end()) { p.clev[j] = it->second.first; p.ch[j] = it->second.second; }
+        else p.ch[j] = newidx[p.ch[j]];
+      }
+    }
+    for (uint32_t low = L - 2; low >= lev; --low) {
+      for (auto& p : o->d[low]) {
+        for (int j = 0; j < 8; ++j) {
+          if (p.has_child(j) && p.clev[j] == lev) {
+            if (newidx[p.ch[j]] == 0xFFFFFFFFu) ++missing;
+            p.ch[j] = newidx[p.ch[j]];
+          }
+        }
+      }
+      if (low == 0) break;
+    }
+  }
+  o->st.n_nodes_dag = o->n_nodes;
+  o->st.n_cross_level_merged = removed_total;
+  if (n_missing) *n_missing = missing;
+  return 0;
+}
+
+// GeomOctree::buildDAG (src/symvox/geom_octree.cpp:289-435): a top SVO of
+// step_level+1 levels, one sub-SVO + toDAG per top-level voxel (OpenMP,
+// dynamic schedule), joined level by level with pointer offsets, then one
+// toDAG over the whole tree.
+void build_dag_chunked(ora_octree* o, const float* tris, uint64_t n_tris, const double bb[6], uint32_t levels,
+                       uint32_t step_level, int n_threads) {
+  const uint32_t top = step_level + 1;
+  build_svo(o, tris, n_tris, bb, top);
+  // centres of the top SVO's leaf nodes in creation order
+  // (buildSVO's leavesCenters, geom_octree.cpp:245-246)
+  std::vector<std::array<double, 3>> centers(o->d[top - 1].size());
+  {
+    // recompute by walking the top SVO from the root
+    double rc[3];
+    for (int k = 0; k < 3; ++k) rc[k] = (bb[k] + bb[3 + k]) * 0.5;
+    struct W { uint32_t lev, id; double c[3]; };
+    std::vector<W> stack{W{0, 0, {rc[0], rc[1], rc[2]}}};
+    if (top == 1) centers[0] = {rc[0], rc[1], rc[2]};
+    while (!stack.empty()) {
+      W w = stack.back();
+      stack.pop_back();
+      if (w.lev + 1 >= top) continue;
+      double k = o->root_side / double(1u << (w.lev + 2));
+      const Node& n = o->d[w.lev][w.id];
+      for (int i = 0; i < 8; ++i) {
+        if (n.ch[i] == kNull) continue;
+        double cc[3] = {w.c[0] + ((i & 4) ? k : -k), w.c[1] + ((i & 2) ? k : -k), w.c[2] + ((i & 1) ? k : -k)};
+        if (w.lev + 1 == top - 1) centers[n.ch[i]] = {cc[0], cc[1], cc[2]};
+        stack.push_back(W{w.lev + 1, n.ch[i], {cc[0], cc[1], cc[2]}});
+      }
+    }
+  }
+  const double lhs = o->root_side / double(1u << top);  // getHalfSideD(stepLevels-1)
+  const size_t n_top = o->d[top - 1].size();
+  std::vector<ora_octree*> sub(n_top * 8, nullptr);
+  uint64_t svo_nodes = o->n_nodes, svo_last = 0, vox = o->n_voxels;
+#pragma omp parallel for schedule(dynamic, 2) num_threads(n_threads > 0 ? n_threads : omp_get_max_threads()) reduction(+ : svo_nodes, svo_last, vox)
+  for (long i = 0; i < long(n_top); ++i) {
+    for (int j = 7; j >= 0; --j) {
+      if (!((o->d[top - 1][i].mask >> j) & 1u)) continue;
+      const auto& c = centers[i];
+      double q[3] = {c[0] + ((j & 4) ? lhs : -lhs), c[1] + ((j & 2) ? lhs : -lhs), c[2] + ((j & 1) ? lhs : -lhs)};
+      double sb[6];
+      for (int k = 0; k < 3; ++k) { sb[k] = std::min(c[k], q[k]); sb[3 + k] = std::max(c[k], q[k]); }
+      ora_octree* so = new ora_octree();
+      build_svo(so, tris, n_tris, sb, levels - top);
+      svo_nodes += so->n_nodes;
+      svo_last += so->d[so->levels - 1].size();
+      vox += so->n_voxels - 1;
+      to_dag(so);
+      sub[size_t(i) * 8 + j] = so;
+    }
+  }
+  o->st.n_nodes_svo = svo_nodes;
+  o->st.n_nodes_last_lev_svo = svo_last;
+  o->st.n_total_voxels = vox;
+  o->n_voxels = vox;
+  o->d.resize(levels);
+  o->levels = levels;
+  for (size_t i = 0; i < n_top; ++i) {
+    for (int j = 7; j >= 0; --j) {
+      if (!((o->d[top - 1][i].mask >> j) & 1u)) continue;
+      ora_octree* so = sub[i * 8 + j];
+      o->d[top - 1][i].ch[j] = uint32_t(o->d[top].size());
+      for (uint32_t k = top; k < levels; ++k) {
+        if (k < levels - 1) {
+          uint32_t off = uint32_t(o->d[k + 1].size());
+          for (auto& n : so->d[k - top])
+            for (int c = 0; c < 8; ++c)
+              if (n.has_ptr(c)) n.ch[c] += off;
+        }
+        o->d[k].insert(o->d[k].end(), so->d[k - top].begin(), so->d[k - top].end());
+      }
+      delete so;
+    }
+  }
+  o->state = 1;
+  to_dag(o);
+}
+
+}  // namespace
+
+extern "C" {
+
+ora_octree* ora_create(void) { return new ora_octree(); }
+void ora_destroy(ora_octree* o) { delete o; }
+ora_octree* ora_clone(const ora_octree* o) { return new ora_octree(*o); }
+
+int ora_build_svo(ora_octree* o, const float* tris, uint64_t n_tris, const double bbox[6], uint32_t levels) {
+  if (!o || levels < 1 || levels > 31) return -1;
+  build_svo(o, tris, n_tris, bbox, levels);
+  o->st.levels = levels;
+  return 0;
+}
+
+int ora_build_dag_chunked(ora_octree* o, const float* tris, uint64_t n_tris, const double bbox[6], uint32_t levels,
+                          uint32_t step_level, int n_threads) {
+  if (!o || step_level == 0 || step_level + 1 >= levels) return -1;
+  build_dag_chunked(o, tris, n_tris, bbox, levels, step_level, n_threads);
+  o->st.levels = levels;
+  return 0;
+}
+
+int ora_to_dag(ora_octree* o) { return o ? to_dag(o) : -1; }
+int ora_to_sdag(ora_octree* o) { return o ? to_sdag(o) : -1; }
+int ora_init_child_levels(ora_octree* o) {
+  if (!o) return -1;
+  init_child_levels(o);
+  return 0;
+}
+int ora_merge_across_levels(ora_octree* o) {
+  if (!o || o->state != 2) return -1;
+  uint64_t miss = 0;
+  int r = merge_across_levels(o, &miss);
+  o->st.n_missing_correspondences = miss;
+  return r;
+}
+
+uint64_t ora_level_count(const ora_octree* o, uint32_t level) {
+  return (o && level < o->d.size()) ? o->d[level].size() : 0;
+}
+
+int ora_get_level(const ora_octree* o, uint32_t level, uint8_t* rec) {
+  if (!o || level >= o->d.size()) return -1;
+  for (size_t i = 0; i < o->d[level].size(); ++i) {
+    const Node& n = o->d[level][i];
+    uint8_t* r = rec + 48 * i;
+    uint32_t hdr = uint32_t(n.mask) | (uint32_t(n.mir[0]) << 8) | (uint32_t(n.mir[1]) << 16) | (uint32_t(n.mir[2]) << 24);
+    std::memcpy(r, &hdr, 4);
+    std::memcpy(r + 4, n.ch, 32);
+    for (int c = 0; c < 8; ++c) r[36 + c] = uint8_t(n.clev[c] & 0xFFu);
+    r[44] = n.inv;
+    r[45] = r[46] = r[47] = 0;
+  }
+  return 0;
+}
+
+int ora_get_stats(const ora_octree* o, ora_stats* s) {
+  if (!o || !s) return -1;
+  *s = o->st;
+  s->n_nodes = o->n_nodes;
+  s->levels = o->levels;
+  s->state = uint32_t(o->state);
+  return 0;
+}
+
+int ora_tri_box(const double center[3], double half_side, const float tri[9]) {
+  return tri_box(center, half_side, tri) ? 1 : 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,20 @@
+// Host-side helpers of the SVDAG build: seeded synthetic scenes and the OBJ
+// writer.  These are not part of the GPU boundary (include/svdag_gpu.h); they
+// feed it.
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+uint64_t svdag_synth_icosphere_count(uint32_t subdiv);
+int svdag_synth_icosphere(uint32_t subdiv, double radius, double amp, uint64_t seed, float* out_tris);
+uint64_t svdag_synth_terrain_count(uint32_t grid);
+int svdag_synth_terrain(uint32_t grid, uint32_t octaves, double height, uint64_t seed, float* out_tris);
+int svdag_synth_boxes(const float* lo, const float* hi, uint64_t n_boxes, float* out_tris);
+int svdag_write_obj(const char* path, const float* tris, uint64_t n_tris, int pin_unit_cube);
+
+#ifdef __cplusplus
+}
+#endif
