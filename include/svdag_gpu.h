@@ -1,0 +1,115 @@
+/*
+ * svdag_gpu.h -- C ABI of the GB300 (sm_103a) SVDAG construction path.
+ *
+ * Drop-in replacement for the compute of SymVox's GeomOctree build path:
+ * voxelization into an SVO, bottom-up reduction to an SVDAG, the
+ * symmetry-aware SSVDAG reduction and the cross-level CSVDAG merge.  Results
+ * (node pools per level, counts, statistics) are bit-identical to the
+ * reference's; only the place the work runs changes.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (SVDAG_OK == 0).  On failure
+ *     svdag_last_error() gives a one-line reason.  The reference prints and
+ *     returns on a wrong octree state (src/symvox/geom_octree.cpp:464-469,
+ *     553-563); here that case is SVDAG_ERR_INVALID_STATE.
+ *   - A context owns one CUDA stream and all device memory of one octree.
+ *     It is not thread-safe: use one context per host thread, as the
+ *     reference uses one GeomOctree per OpenMP thread
+ *     (src/symvox/geom_octree.cpp:339).
+ *   - Node records use the reference's node fields in fixed-width form:
+ *       hdr       = childrenBitmask | mirX<<8 | mirY<<16 | mirZ<<24
+ *       children  = 8 x u32 per node, 0xFFFFFFFE for no child
+ *                   (Octree::nullNode, src/symvox/octree.cpp:22)
+ *       childLevels = 8 x u8 per node (low byte of the reference's value,
+ *                   0xFF when never initialised)
+ *       invariant = u8 invariantBitmask (bit0 X, bit1 Y, bit2 Z)
+ *     Child index c = 4x + 2y + z (src/symvox/octree.hpp:33-42).
+ */
+#ifndef SVDAG_GPU_H
+#define SVDAG_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum svdag_status {
+  SVDAG_OK = 0,
+  SVDAG_ERR_INVALID_ARG = 1,
+  SVDAG_ERR_INVALID_STATE = 2,
+  SVDAG_ERR_CUDA = 3,
+  SVDAG_ERR_OOM = 4,
+  SVDAG_ERR_OVERFLOW = 5,
+  SVDAG_ERR_TIMEOUT = 6,
+  SVDAG_ERR_NO_DEVICE = 7
+};
+
+/* GeomOctree::State (src/symvox/geom_octree.hpp:36-41) */
+enum svdag_state { SVDAG_S_EMPTY = 0, SVDAG_S_SVO = 1, SVDAG_S_DAG = 2, SVDAG_S_SDAG = 3 };
+
+typedef struct svdag_ctx svdag_ctx;
+
+/* GeomOctree::Stats subset (src/symvox/geom_octree.hpp:43-56) plus device
+ * times of each phase measured with CUDA events on the context stream. */
+typedef struct svdag_stats {
+  uint64_t n_total_voxels;
+  uint64_t n_nodes_svo;
+  uint64_t n_nodes_last_lev_svo;
+  uint64_t n_nodes_dag;
+  uint64_t n_nodes_sdag;
+  uint64_t n_nodes;                 /* current node count (reference _nNodes) */
+  uint64_t n_cross_level_merged;
+  uint64_t n_missing_correspondences;
+  uint32_t levels;
+  uint32_t state;                   /* enum svdag_state */
+  double svo_ms, dag_ms, sdag_ms, csv_ms;
+  uint64_t gpu_launches;            /* kernels launched by this context */
+} svdag_stats;
+
+/* Lifetime.  `stream` is a cudaStream_t to run on, or NULL for a new one. */
+int svdag_create(svdag_ctx** out, int device, void* stream);
+int svdag_destroy(svdag_ctx* ctx);
+/* Device-side deep copy (same device and stream): lets one DAG feed both the
+ * SSVDAG and the CSVDAG reductions, as GeomOctree's copy constructor does
+ * (src/symvox/geom_octree.cpp:40-45). */
+int svdag_clone(const svdag_ctx* src, svdag_ctx** out);
+const char* svdag_last_error(const svdag_ctx* ctx);
+const char* svdag_status_string(int status);
+int svdag_synchronize(svdag_ctx* ctx);
+
+/* Scene input: triangles as float[9] each (v0 v1 v2, xyz), the layout of
+ * Scene::getTrianglePtr (src/symvox/scene.hpp:78).  upload copies from host
+ * memory; set_device borrows a device buffer that must outlive the build. */
+int svdag_upload_triangles(svdag_ctx* ctx, const float* host_tris, uint64_t n_tris);
+int svdag_set_device_triangles(svdag_ctx* ctx, const float* device_tris, uint64_t n_tris);
+
+/* GeomOctree::buildSVO(levels, bbox) (src/symvox/geom_octree.cpp:171-280):
+ * bbox = {minx, miny, minz, maxx, maxy, maxz} in double, 1 <= levels <= 21. */
+int svdag_voxelize(svdag_ctx* ctx, uint32_t levels, const double bbox[6]);
+/* GeomOctree::toDAG (src/symvox/geom_octree.cpp:462-548) */
+int svdag_reduce_dag(svdag_ctx* ctx);
+/* GeomOctree::initChildLevels (src/symvox/geom_octree_extension.cpp:21-30) */
+int svdag_init_child_levels(svdag_ctx* ctx);
+/* GeomOctree::toSDAG(false, false) (src/symvox/geom_octree.cpp:551-697) */
+int svdag_reduce_sdag(svdag_ctx* ctx);
+/* GeomOctree::mergeAcrossAllLevels (src/symvox/geom_octree_extension.cpp:1192-1544) */
+int svdag_cross_level_merge(svdag_ctx* ctx);
+
+/* Results.  Host buffers sized by svdag_level_count; any pointer may be NULL
+ * to skip that field.  children/child_levels take 8 entries per node. */
+int svdag_level_count(const svdag_ctx* ctx, uint32_t level, uint64_t* count);
+int svdag_download_level(svdag_ctx* ctx, uint32_t level, uint32_t* hdr, uint32_t* children,
+                         uint8_t* child_levels, uint8_t* invariant);
+int svdag_get_stats(const svdag_ctx* ctx, svdag_stats* out);
+/* Device pointers of one level's arrays (valid until the next build call on
+ * the context); children is NULL on the leaf level. */
+int svdag_level_device_ptrs(const svdag_ctx* ctx, uint32_t level, const uint32_t** hdr,
+                            const uint32_t** children, const uint8_t** child_levels,
+                            const uint8_t** invariant);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SVDAG_GPU_H */

@@ -1,0 +1,152 @@
+"""ctypes wrapper of the restated CPU oracle (oracle/build/liboracle.so) and
+readers for the reference dump format.  TEST INFRASTRUCTURE: imported only by
+tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, as the
+checker; the product never uses it.
+"""
+import ctypes
+import os
+import struct
+
+import numpy as np
+
+ORACLE_DIR = os.path.dirname(os.path.abspath(__file__))
+REC = np.dtype([("hdr", "<u4"), ("ch", "<u4", (8,)), ("cl", "u1", (8,)), ("inv", "u1"), ("pad", "u1", (3,))])
+
+
+class _OraStats(ctypes.Structure):
+    _fields_ = [
+        ("n_total_voxels", ctypes.c_uint64),
+        ("n_nodes_svo", ctypes.c_uint64),
+        ("n_nodes_last_lev_svo", ctypes.c_uint64),
+        ("n_nodes_dag", ctypes.c_uint64),
+        ("n_nodes_sdag", ctypes.c_uint64),
+        ("n_nodes", ctypes.c_uint64),
+        ("n_cross_level_merged", ctypes.c_uint64),
+        ("n_missing_correspondences", ctypes.c_uint64),
+        ("levels", ctypes.c_uint32),
+        ("state", ctypes.c_uint32),
+    ]
+
+
+_VP, _U32, _U64, _I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+_SIGS = {
+    "ora_create": (_VP, []),
+    "ora_destroy": (None, [_VP]),
+    "ora_clone": (_VP, [_VP]),
+    "ora_build_svo": (_I, [_VP, _VP, _U64, _VP, _U32]),
+    "ora_build_dag_chunked": (_I, [_VP, _VP, _U64, _VP, _U32, _U32, _I]),
+    "ora_to_dag": (_I, [_VP]),
+    "ora_to_sdag": (_I, [_VP]),
+    "ora_init_child_levels": (_I, [_VP]),
+    "ora_merge_across_levels": (_I, [_VP]),
+    "ora_level_count": (_U64, [_VP, _U32]),
+    "ora_get_level": (_I, [_VP, _U32, _VP]),
+    "ora_get_stats": (_I, [_VP, ctypes.POINTER(_OraStats)]),
+    "ora_tri_box": (_I, [_VP, ctypes.c_double, _VP]),
+}
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        p = os.path.join(ORACLE_DIR, "build", "liboracle.so")
+        if not os.path.exists(p):
+            raise RuntimeError("oracle/build/liboracle.so not built")
+        lib = ctypes.CDLL(p)
+        for k, (r, a) in _SIGS.items():
+            f = getattr(lib, k)
+            f.restype = r
+            f.argtypes = a
+        _lib = lib
+    return _lib
+
+
+class OracleOctree:
+    def __init__(self, _h=None):
+        self.L = load()
+        self.h = _h if _h is not None else self.L.ora_create()
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.L.ora_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def clone(self):
+        return OracleOctree(self.L.ora_clone(self.h))
+
+    def buildSVO(self, tris, levels, bbox=(0, 0, 0, 1, 1, 1)):
+        tris = np.ascontiguousarray(tris, np.float32)
+        bb = np.array(bbox, np.float64)
+        assert self.L.ora_build_svo(self.h, tris.ctypes.data, tris.shape[0], bb.ctypes.data, levels) == 0
+
+    def buildDAG(self, tris, levels, step_level, bbox=(0, 0, 0, 1, 1, 1), threads=0):
+        tris = np.ascontiguousarray(tris, np.float32)
+        bb = np.array(bbox, np.float64)
+        assert self.L.ora_build_dag_chunked(self.h, tris.ctypes.data, tris.shape[0], bb.ctypes.data, levels,
+                                            step_level, threads) == 0
+
+    def toDAG(self):
+        assert self.L.ora_to_dag(self.h) == 0
+
+    def toSDAG(self):
+        assert self.L.ora_to_sdag(self.h) == 0
+
+    def initChildLevels(self):
+        assert self.L.ora_init_child_levels(self.h) == 0
+
+    def mergeAcrossAllLevels(self):
+        assert self.L.ora_merge_across_levels(self.h) == 0
+
+    def stats(self):
+        s = _OraStats()
+        self.L.ora_get_stats(self.h, ctypes.byref(s))
+        return {k: getattr(s, k) for k, _ in _OraStats._fields_}
+
+    def level(self, l):
+        n = self.L.ora_level_count(self.h, l)
+        a = np.zeros(n, REC)
+        if n:
+            self.L.ora_get_level(self.h, l, a.ctypes.data)
+        return a
+
+    def pool(self):
+        return [self.level(l) for l in range(self.stats()["levels"])]
+
+
+def tri_box(center, half, tri):
+    c = np.array(center, np.float64)
+    t = np.ascontiguousarray(tri, np.float32)
+    return bool(load().ora_tri_box(c.ctypes.data, half, t.ctypes.data))
+
+
+def read_pool(path):
+    """Reads a pool file written by ref_dump (layout in oracle/ref_dump.cpp)."""
+    with open(path, "rb") as f:
+        b = f.read()
+    assert b[:4] == b"SVDP"
+    ver, levels, state = struct.unpack_from("<III", b, 4)
+    nvox, nn = struct.unpack_from("<QQ", b, 16)
+    off = 32
+    out = []
+    for _ in range(levels):
+        (n,) = struct.unpack_from("<Q", b, off)
+        off += 8
+        out.append(np.frombuffer(b, REC, n, off).copy())
+        off += 48 * n
+    return {"levels": levels, "state": state, "nvoxels": nvox, "nnodes": nn, "pool": out}
+
+
+def pool_digest(pool):
+    """SHA-256 over the concatenated level records (hdr, children, childLevels,
+    invariant) -- the form the golden fixtures store."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for lev in pool:
+        h.update(np.uint64(len(lev)).tobytes())
+        h.update(np.ascontiguousarray(lev).tobytes())
+    return h.hexdigest()

@@ -1,0 +1,255 @@
+// C ABI of the SVDAG construction path (include/svdag_gpu.h).
+#include <cstring>
+#include <new>
+
+#include "ctx.cuh"
+
+using svdag::Ctx;
+using svdag::Error;
+
+namespace {
+
+int fail(svdag_ctx* h, int code, const std::string& msg) {
+  if (h) h->c.last_error = msg;
+  return code;
+}
+
+template <class F>
+int guarded(svdag_ctx* h, F&& f) {
+  if (!h) return SVDAG_ERR_INVALID_ARG;
+  try {
+    SVDAG_CUDA(cudaSetDevice(h->c.device));
+    f(h->c);
+    h->c.last_error.clear();
+    return SVDAG_OK;
+  } catch (const Error& e) {
+    return fail(h, e.code, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(h, SVDAG_ERR_OOM, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(h, SVDAG_ERR_CUDA, e.what());
+  }
+}
+
+// Runs one build phase between two events on the context stream and returns
+// its device time in milliseconds.
+template <class F>
+double timed(Ctx& c, F&& f) {
+  SVDAG_CUDA(cudaEventRecord(c.ev0, c.stream));
+  f();
+  SVDAG_CUDA(cudaEventRecord(c.ev1, c.stream));
+  SVDAG_CUDA(cudaEventSynchronize(c.ev1));
+  float ms = 0.f;
+  SVDAG_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+  return double(ms);
+}
+
+void copy_level(const Ctx& src, svdag::Level& dst, const svdag::Level& s, cudaStream_t st) {
+  dst.n = s.n;
+  auto cp = [&](auto& d, const auto& v) {
+    if (!v.get()) return;
+    d.alloc(v.n, st);
+    SVDAG_CUDA(cudaMemcpyAsync(d.get(), v.get(), v.bytes(), cudaMemcpyDeviceToDevice, st));
+  };
+  cp(dst.hdr, s.hdr);
+  cp(dst.ch, s.ch);
+  cp(dst.inv, s.inv);
+  cp(dst.clev, s.clev);
+  (void)src;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* svdag_status_string(int s) {
+  switch (s) {
+    case SVDAG_OK: return "ok";
+    case SVDAG_ERR_INVALID_ARG: return "invalid argument";
+    case SVDAG_ERR_INVALID_STATE: return "invalid octree state";
+    case SVDAG_ERR_CUDA: return "CUDA error";
+    case SVDAG_ERR_OOM: return "out of device memory";
+    case SVDAG_ERR_OVERFLOW: return "capacity overflow";
+    case SVDAG_ERR_TIMEOUT: return "bounded wait expired";
+    case SVDAG_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char* svdag_last_error(const svdag_ctx* h) { return h ? h->c.last_error.c_str() : "null context"; }
+
+int svdag_create(svdag_ctx** out, int device, void* stream) {
+  if (!out) return SVDAG_ERR_INVALID_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return SVDAG_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return SVDAG_ERR_INVALID_ARG;
+  svdag_ctx* h = new (std::nothrow) svdag_ctx();
+  if (!h) return SVDAG_ERR_OOM;
+  Ctx& c = h->c;
+  c.device = device;
+  try {
+    SVDAG_CUDA(cudaSetDevice(device));
+    if (stream) {
+      c.stream = static_cast<cudaStream_t>(stream);
+    } else {
+      SVDAG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+      c.own_stream = true;
+    }
+    int sms = 0;
+    SVDAG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    c.ex.stream = c.stream;
+    c.ex.sm_count = sms;
+    c.ex.launches = &c.launches;
+    SVDAG_CUDA(cudaEventCreate(&c.ev0));
+    SVDAG_CUDA(cudaEventCreate(&c.ev1));
+  } catch (const Error& e) {
+    delete h;
+    return e.code;
+  }
+  *out = h;
+  return SVDAG_OK;
+}
+
+int svdag_destroy(svdag_ctx* h) {
+  if (!h) return SVDAG_ERR_INVALID_ARG;
+  Ctx& c = h->c;
+  cudaSetDevice(c.device);
+  c.lev.clear();
+  c.owned_tris.release();
+  cudaStreamSynchronize(c.stream);
+  if (c.ev0) cudaEventDestroy(c.ev0);
+  if (c.ev1) cudaEventDestroy(c.ev1);
+  if (c.own_stream) cudaStreamDestroy(c.stream);
+  delete h;
+  return SVDAG_OK;
+}
+
+int svdag_clone(const svdag_ctx* src, svdag_ctx** out) {
+  if (!src || !out) return SVDAG_ERR_INVALID_ARG;
+  const Ctx& s = src->c;
+  int r = svdag_create(out, s.device, s.own_stream ? nullptr : s.stream);
+  if (r != SVDAG_OK) return r;
+  return guarded(*out, [&](Ctx& c) {
+    c.tris = s.owned_tris.get() ? nullptr : s.tris;
+    c.n_tris = s.owned_tris.get() ? 0 : s.n_tris;
+    // wait for the source stream's work before copying on the new stream
+    SVDAG_CUDA(cudaStreamSynchronize(s.stream));
+    c.levels = s.levels;
+    c.state = s.state;
+    c.child_levels_init = s.child_levels_init;
+    std::memcpy(c.bbox, s.bbox, sizeof(c.bbox));
+    c.root_side = s.root_side;
+    c.st = s.st;
+    c.lev.resize(s.lev.size());
+    for (size_t l = 0; l < s.lev.size(); ++l) copy_level(s, c.lev[l], s.lev[l], c.stream);
+    SVDAG_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int svdag_synchronize(svdag_ctx* h) {
+  return guarded(h, [&](Ctx& c) { SVDAG_CUDA(cudaStreamSynchronize(c.stream)); });
+}
+
+int svdag_upload_triangles(svdag_ctx* h, const float* host_tris, uint64_t n_tris) {
+  if (!host_tris && n_tris) return fail(h, SVDAG_ERR_INVALID_ARG, "upload: null triangle pointer");
+  return guarded(h, [&](Ctx& c) {
+    c.owned_tris.alloc(9 * (n_tris ? n_tris : 1), c.stream);
+    if (n_tris)
+      SVDAG_CUDA(cudaMemcpyAsync(c.owned_tris.get(), host_tris, 36 * n_tris, cudaMemcpyHostToDevice, c.stream));
+    c.tris = c.owned_tris.get();
+    c.n_tris = n_tris;
+  });
+}
+
+int svdag_set_device_triangles(svdag_ctx* h, const float* device_tris, uint64_t n_tris) {
+  if (!device_tris && n_tris) return fail(h, SVDAG_ERR_INVALID_ARG, "set_device_triangles: null pointer");
+  return guarded(h, [&](Ctx& c) {
+    c.owned_tris.release();
+    c.tris = device_tris;
+    c.n_tris = n_tris;
+  });
+}
+
+int svdag_voxelize(svdag_ctx* h, uint32_t levels, const double bbox[6]) {
+  if (!bbox) return fail(h, SVDAG_ERR_INVALID_ARG, "voxelize: null bbox");
+  return guarded(h, [&](Ctx& c) { c.st.svo_ms = timed(c, [&] { svdag::phase_voxelize(c, levels, bbox); }); });
+}
+
+int svdag_reduce_dag(svdag_ctx* h) {
+  return guarded(h, [&](Ctx& c) { c.st.dag_ms = timed(c, [&] { svdag::phase_reduce_dag(c); }); });
+}
+
+int svdag_init_child_levels(svdag_ctx* h) {
+  return guarded(h, [&](Ctx& c) {
+    if (c.state == SVDAG_S_EMPTY) throw Error(SVDAG_ERR_INVALID_STATE, "initChildLevels: empty octree");
+    for (auto& L : c.lev) L.clev.release();
+    c.child_levels_init = true;
+  });
+}
+
+int svdag_reduce_sdag(svdag_ctx* h) {
+  return guarded(h, [&](Ctx& c) { c.st.sdag_ms = timed(c, [&] { svdag::phase_reduce_sdag(c); }); });
+}
+
+int svdag_cross_level_merge(svdag_ctx* h) {
+  return guarded(h, [&](Ctx& c) { c.st.csv_ms = timed(c, [&] { svdag::phase_cross_level_merge(c); }); });
+}
+
+int svdag_level_count(const svdag_ctx* h, uint32_t level, uint64_t* count) {
+  if (!h || !count) return SVDAG_ERR_INVALID_ARG;
+  if (level >= h->c.lev.size()) return SVDAG_ERR_INVALID_ARG;
+  *count = h->c.lev[level].n;
+  return SVDAG_OK;
+}
+
+int svdag_download_level(svdag_ctx* h, uint32_t level, uint32_t* hdr, uint32_t* children, uint8_t* child_levels,
+                         uint8_t* invariant) {
+  return guarded(h, [&](Ctx& c) {
+    if (level >= c.lev.size()) throw Error(SVDAG_ERR_INVALID_ARG, "download: level out of range");
+    const svdag::Level& L = c.lev[level];
+    const uint64_t n = L.n;
+    if (hdr && n) SVDAG_CUDA(cudaMemcpyAsync(hdr, L.hdr.get(), 4 * n, cudaMemcpyDeviceToHost, c.stream));
+    if (children && n) {
+      if (L.ch.get())
+        SVDAG_CUDA(cudaMemcpyAsync(children, L.ch.get(), 32 * n, cudaMemcpyDeviceToHost, c.stream));
+      else
+        for (uint64_t i = 0; i < 8 * n; ++i) children[i] = svdag::kNull;
+    }
+    if (invariant && n) {
+      if (L.inv.get())
+        SVDAG_CUDA(cudaMemcpyAsync(invariant, L.inv.get(), n, cudaMemcpyDeviceToHost, c.stream));
+      else
+        std::memset(invariant, 0, n);
+    }
+    if (child_levels && n) {
+      if (L.clev.get())
+        SVDAG_CUDA(cudaMemcpyAsync(child_levels, L.clev.get(), 8 * n, cudaMemcpyDeviceToHost, c.stream));
+      else
+        std::memset(child_levels, c.child_levels_init ? int(level + 1) : 0xFF, 8 * n);
+    }
+    SVDAG_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int svdag_get_stats(const svdag_ctx* h, svdag_stats* out) {
+  if (!h || !out) return SVDAG_ERR_INVALID_ARG;
+  *out = h->c.st;
+  out->levels = h->c.levels;
+  out->state = uint32_t(h->c.state);
+  out->gpu_launches = h->c.launches;
+  return SVDAG_OK;
+}
+
+int svdag_level_device_ptrs(const svdag_ctx* h, uint32_t level, const uint32_t** hdr, const uint32_t** children,
+                            const uint8_t** child_levels, const uint8_t** invariant) {
+  if (!h || level >= h->c.lev.size()) return SVDAG_ERR_INVALID_ARG;
+  const svdag::Level& L = h->c.lev[level];
+  if (hdr) *hdr = L.hdr.get();
+  if (children) *children = L.ch.get();
+  if (child_levels) *child_levels = L.clev.get();
+  if (invariant) *invariant = L.inv.get();
+  return SVDAG_OK;
+}
+
+}  // extern "C"

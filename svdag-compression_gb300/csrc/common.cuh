@@ -1,0 +1,277 @@
+// Shared device utilities of the SVDAG build: error handling, stream-ordered
+// device buffers, launch accounting, node-key hashing and a device-wide
+// exclusive scan.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "svdag_gpu.h"
+
+namespace svdag {
+
+constexpr uint32_t kNull = 0xFFFFFFFEu;   // Octree::nullNode (src/symvox/octree.cpp:22)
+constexpr uint32_t kNone = 0xFFFFFFFFu;   // "no entry" in internal tables
+constexpr uint64_t kEmpty64 = ~0ull;      // empty hash-table slot
+
+struct Error : public std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define SVDAG_CUDA(expr)                                                                   \
+  do {                                                                                     \
+    cudaError_t e__ = (expr);                                                              \
+    if (e__ != cudaSuccess) {                                                              \
+      throw ::svdag::Error(e__ == cudaErrorMemoryAllocation ? SVDAG_ERR_OOM : SVDAG_ERR_CUDA, \
+                           std::string(#expr) + ": " + cudaGetErrorString(e__));          \
+    }                                                                                      \
+  } while (0)
+
+// Per-context execution environment handed to every launch helper.
+struct Exec {
+  cudaStream_t stream = nullptr;
+  int sm_count = 152;
+  uint64_t* launches = nullptr;  // incremented once per kernel launch
+};
+
+// Grid for a grid-stride loop over n items.
+inline unsigned grid_for(const Exec& ex, uint64_t n, unsigned threads, unsigned per_sm = 16) {
+  uint64_t want = (n + threads - 1) / threads;
+  uint64_t cap = uint64_t(ex.sm_count) * per_sm;
+  if (want < 1) want = 1;
+  return unsigned(want < cap ? want : cap);
+}
+
+#define SVDAG_LAUNCH(ex, kernel, grid, block, smem, ...)                 \
+  do {                                                                   \
+    kernel<<<(grid), (block), (smem), (ex).stream>>>(__VA_ARGS__);       \
+    if ((ex).launches) ++*(ex).launches;                                 \
+    SVDAG_CUDA(cudaPeekAtLastError());                                   \
+  } while (0)
+
+// Stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync).
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  uint64_t n = 0;
+  cudaStream_t s = nullptr;
+  DBuf() = default;
+  DBuf(uint64_t count, cudaStream_t st) { alloc(count, st); }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; s = o.s; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void alloc(uint64_t count, cudaStream_t st) {
+    release();
+    s = st;
+    n = count;
+    if (count) SVDAG_CUDA(cudaMallocAsync((void**)&p, sizeof(T) * (count ? count : 1), st));
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    n = 0;
+  }
+  T* get() const { return p; }
+  uint64_t bytes() const { return n * sizeof(T); }
+};
+
+// ---------------------------------------------------------------------------
+// 64-bit hash of a node key (hdr word + 8 child words).
+__host__ __device__ __forceinline__ uint64_t mix_word(uint64_t h, uint32_t w) {
+  h ^= w;
+  h *= 0xFF51AFD7ED558CCDull;
+  h ^= h >> 32;
+  return h;
+}
+__host__ __device__ __forceinline__ uint64_t finish_hash(uint64_t h) {
+  h ^= h >> 29;
+  h *= 0xC4CEB9FE1A85EC53ull;
+  h ^= h >> 32;
+  return h;
+}
+__device__ __forceinline__ uint64_t hash_key9(uint32_t hdr, const uint32_t ch[8]) {
+  uint64_t h = mix_word(0x9E3779B97F4A7C15ull, hdr);
+#pragma unroll
+  for (int c = 0; c < 8; ++c) h = mix_word(h, ch[c]);
+  return finish_hash(h);
+}
+
+__device__ __forceinline__ void load_children(const uint32_t* ch, uint64_t i, uint32_t out[8]) {
+  const uint4* p = reinterpret_cast<const uint4*>(ch + 8 * i);
+  uint4 a = p[0], b = p[1];
+  out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
+  out[4] = b.x; out[5] = b.y; out[6] = b.z; out[7] = b.w;
+}
+__device__ __forceinline__ void store_children(uint32_t* ch, uint64_t i, const uint32_t v[8]) {
+  uint4* p = reinterpret_cast<uint4*>(ch + 8 * i);
+  p[0] = make_uint4(v[0], v[1], v[2], v[3]);
+  p[1] = make_uint4(v[4], v[5], v[6], v[7]);
+}
+
+inline uint64_t next_pow2(uint64_t x) {
+  uint64_t p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+// ---------------------------------------------------------------------------
+// Device-wide exclusive scan.  `In` maps an index to a value; `Out` receives
+// (index, exclusive prefix, value) for every index.  Three kernels: tile
+// reduce, (recursive) scan of tile sums, tile scan + emit.
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+template <class T>
+__device__ __forceinline__ T warp_incl_scan(T v) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T n = __shfl_up_sync(0xFFFFFFFFu, v, o);
+    if ((threadIdx.x & 31) >= o) v += n;
+  }
+  return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the block total
+// in *total (all threads).
+template <class T>
+__device__ __forceinline__ T block_excl_scan(T v, T* total) {
+  __shared__ T warp_sums[kScanThreads / 32];
+  __shared__ T tot;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  T inc = warp_incl_scan(v);
+  if (lane == 31) warp_sums[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    T s = (lane < kScanThreads / 32) ? warp_sums[lane] : T(0);
+    T si = warp_incl_scan(s);
+    if (lane < kScanThreads / 32) warp_sums[lane] = si - s;
+    if (lane == kScanThreads / 32 - 1) tot = si;
+  }
+  __syncthreads();
+  T excl = warp_sums[w] + inc - v;
+  *total = tot;
+  __syncthreads();
+  return excl;
+}
+
+template <class T, class In>
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(In in, uint64_t n, T* sums) {
+  const uint64_t base = uint64_t(blockIdx.x) * kScanTile;
+  T s = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    uint64_t i = base + uint64_t(j) * kScanThreads + threadIdx.x;
+    if (i < n) s += T(in(i));
+  }
+  T tot;
+  block_excl_scan<T>(s, &tot);
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+template <class T, class In, class Out>
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile_emit(In in, uint64_t n, const T* offs, Out out) {
+  __shared__ T sv[kScanTile];
+  const uint64_t base = uint64_t(blockIdx.x) * kScanTile;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    uint64_t i = base + uint64_t(j) * kScanThreads + threadIdx.x;
+    sv[j * kScanThreads + threadIdx.x] = (i < n) ? T(in(i)) : T(0);
+  }
+  __syncthreads();
+  T loc[kScanItems];
+  T run = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    loc[j] = sv[threadIdx.x * kScanItems + j];
+    run += loc[j];
+  }
+  T tot;
+  T pre = block_excl_scan<T>(run, &tot) + (offs ? offs[blockIdx.x] : T(0));
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    T v = loc[j];
+    sv[threadIdx.x * kScanItems + j] = pre;
+    pre += v;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    uint64_t i = base + uint64_t(j) * kScanThreads + threadIdx.x;
+    if (i < n) out(i, sv[j * kScanThreads + threadIdx.x]);
+  }
+}
+
+template <class T>
+struct ArrayIn {
+  const T* a;
+  __device__ __forceinline__ T operator()(uint64_t i) const { return a[i]; }
+};
+template <class T>
+struct ArrayOut {
+  T* a;
+  __device__ __forceinline__ void operator()(uint64_t i, T v) const { a[i] = v; }
+};
+
+template <class T>
+__global__ void k_store_total(const T* sums, const T* offs, uint64_t nb, T* total) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *total = nb ? offs[nb - 1] + sums[nb - 1] : T(0);
+}
+
+// Exclusive scan of in(0..n-1); out(i, prefix) for every i; the grand total
+// is written to *d_total (device) when d_total != nullptr.
+template <class T, class In, class Out>
+void device_exclusive_scan(const Exec& ex, In in, uint64_t n, Out out, T* d_total) {
+  if (n == 0) {
+    if (d_total) SVDAG_CUDA(cudaMemsetAsync(d_total, 0, sizeof(T), ex.stream));
+    return;
+  }
+  const uint64_t nb = (n + kScanTile - 1) / kScanTile;
+  if (nb == 1) {
+    DBuf<T> s(1, ex.stream);
+    SVDAG_LAUNCH(ex, (k_scan_tile_sums<T, In>), 1, kScanThreads, 0, in, n, s.get());
+    SVDAG_LAUNCH(ex, (k_scan_tile_emit<T, In, Out>), 1, kScanThreads, 0, in, n, (const T*)nullptr, out);
+    if (d_total) {
+      DBuf<T> z(1, ex.stream);
+      SVDAG_CUDA(cudaMemsetAsync(z.get(), 0, sizeof(T), ex.stream));
+      SVDAG_LAUNCH(ex, k_store_total<T>, 1, 32, 0, s.get(), z.get(), 1, d_total);
+    }
+    return;
+  }
+  DBuf<T> sums(nb, ex.stream), offs(nb, ex.stream);
+  SVDAG_LAUNCH(ex, (k_scan_tile_sums<T, In>), unsigned(nb), kScanThreads, 0, in, n, sums.get());
+  device_exclusive_scan<T>(ex, ArrayIn<T>{sums.get()}, nb, ArrayOut<T>{offs.get()}, (T*)nullptr);
+  SVDAG_LAUNCH(ex, (k_scan_tile_emit<T, In, Out>), unsigned(nb), kScanThreads, 0, in, n, (const T*)offs.get(), out);
+  if (d_total) SVDAG_LAUNCH(ex, k_store_total<T>, 1, 32, 0, sums.get(), offs.get(), nb, d_total);
+}
+
+template <class T>
+inline T read_scalar(const Exec& ex, const T* d) {
+  T h;
+  SVDAG_CUDA(cudaMemcpyAsync(&h, d, sizeof(T), cudaMemcpyDeviceToHost, ex.stream));
+  SVDAG_CUDA(cudaStreamSynchronize(ex.stream));
+  return h;
+}
+
+template <class T>
+__global__ void k_fill(T* p, uint64_t n, T v) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) p[i] = v;
+}
+template <class T>
+inline void fill(const Exec& ex, T* p, uint64_t n, T v) {
+  if (n) SVDAG_LAUNCH(ex, k_fill<T>, grid_for(ex, n, 256), 256, 0, p, n, v);
+}
+
+}  // namespace svdag

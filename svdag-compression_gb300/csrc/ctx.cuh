@@ -1,0 +1,61 @@
+// Internal state of one SVDAG build context and the phase entry points the
+// C ABI (api.cu) dispatches to.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace svdag {
+
+// One octree level in HBM, structure-of-arrays.
+//   hdr[n]      : mask | mirX<<8 | mirY<<16 | mirZ<<24
+//   ch[8n]      : child ids (kNull when absent); empty on the leaf level
+//   inv[n]      : invariant mask (SDAG only; empty otherwise)
+//   clev[8n]    : child levels (CSVDAG only; empty otherwise)
+//   path[n]     : 3 bits per level Morton path from the root (SVO build only)
+struct Level {
+  uint64_t n = 0;
+  DBuf<uint32_t> hdr;
+  DBuf<uint32_t> ch;
+  DBuf<uint8_t> inv;
+  DBuf<uint8_t> clev;
+  DBuf<uint64_t> path;
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  Exec ex;
+  uint64_t launches = 0;
+
+  const float* tris = nullptr;
+  uint64_t n_tris = 0;
+  DBuf<float> owned_tris;
+
+  uint32_t levels = 0;
+  int state = SVDAG_S_EMPTY;
+  bool child_levels_init = false;  // initChildLevels called (clev = lev+1 implicitly)
+  std::vector<Level> lev;
+  float bbox[6] = {0, 0, 0, 0, 0, 0};
+  double root_side = 0.0;
+
+  svdag_stats st{};
+  std::string last_error;
+
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+// Phases (each throws svdag::Error on failure).
+void phase_voxelize(Ctx& c, uint32_t levels, const double bbox[6]);
+void phase_reduce_dag(Ctx& c);
+void phase_reduce_sdag(Ctx& c);
+void phase_cross_level_merge(Ctx& c);
+
+}  // namespace svdag
+
+struct svdag_ctx {
+  svdag::Ctx c;
+};

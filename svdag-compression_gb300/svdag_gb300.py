@@ -1,0 +1,261 @@
+"""Python mirror of the GeomOctree build surface over the sm_103a C ABI.
+
+``Octree`` follows the reference's GeomOctree call surface
+(src/symvox/geom_octree.hpp:106-157): ``buildSVO`` / ``toDAG`` /
+``initChildLevels`` / ``toSDAG`` / ``mergeAcrossAllLevels`` and the getters.
+All compute runs in libsvdag_gpu.so on the GPU; there is no CPU fallback and
+loading fails loudly when the library or a device is missing.
+
+Node pools are returned per level as numpy structured arrays with the
+48-byte record layout ``REC`` (hdr, children[8], childLevels[8], invariant).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(PKG_DIR, "lib")
+NULL_NODE = 0xFFFFFFFE
+
+REC = np.dtype([("hdr", "<u4"), ("ch", "<u4", (8,)), ("cl", "u1", (8,)), ("inv", "u1"), ("pad", "u1", (3,))])
+
+STATES = {0: "S_EMPTY", 1: "S_SVO", 2: "S_DAG", 3: "S_SDAG"}
+
+
+class SvdagError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("svdag status %d: %s" % (status, message))
+        self.status = status
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [
+        ("n_total_voxels", ctypes.c_uint64),
+        ("n_nodes_svo", ctypes.c_uint64),
+        ("n_nodes_last_lev_svo", ctypes.c_uint64),
+        ("n_nodes_dag", ctypes.c_uint64),
+        ("n_nodes_sdag", ctypes.c_uint64),
+        ("n_nodes", ctypes.c_uint64),
+        ("n_cross_level_merged", ctypes.c_uint64),
+        ("n_missing_correspondences", ctypes.c_uint64),
+        ("levels", ctypes.c_uint32),
+        ("state", ctypes.c_uint32),
+        ("svo_ms", ctypes.c_double),
+        ("dag_ms", ctypes.c_double),
+        ("sdag_ms", ctypes.c_double),
+        ("csv_ms", ctypes.c_double),
+        ("gpu_launches", ctypes.c_uint64),
+    ]
+
+
+# Every symbol include/svdag_gpu.h declares, with its ctypes signature.
+_VP, _U32, _U64, _I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+GPU_SYMBOLS = {
+    "svdag_create": (_I, [ctypes.POINTER(_VP), _I, _VP]),
+    "svdag_destroy": (_I, [_VP]),
+    "svdag_clone": (_I, [_VP, ctypes.POINTER(_VP)]),
+    "svdag_last_error": (ctypes.c_char_p, [_VP]),
+    "svdag_status_string": (ctypes.c_char_p, [_I]),
+    "svdag_synchronize": (_I, [_VP]),
+    "svdag_upload_triangles": (_I, [_VP, _VP, _U64]),
+    "svdag_set_device_triangles": (_I, [_VP, _VP, _U64]),
+    "svdag_voxelize": (_I, [_VP, _U32, _VP]),
+    "svdag_reduce_dag": (_I, [_VP]),
+    "svdag_init_child_levels": (_I, [_VP]),
+    "svdag_reduce_sdag": (_I, [_VP]),
+    "svdag_cross_level_merge": (_I, [_VP]),
+    "svdag_level_count": (_I, [_VP, _U32, ctypes.POINTER(_U64)]),
+    "svdag_download_level": (_I, [_VP, _U32, _VP, _VP, _VP, _VP]),
+    "svdag_get_stats": (_I, [_VP, ctypes.POINTER(_Stats)]),
+    "svdag_level_device_ptrs": (_I, [_VP, _U32, _VP, _VP, _VP, _VP]),
+}
+
+HOST_SYMBOLS = {
+    "svdag_synth_icosphere_count": (_U64, [_U32]),
+    "svdag_synth_icosphere": (_I, [_U32, ctypes.c_double, ctypes.c_double, _U64, _VP]),
+    "svdag_synth_terrain_count": (_U64, [_U32]),
+    "svdag_synth_terrain": (_I, [_U32, _U32, ctypes.c_double, _U64, _VP]),
+    "svdag_synth_boxes": (_I, [_VP, _VP, _U64, _VP]),
+    "svdag_write_obj": (_I, [ctypes.c_char_p, _VP, _U64, _I]),
+}
+
+_gpu = None
+_host = None
+
+
+def _bind(lib, table):
+    for name, (res, args) in table.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+def gpu_library_path():
+    return os.path.join(LIB_DIR, "libsvdag_gpu.so")
+
+
+def load_gpu():
+    """Loads libsvdag_gpu.so (raises if it was not built)."""
+    global _gpu
+    if _gpu is None:
+        p = gpu_library_path()
+        if not os.path.exists(p):
+            raise SvdagError(-1, "libsvdag_gpu.so not built (run __graft_entry__.build())")
+        _gpu = _bind(ctypes.CDLL(p), GPU_SYMBOLS)
+    return _gpu
+
+
+def load_host():
+    global _host
+    if _host is None:
+        p = os.path.join(LIB_DIR, "libsvdag_host.so")
+        if not os.path.exists(p):
+            raise SvdagError(-1, "libsvdag_host.so not built (run __graft_entry__.build())")
+        _host = _bind(ctypes.CDLL(p), HOST_SYMBOLS)
+    return _host
+
+
+# --------------------------------------------------------------------------
+# seeded synthetic scenes (host)
+
+def icosphere(subdiv=5, radius=0.4, amp=0.08, seed=1234):
+    h = load_host()
+    n = h.svdag_synth_icosphere_count(subdiv)
+    out = np.empty((n, 9), np.float32)
+    if h.svdag_synth_icosphere(subdiv, radius, amp, seed, out.ctypes.data) != 0:
+        raise SvdagError(-1, "icosphere synthesis failed")
+    return out
+
+
+def terrain(grid=2048, octaves=8, height=0.3, seed=7):
+    h = load_host()
+    n = h.svdag_synth_terrain_count(grid)
+    out = np.empty((n, 9), np.float32)
+    if h.svdag_synth_terrain(grid, octaves, height, seed, out.ctypes.data) != 0:
+        raise SvdagError(-1, "terrain synthesis failed")
+    return out
+
+
+def boxes(lo, hi):
+    h = load_host()
+    lo = np.ascontiguousarray(lo, np.float32)
+    hi = np.ascontiguousarray(hi, np.float32)
+    n = lo.shape[0]
+    out = np.empty((n * 12, 9), np.float32)
+    h.svdag_synth_boxes(lo.ctypes.data, hi.ctypes.data, n, out.ctypes.data)
+    return out
+
+
+def write_obj(path, tris, pin_unit_cube=True):
+    h = load_host()
+    tris = np.ascontiguousarray(tris, np.float32)
+    if h.svdag_write_obj(path.encode(), tris.ctypes.data, tris.shape[0], 1 if pin_unit_cube else 0) != 0:
+        raise SvdagError(-1, "cannot write " + path)
+
+
+UNIT_BOX = (0.0, 0.0, 0.0, 1.0, 1.0, 1.0)
+
+
+# --------------------------------------------------------------------------
+class Octree:
+    """GPU octree with the GeomOctree build surface."""
+
+    def __init__(self, device=0, stream=None, _handle=None):
+        self._lib = load_gpu()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            h = ctypes.c_void_p()
+            self._check(self._lib.svdag_create(ctypes.byref(h), device, stream), None)
+            self._h = h
+        self._tris_ref = None
+
+    def _check(self, status, h=-1):
+        if status != 0:
+            hh = self._h if h == -1 else h
+            msg = self._lib.svdag_last_error(hh).decode() if hh else self._lib.svdag_status_string(status).decode()
+            raise SvdagError(status, msg or self._lib.svdag_status_string(status).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.svdag_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # scene input
+    def upload_triangles(self, tris):
+        tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+        self._check(self._lib.svdag_upload_triangles(self._h, tris.ctypes.data, tris.shape[0]))
+        self._lib.svdag_synchronize(self._h)
+
+    def set_device_triangles(self, dev_ptr, n_tris, keepalive=None):
+        self._tris_ref = keepalive
+        self._check(self._lib.svdag_set_device_triangles(self._h, ctypes.c_void_p(dev_ptr), n_tris))
+
+    # GeomOctree surface
+    def buildSVO(self, levels, bbox=UNIT_BOX):
+        bb = (ctypes.c_double * 6)(*bbox)
+        self._check(self._lib.svdag_voxelize(self._h, levels, bb))
+
+    def toDAG(self):
+        self._check(self._lib.svdag_reduce_dag(self._h))
+
+    def initChildLevels(self):
+        self._check(self._lib.svdag_init_child_levels(self._h))
+
+    def toSDAG(self):
+        self._check(self._lib.svdag_reduce_sdag(self._h))
+
+    def mergeAcrossAllLevels(self):
+        self._check(self._lib.svdag_cross_level_merge(self._h))
+        return self.stats()["n_cross_level_merged"]
+
+    def clone(self):
+        h = ctypes.c_void_p()
+        self._check(self._lib.svdag_clone(self._h, ctypes.byref(h)))
+        return Octree(_handle=h)
+
+    # results
+    def stats(self):
+        s = _Stats()
+        self._check(self._lib.svdag_get_stats(self._h, ctypes.byref(s)))
+        d = {k: getattr(s, k) for k, _ in _Stats._fields_}
+        d["state_name"] = STATES.get(d["state"], "?")
+        return d
+
+    def getLevels(self):
+        return self.stats()["levels"]
+
+    def level_count(self, level):
+        n = ctypes.c_uint64()
+        self._check(self._lib.svdag_level_count(self._h, level, ctypes.byref(n)))
+        return n.value
+
+    def level(self, level):
+        n = self.level_count(level)
+        hdr = np.zeros(n, np.uint32)
+        ch = np.zeros((n, 8), np.uint32)
+        cl = np.zeros((n, 8), np.uint8)
+        inv = np.zeros(n, np.uint8)
+        if n:
+            self._check(self._lib.svdag_download_level(self._h, level, hdr.ctypes.data, ch.ctypes.data,
+                                                       cl.ctypes.data, inv.ctypes.data))
+        rec = np.zeros(n, REC)
+        rec["hdr"], rec["ch"], rec["cl"], rec["inv"] = hdr, ch, cl, inv
+        return rec
+
+    def pool(self):
+        return [self.level(l) for l in range(self.getLevels())]

@@ -1,0 +1,37 @@
+"""Seeded scenes shared by the tests (same builders as tests/golden/make_golden.py)."""
+import json
+import os
+
+import numpy as np
+
+import svdag_gb300 as sv
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+
+
+def box_scene(n, levels, seed):
+    rng = np.random.default_rng(seed)
+    res = 2 ** levels
+    lo = rng.integers(0, res - 8, size=(n, 3))
+    side = rng.integers(1, 16, size=(n, 3))
+    hi = np.minimum(lo + side, res)
+    return sv.boxes((lo + 0.25) / res, (hi - 0.25) / res)
+
+
+SCENES = {
+    "ico5_L9": lambda: sv.icosphere(5, 0.4, 0.08, 1234),
+    "ico5_L7": lambda: sv.icosphere(5, 0.4, 0.08, 1234),
+    "ico3_L6": lambda: sv.icosphere(3, 0.4, 0.08, 99),
+    "ico4_L8_seed5": lambda: sv.icosphere(4, 0.35, 0.08, 5),
+    "terrain65_L8": lambda: sv.terrain(65, 8, 0.3, 7),
+    "terrain129_L9": lambda: sv.terrain(129, 8, 0.3, 11),
+    "terrain129_L9_step1": lambda: sv.terrain(129, 8, 0.3, 11),
+    "terrain257_L10": lambda: sv.terrain(257, 8, 0.3, 3),
+    "boxes_L8": lambda: box_scene(300, 8, 21),
+}
+
+
+def golden():
+    with open(os.path.join(GOLDEN, "golden.json")) as f:
+        return json.load(f)

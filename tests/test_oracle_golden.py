@@ -1,0 +1,68 @@
+"""The restated CPU oracle against the reference's own outputs (golden
+fixtures made by tests/golden/make_golden.py from the compiled reference)."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle_py
+from _scenes import SCENES, golden
+
+G = golden()
+
+
+@pytest.mark.parametrize("name", sorted(G))
+def test_scene_generator_is_reproducible(name):
+    tris = SCENES[name]()
+    assert tris.shape[0] == G[name]["n_tris"]
+    assert hashlib.sha256(np.ascontiguousarray(tris).tobytes()).hexdigest() == G[name]["tris_sha256"]
+
+
+@pytest.mark.parametrize("name", sorted(G))
+def test_oracle_matches_reference_pools(name):
+    g = G[name]
+    tris = SCENES[name]()
+    o = oracle_py.OracleOctree()
+    if g["step_levels"]:
+        o.buildDAG(tris, g["levels"], g["step_levels"])
+    else:
+        o.buildSVO(tris, g["levels"])
+        assert oracle_py.pool_digest(o.pool()) == g["svo"]["digest"]
+        assert o.stats()["n_total_voxels"] == g["nTotalVoxels"]
+        assert o.stats()["n_nodes_svo"] == g["nNodesSVO"]
+        o.toDAG()
+    o.initChildLevels()
+    assert [len(l) for l in o.pool()] == g["dag"]["counts"]
+    assert oracle_py.pool_digest(o.pool()) == g["dag"]["digest"]
+    assert o.stats()["n_nodes_dag"] == g["nNodesDAG"]
+    s = o.clone()
+    s.toSDAG()
+    assert oracle_py.pool_digest(s.pool()) == g["sdag"]["digest"]
+    assert s.stats()["n_nodes_sdag"] == g["nNodesSDAG"]
+    c = o.clone()
+    c.mergeAcrossAllLevels()
+    assert oracle_py.pool_digest(c.pool()) == g["csv"]["digest"]
+    assert c.stats()["n_nodes"] == g["nNodesCSVDAG"]
+    assert c.stats()["n_cross_level_merged"] == g["nCrossLevelMerged"]
+
+
+@pytest.mark.parametrize("name", ["ico5_L7", "ico3_L6", "terrain65_L8"])
+def test_full_pools_fixture(name):
+    """Full DAG/SDAG/CSVDAG pools kept for the small cases match the oracle."""
+    import os
+
+    from _scenes import GOLDEN
+
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    g = G[name]
+    o = oracle_py.OracleOctree()
+    o.buildSVO(SCENES[name](), g["levels"])
+    o.toDAG()
+    o.initChildLevels()
+    s = o.clone()
+    s.toSDAG()
+    c = o.clone()
+    c.mergeAcrossAllLevels()
+    for kind, oc in (("dag", o), ("sdag", s), ("csv", c)):
+        for l, lev in enumerate(oc.pool()):
+            np.testing.assert_array_equal(lev, z["%s_%d" % (kind, l)])
