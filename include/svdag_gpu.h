@@ -65,6 +65,8 @@ typedef struct svdag_stats {
   uint32_t state;                   /* enum svdag_state */
   double svo_ms, dag_ms, sdag_ms, csv_ms;
   uint64_t gpu_launches;            /* kernels launched by this context */
+  uint64_t frontier_pairs;          /* (triangle, node) visits of the last voxelization */
+  uint64_t sat_fallbacks;           /* box predicates decided in fp64 (fp32 filter undecided) */
 } svdag_stats;
 
 /* Lifetime.  `stream` is a cudaStream_t to run on, or NULL for a new one. */
@@ -96,6 +98,16 @@ int svdag_reduce_sdag(svdag_ctx* ctx);
 /* GeomOctree::mergeAcrossAllLevels (src/symvox/geom_octree_extension.cpp:1192-1544) */
 int svdag_cross_level_merge(svdag_ctx* ctx);
 
+/* GeomOctree(const NodeData&, bbox, rootSide, levels, stats)
+ * (src/symvox/geom_octree.cpp:49-60): replaces the context's octree with host
+ * node pools in DAG state -- the route a decoded .svdag input takes
+ * (src/svbuilder/main.cpp:97-101).  import_begin sizes the tree; each level is
+ * then given by import_level (children may be NULL on the leaf level). */
+int svdag_import_begin(svdag_ctx* ctx, uint32_t levels, const float bbox[6], double root_side,
+                       uint64_t n_total_voxels);
+int svdag_import_level(svdag_ctx* ctx, uint32_t level, uint64_t count, const uint32_t* hdr,
+                       const uint32_t* children);
+
 /* Results.  Host buffers sized by svdag_level_count; any pointer may be NULL
  * to skip that field.  children/child_levels take 8 entries per node. */
 int svdag_level_count(const svdag_ctx* ctx, uint32_t level, uint64_t* count);
@@ -107,6 +119,15 @@ int svdag_get_stats(const svdag_ctx* ctx, svdag_stats* out);
 int svdag_level_device_ptrs(const svdag_ctx* ctx, uint32_t level, const uint32_t** hdr,
                             const uint32_t** children, const uint8_t** child_levels,
                             const uint8_t** invariant);
+
+/* Per-kernel device timing (no counterpart in the reference, whose Stats
+ * hold phase times only, src/symvox/geom_octree.hpp:54).  While enabled,
+ * every kernel launch of the context is bracketed by CUDA events on its
+ * stream.  The report is text, one line per kernel name:
+ *   "<kernel>;<launches>;<total_ms>\n"
+ * and reading it clears the accumulated records. */
+int svdag_profile_enable(svdag_ctx* ctx, int enable);
+int svdag_profile_report(svdag_ctx* ctx, char* buf, uint64_t capacity);
 
 #ifdef __cplusplus
 }

@@ -25,7 +25,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["api.cu", "voxelize.cu", "reduce.cu", "csvdag.cu"]
-HOST_SOURCES = ["synth.cpp"]
+HOST_SOURCES = ["synth.cpp", "encoders.cpp"]
 
 
 def _run(cmd, cwd=None):

@@ -196,6 +196,46 @@ int svdag_cross_level_merge(svdag_ctx* h) {
   return guarded(h, [&](Ctx& c) { c.st.csv_ms = timed(c, [&] { svdag::phase_cross_level_merge(c); }); });
 }
 
+int svdag_import_begin(svdag_ctx* h, uint32_t levels, const float bbox[6], double root_side, uint64_t n_total_voxels) {
+  if (!bbox) return fail(h, SVDAG_ERR_INVALID_ARG, "import_begin: null bbox");
+  return guarded(h, [&](Ctx& c) {
+    if (levels < 1 || levels > 21) throw Error(SVDAG_ERR_INVALID_ARG, "import_begin: levels must be in [1, 21]");
+    c.lev.clear();
+    c.lev.resize(levels);
+    c.levels = levels;
+    std::memcpy(c.bbox, bbox, sizeof(c.bbox));
+    c.root_side = root_side;
+    c.state = SVDAG_S_DAG;
+    c.child_levels_init = false;
+    c.st = svdag_stats{};
+    c.st.n_total_voxels = n_total_voxels;
+    c.st.levels = levels;
+  });
+}
+
+int svdag_import_level(svdag_ctx* h, uint32_t level, uint64_t count, const uint32_t* hdr, const uint32_t* children) {
+  return guarded(h, [&](Ctx& c) {
+    if (level >= c.lev.size()) throw Error(SVDAG_ERR_INVALID_ARG, "import_level: level out of range");
+    if (count && !hdr) throw Error(SVDAG_ERR_INVALID_ARG, "import_level: null hdr");
+    const bool inner = level + 1 < c.lev.size();
+    if (count && inner && !children) throw Error(SVDAG_ERR_INVALID_ARG, "import_level: inner level needs children");
+    svdag::Level& L = c.lev[level];
+    L = svdag::Level();
+    L.n = count;
+    L.hdr.alloc(count ? count : 1, c.stream);
+    if (count) SVDAG_CUDA(cudaMemcpyAsync(L.hdr.get(), hdr, 4 * count, cudaMemcpyHostToDevice, c.stream));
+    if (inner) {
+      L.ch.alloc(8 * (count ? count : 1), c.stream);
+      if (count) SVDAG_CUDA(cudaMemcpyAsync(L.ch.get(), children, 32 * count, cudaMemcpyHostToDevice, c.stream));
+    }
+    SVDAG_CUDA(cudaStreamSynchronize(c.stream));
+    uint64_t n = 1;
+    for (size_t l = 1; l < c.lev.size(); ++l) n += c.lev[l].n;
+    c.st.n_nodes = n;
+    c.st.n_nodes_dag = n;
+  });
+}
+
 int svdag_level_count(const svdag_ctx* h, uint32_t level, uint64_t* count) {
   if (!h || !count) return SVDAG_ERR_INVALID_ARG;
   if (level >= h->c.lev.size()) return SVDAG_ERR_INVALID_ARG;
@@ -239,6 +279,40 @@ int svdag_get_stats(const svdag_ctx* h, svdag_stats* out) {
   out->state = uint32_t(h->c.state);
   out->gpu_launches = h->c.launches;
   return SVDAG_OK;
+}
+
+int svdag_profile_enable(svdag_ctx* h, int enable) {
+  return guarded(h, [&](Ctx& c) { c.ex.prof = enable ? &c.prof : nullptr; });
+}
+
+int svdag_profile_report(svdag_ctx* h, char* buf, uint64_t cap) {
+  if (!buf || cap == 0) return fail(h, SVDAG_ERR_INVALID_ARG, "profile_report: no buffer");
+  return guarded(h, [&](Ctx& c) {
+    SVDAG_CUDA(cudaStreamSynchronize(c.stream));
+    std::vector<std::string> order;
+    std::vector<std::pair<uint64_t, double>> acc;
+    for (auto& r : c.prof.recs) {
+      float ms = 0.f;
+      SVDAG_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+      size_t k = 0;
+      while (k < order.size() && order[k] != r.name) ++k;
+      if (k == order.size()) { order.push_back(r.name); acc.push_back({0, 0.0}); }
+      acc[k].first += 1;
+      acc[k].second += ms;
+      c.prof.pool.push_back(r.a);
+      c.prof.pool.push_back(r.b);
+    }
+    c.prof.recs.clear();
+    std::string out;
+    char line[512];
+    for (size_t k = 0; k < order.size(); ++k) {
+      std::snprintf(line, sizeof(line), "%s;%llu;%.6f\n", order[k].c_str(), (unsigned long long)acc[k].first,
+                    acc[k].second);
+      out += line;
+    }
+    if (out.size() + 1 > cap) throw Error(SVDAG_ERR_OVERFLOW, "profile_report: buffer too small");
+    std::memcpy(buf, out.c_str(), out.size() + 1);
+  });
 }
 
 int svdag_level_device_ptrs(const svdag_ctx* h, uint32_t level, const uint32_t** hdr, const uint32_t** children,

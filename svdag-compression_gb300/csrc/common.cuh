@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "svdag_gpu.h"
 
@@ -32,11 +33,31 @@ struct Error : public std::runtime_error {
     }                                                                                      \
   } while (0)
 
+// Optional per-launch device timing: each launch is bracketed by two CUDA
+// events on the context stream; durations are summed per kernel name when
+// the report is read.
+struct Profiler {
+  struct Rec { const char* name; cudaEvent_t a, b; };
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t get() {
+    if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+    cudaEvent_t e;
+    SVDAG_CUDA(cudaEventCreate(&e));
+    return e;
+  }
+  ~Profiler() {
+    for (auto& r : recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
 // Per-context execution environment handed to every launch helper.
 struct Exec {
   cudaStream_t stream = nullptr;
   int sm_count = 152;
   uint64_t* launches = nullptr;  // incremented once per kernel launch
+  Profiler* prof = nullptr;      // non-null while kernel timing is enabled
 };
 
 // Grid for a grid-stride loop over n items.
@@ -49,9 +70,20 @@ inline unsigned grid_for(const Exec& ex, uint64_t n, unsigned threads, unsigned 
 
 #define SVDAG_LAUNCH(ex, kernel, grid, block, smem, ...)                 \
   do {                                                                   \
+    ::svdag::Profiler* p__ = (ex).prof;                                  \
+    cudaEvent_t a__ = nullptr, b__ = nullptr;                            \
+    if (p__) {                                                           \
+      a__ = p__->get();                                                  \
+      b__ = p__->get();                                                  \
+      SVDAG_CUDA(cudaEventRecord(a__, (ex).stream));                     \
+    }                                                                    \
     kernel<<<(grid), (block), (smem), (ex).stream>>>(__VA_ARGS__);       \
     if ((ex).launches) ++*(ex).launches;                                 \
     SVDAG_CUDA(cudaPeekAtLastError());                                   \
+    if (p__) {                                                           \
+      SVDAG_CUDA(cudaEventRecord(b__, (ex).stream));                     \
+      p__->recs.push_back({#kernel, a__, b__});                          \
+    }                                                                    \
   } while (0)
 
 // Stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync).

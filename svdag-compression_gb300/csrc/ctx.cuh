@@ -14,14 +14,14 @@ namespace svdag {
 //   ch[8n]      : child ids (kNull when absent); empty on the leaf level
 //   inv[n]      : invariant mask (SDAG only; empty otherwise)
 //   clev[8n]    : child levels (CSVDAG only; empty otherwise)
-//   path[n]     : 3 bits per level Morton path from the root (SVO build only)
+//   ctr[3n]     : fp64 node centre (SVO build only)
 struct Level {
   uint64_t n = 0;
   DBuf<uint32_t> hdr;
   DBuf<uint32_t> ch;
   DBuf<uint8_t> inv;
   DBuf<uint8_t> clev;
-  DBuf<uint64_t> path;
+  DBuf<double> ctr;
 };
 
 struct Ctx {
@@ -46,6 +46,7 @@ struct Ctx {
   std::string last_error;
 
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  Profiler prof;
 };
 
 // Phases (each throws svdag::Error on failure).

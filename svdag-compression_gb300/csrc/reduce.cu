@@ -22,104 +22,13 @@
 // always resolves, so rounds terminate) and give exactly the sequential
 // result.
 #include "ctx.cuh"
+#include "dedup.cuh"
 
 namespace svdag {
 namespace {
 
 constexpr uint32_t kUndecided = 0xFFFFFFFFu;
 constexpr uint32_t kUnique = 0xFFFFFFFEu;
-
-__device__ __forceinline__ uint64_t ld_cg64(const unsigned long long* p) { return __ldcg(p); }
-__device__ __forceinline__ uint32_t ld_cg32(const uint32_t* p) { return __ldcg(p); }
-
-__device__ __forceinline__ void load_key(const uint32_t* hdr, const uint32_t* ch, uint64_t i, uint32_t& h, uint32_t c[8]) {
-  h = hdr[i];
-  if (ch) {
-    load_children(ch, i, c);
-  } else {
-#pragma unroll
-    for (int k = 0; k < 8; ++k) c[k] = kNull;
-  }
-}
-
-__device__ __forceinline__ bool key_equal_at(const uint32_t* hdr, const uint32_t* ch, uint64_t j, uint32_t h,
-                                             const uint32_t c[8]) {
-  if (hdr[j] != h) return false;
-  if (!ch) return true;
-  uint32_t d[8];
-  load_children(ch, j, d);
-  bool eq = true;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) eq &= (d[k] == c[k]);
-  return eq;
-}
-
-struct Table {
-  unsigned long long* slots;
-  uint64_t mask;  // size - 1 (power of two)
-};
-
-// Insert node i's key; equal keys keep the minimum index.  Returns the slot.
-__device__ uint64_t table_insert(Table T, const uint32_t* hdr, const uint32_t* ch, uint32_t i, uint32_t h,
-                                 const uint32_t c[8], int* err) {
-  const uint64_t hk = hash_key9(h, c);
-  const uint64_t tag = hk >> 32;
-  const unsigned long long mine = (tag << 32) | i;
-  uint64_t pos = hk & T.mask;
-  for (uint64_t probe = 0; probe <= T.mask; ++probe) {
-    unsigned long long cur = ld_cg64(&T.slots[pos]);
-    if (cur == kEmpty64) {
-      const unsigned long long prev = atomicCAS(&T.slots[pos], kEmpty64, mine);
-      if (prev == kEmpty64) return pos;
-      cur = prev;
-    }
-    if ((cur >> 32) == tag) {
-      const uint32_t j = uint32_t(cur);
-      if (key_equal_at(hdr, ch, j, h, c)) {
-        if (i < j) atomicMin(&T.slots[pos], mine);
-        return pos;
-      }
-    }
-    pos = (pos + 1) & T.mask;
-  }
-  atomicExch(err, 1);
-  return kEmpty64;
-}
-
-// Look a key up; returns the minimum index stored for it or kNone.
-__device__ uint32_t table_find(Table T, const uint32_t* hdr, const uint32_t* ch, uint32_t h, const uint32_t c[8]) {
-  const uint64_t hk = hash_key9(h, c);
-  const uint64_t tag = hk >> 32;
-  uint64_t pos = hk & T.mask;
-  for (uint64_t probe = 0; probe <= T.mask; ++probe) {
-    const unsigned long long cur = T.slots[pos];
-    if (cur == kEmpty64) return kNone;
-    if ((cur >> 32) == tag) {
-      const uint32_t j = uint32_t(cur);
-      if (key_equal_at(hdr, ch, j, h, c)) return j;
-    }
-    pos = (pos + 1) & T.mask;
-  }
-  return kNone;
-}
-
-__global__ void k_insert(Table T, const uint32_t* __restrict__ hdr, const uint32_t* __restrict__ ch, uint64_t n,
-                         uint32_t* __restrict__ slot_of, int* err) {
-  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
-    uint32_t h, c[8];
-    load_key(hdr, ch, i, h, c);
-    if ((h & 0xFFu) == 0) { slot_of[i] = kNone; continue; }  // empty nodes are skipped (geom_octree.cpp:495)
-    const uint64_t s = table_insert(T, hdr, ch, uint32_t(i), h, c, err);
-    slot_of[i] = uint32_t(s);
-  }
-}
-
-__global__ void k_rep(Table T, const uint32_t* __restrict__ slot_of, uint64_t n, uint32_t* __restrict__ rep) {
-  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
-    const uint32_t s = slot_of[i];
-    rep[i] = (s == kNone) ? kNone : uint32_t(T.slots[s]);
-  }
-}
 
 struct RepFlagIn {
   const uint32_t* rep;
@@ -400,17 +309,6 @@ __global__ void k_remap_parents_sdag(uint32_t* __restrict__ phdr, uint32_t* __re
     store_children(pch, p, c);
     if (mx | my | mz) phdr[p] |= (mx << 8) | (my << 16) | (mz << 24);
   }
-}
-
-Table make_table(const Exec& ex, uint64_t n, DBuf<unsigned long long>& buf) {
-  const uint64_t size = next_pow2(n < 16 ? 32 : 2 * n);
-  buf.alloc(size, ex.stream);
-  SVDAG_CUDA(cudaMemsetAsync(buf.get(), 0xFF, size * 8, ex.stream));
-  return Table{buf.get(), size - 1};
-}
-
-void check_err(const Exec& ex, const int* d_err, const char* what) {
-  if (read_scalar(ex, d_err)) throw Error(SVDAG_ERR_OVERFLOW, std::string(what) + ": hash table probe limit reached");
 }
 
 }  // namespace

@@ -1,0 +1,379 @@
+// Triangle / box overlap with the reference's exact fp64 decisions
+// (src/symvox/test_triangle_box.cpp:38-184), evaluated through a certified
+// fp32 filter.
+//
+// testTriBox rejects a box as soon as one of 13 independent tests fails (9
+// edge-axis tests, 3 bounding-box tests, 1 plane test); the answer is the AND
+// of the 13 fp64 predicates whatever their order.  Each predicate compares
+// fp64 values that the reference computes in a fixed operation order.  Here
+// every predicate is first evaluated in fp32 together with a forward error
+// bound that covers both the fp32 evaluation and the reference's fp64
+// evaluation, relative to the exact real value of the same expression.  When
+// the fp32 margin exceeds the bound the fp64 predicate provably has the same
+// outcome; otherwise (near-ties, non-finite or huge inputs) that one
+// predicate is recomputed in fp64 exactly as the reference does.  The result
+// is identical to the reference's for every input.
+//
+// Error model: fl(a op b) = (a op b)(1 + d), |d| <= u (u32 = 2^-24,
+// u64 = 2^-53), plus an absolute slack of 2^-100 against fp32 underflow.
+// Bounds (exact-real anchors t - c, t_j - t_i; derivation in the design doc):
+//   edge-axis value p = a*u - b*w:  |p_f - p*| <= 4.1 u32 S + 1.02 (|a|+|b|) clo
+//                                   S = |a u| + |b w|,   clo = |c - fl32(c)|
+//   rad = (|a|+|b|) h:              |rad_f - rad*| <= 3.1 u32 rad
+//   fp64 side:                      <= 2^-47 (V^2 + V h)
+// where V bounds |t - c| over the pair.  Plane test bounds are in
+// plane_decide().
+//
+// Compiled as host code (tests) with -ffp-contract=off and as device code
+// with explicitly rounded intrinsics, so both builds make the same decisions.
+#pragma once
+
+#include <stdint.h>
+
+#include <cmath>
+
+#if defined(__CUDACC__)
+#define SAT_HD __host__ __device__ __forceinline__
+#else
+#define SAT_HD inline
+#endif
+
+namespace svdag {
+namespace sat {
+
+#if defined(__CUDA_ARCH__)
+SAT_HD float fadd(float a, float b) { return __fadd_rn(a, b); }
+SAT_HD float fsub(float a, float b) { return __fsub_rn(a, b); }
+SAT_HD float fmul(float a, float b) { return __fmul_rn(a, b); }
+SAT_HD double dadd(double a, double b) { return __dadd_rn(a, b); }
+SAT_HD double dsub(double a, double b) { return __dsub_rn(a, b); }
+SAT_HD double dmul(double a, double b) { return __dmul_rn(a, b); }
+SAT_HD float fabsf_(float a) { return fabsf(a); }
+SAT_HD double fabs_(double a) { return fabs(a); }
+#else
+SAT_HD float fadd(float a, float b) { return a + b; }
+SAT_HD float fsub(float a, float b) { return a - b; }
+SAT_HD float fmul(float a, float b) { return a * b; }
+SAT_HD double dadd(double a, double b) { return a + b; }
+SAT_HD double dsub(double a, double b) { return a - b; }
+SAT_HD double dmul(double a, double b) { return a * b; }
+SAT_HD float fabsf_(float a) { return std::fabs(a); }
+SAT_HD double fabs_(double a) { return std::fabs(a); }
+#endif
+
+constexpr float kU32 = 5.9604644775390625e-08f;  // 2^-24
+constexpr float kTiny = 7.8886090522101181e-31f; // 2^-100 absolute slack
+constexpr float kD64 = 7.105427357601002e-15f;   // 2^-47 (fp64-side factor)
+
+// Three-valued outcome of one comparison.
+enum Tri : int { kFalse = 0, kTrue = 1, kUnknown = 2 };
+
+// ---------------------------------------------------------------------------
+// Exact fp64 replicas of the reference's individual tests (used for the
+// predicates the filter cannot decide).
+
+// AXISTEST_* reject decision (test_triangle_box.cpp:59-102).  b_first selects
+// the Z12 ordering (p2 < p1).
+SAT_HD bool axis_reject64(double pa, double pb, double fa, double fb, double h, bool b_first) {
+  double mn, mx;
+  if (b_first) {
+    if (pb < pa) { mn = pb; mx = pa; } else { mn = pa; mx = pb; }
+  } else {
+    if (pa < pb) { mn = pa; mx = pb; } else { mn = pb; mx = pa; }
+  }
+  const double rad = dmul(dadd(fa, fb), h);
+  return (mn > rad || mx < -rad);
+}
+
+// p = a*u - b*w (X and Z macros) and p = -a*u + b*w (Y macros)
+SAT_HD double amb64(double a, double u, double b, double w) { return dsub(dmul(a, u), dmul(b, w)); }
+SAT_HD double nab64(double a, double u, double b, double w) { return dadd(dmul(-a, u), dmul(b, w)); }
+
+// fp64 vertex offsets and edges of one box, as the reference computes them.
+struct Box64 {
+  double v[3][3];  // vertex, axis
+  double e[3][3];  // edge, axis
+};
+
+SAT_HD void box64(const float t[9], const double c[3], Box64& b) {
+  for (int i = 0; i < 3; ++i)
+    for (int q = 0; q < 3; ++q) b.v[i][q] = dsub(double(t[3 * i + q]), c[q]);
+  for (int q = 0; q < 3; ++q) {
+    b.e[0][q] = dsub(b.v[1][q], b.v[0][q]);
+    b.e[1][q] = dsub(b.v[2][q], b.v[1][q]);
+    b.e[2][q] = dsub(b.v[0][q], b.v[2][q]);
+  }
+}
+
+// Edge-axis test k (0..8) in the reference's order, fp64.  Returns reject.
+SAT_HD bool edge_test64(const Box64& b, int k, double h) {
+  const int X = 0, Y = 1, Z = 2;
+  const int j = k / 3;  // edge
+  const double* e = b.e[j];
+  const double* v0 = b.v[0];
+  const double* v1 = b.v[1];
+  const double* v2 = b.v[2];
+  const double fx = fabs_(e[X]), fy = fabs_(e[Y]), fz = fabs_(e[Z]);
+  switch (k) {
+    case 0: return axis_reject64(amb64(e[Z], v0[Y], e[Y], v0[Z]), amb64(e[Z], v2[Y], e[Y], v2[Z]), fz, fy, h, false);
+    case 1: return axis_reject64(nab64(e[Z], v0[X], e[X], v0[Z]), nab64(e[Z], v2[X], e[X], v2[Z]), fz, fx, h, false);
+    case 2: return axis_reject64(amb64(e[Y], v1[X], e[X], v1[Y]), amb64(e[Y], v2[X], e[X], v2[Y]), fy, fx, h, true);
+    case 3: return axis_reject64(amb64(e[Z], v0[Y], e[Y], v0[Z]), amb64(e[Z], v2[Y], e[Y], v2[Z]), fz, fy, h, false);
+    case 4: return axis_reject64(nab64(e[Z], v0[X], e[X], v0[Z]), nab64(e[Z], v2[X], e[X], v2[Z]), fz, fx, h, false);
+    case 5: return axis_reject64(amb64(e[Y], v0[X], e[X], v0[Y]), amb64(e[Y], v1[X], e[X], v1[Y]), fy, fx, h, false);
+    case 6: return axis_reject64(amb64(e[Z], v0[Y], e[Y], v0[Z]), amb64(e[Z], v1[Y], e[Y], v1[Z]), fz, fy, h, false);
+    case 7: return axis_reject64(nab64(e[Z], v0[X], e[X], v0[Z]), nab64(e[Z], v1[X], e[X], v1[Z]), fz, fx, h, false);
+    default: return axis_reject64(amb64(e[Y], v1[X], e[X], v1[Y]), amb64(e[Y], v2[X], e[X], v2[Y]), fy, fx, h, true);
+  }
+}
+
+// FINDMINMAX test on one axis (test_triangle_box.cpp:165-174), fp64.
+SAT_HD bool aabb_reject64(const Box64& b, int q, double h) {
+  double mn = b.v[0][q], mx = b.v[0][q];
+  if (b.v[1][q] < mn) mn = b.v[1][q];
+  if (b.v[1][q] > mx) mx = b.v[1][q];
+  if (b.v[2][q] < mn) mn = b.v[2][q];
+  if (b.v[2][q] > mx) mx = b.v[2][q];
+  return (mn > h || mx < -h);
+}
+
+// planeBoxOverlap(e0 x e1, v0, h) (test_triangle_box.cpp:38-56, 179-180), fp64.
+// Returns reject (= !overlap).
+SAT_HD bool plane_reject64(const Box64& b, double h) {
+  const double* e0 = b.e[0];
+  const double* e1 = b.e[1];
+  const double n[3] = {dsub(dmul(e0[1], e1[2]), dmul(e0[2], e1[1])), dsub(dmul(e0[2], e1[0]), dmul(e0[0], e1[2])),
+                       dsub(dmul(e0[0], e1[1]), dmul(e0[1], e1[0]))};
+  double vmin[3], vmax[3];
+  for (int q = 0; q < 3; ++q) {
+    if (n[q] > 0.0) { vmin[q] = dsub(-h, b.v[0][q]); vmax[q] = dsub(h, b.v[0][q]); }
+    else            { vmin[q] = dsub(h, b.v[0][q]);  vmax[q] = dsub(-h, b.v[0][q]); }
+  }
+  const double dmin = dadd(dadd(dmul(n[0], vmin[0]), dmul(n[1], vmin[1])), dmul(n[2], vmin[2]));
+  if (dmin > 0.0) return true;
+  const double dmax = dadd(dadd(dmul(n[0], vmax[0]), dmul(n[1], vmax[1])), dmul(n[2], vmax[2]));
+  return !(dmax >= 0.0);
+}
+
+// The whole reference test in fp64 (reference order).  Returns overlap.
+SAT_HD bool tri_box64(const float t[9], const double c[3], double h) {
+  Box64 b;
+  box64(t, c, b);
+  for (int k = 0; k < 9; ++k)
+    if (edge_test64(b, k, h)) return false;
+  for (int q = 0; q < 3; ++q)
+    if (aabb_reject64(b, q, h)) return false;
+  return !plane_reject64(b, h);
+}
+
+// ---------------------------------------------------------------------------
+// fp32 filter.
+
+// Per (triangle, parent node) data shared by the 8 children.
+struct Pair32 {
+  float t[9];        // triangle (exact)
+  float e[3][3];     // fp32 edges  t1-t0, t2-t1, t0-t2 (edge, axis)
+  float ae[3][3];    // |e|
+  double cd[3][2];   // child centre coordinate per axis and side (fp64, reference values)
+  float chi[3][2];   // fl32(cd)
+  float clo;         // max |cd - chi| over axes and sides
+  float h;           // child half side (exact in fp32)
+  double hd;
+  bool fast;         // fp32 path usable (finite, moderate magnitudes)
+};
+
+// Decides x > y from fp32 values with a tolerance; kUnknown inside it.
+SAT_HD Tri gt(float x, float y, float tol) {
+  const float d = fsub(x, y);
+  if (d > tol) return kTrue;
+  if (d < -tol) return kFalse;
+  return kUnknown;
+}
+
+SAT_HD Tri tri_and(Tri a, Tri b) {
+  if (a == kFalse || b == kFalse) return kFalse;
+  if (a == kTrue && b == kTrue) return kTrue;
+  return kUnknown;
+}
+SAT_HD Tri tri_or(Tri a, Tri b) {
+  if (a == kTrue || b == kTrue) return kTrue;
+  if (a == kFalse && b == kFalse) return kFalse;
+  return kUnknown;
+}
+
+// Builds the per-pair data; c = parent centre, k = child half side.
+SAT_HD void pair_setup(const float t[9], const double c[3], double k, Pair32& P) {
+  for (int i = 0; i < 9; ++i) P.t[i] = t[i];
+  bool ok = true;
+  for (int i = 0; i < 9; ++i) ok = ok && (fabsf_(t[i]) < 1.0e18f);  // also false for NaN
+  float clo = 0.f;
+  for (int q = 0; q < 3; ++q) {
+    // child centre = parent centre + (+-k), as geom_octree.cpp:222-230
+    P.cd[q][0] = dadd(c[q], -k);
+    P.cd[q][1] = dadd(c[q], k);
+    for (int s = 0; s < 2; ++s) {
+      const float hi = float(P.cd[q][s]);
+      P.chi[q][s] = hi;
+      const double lo = dsub(P.cd[q][s], double(hi));
+      const float alo = float(fabs_(lo));
+      clo = (alo > clo) ? alo : clo;
+      ok = ok && (fabs_(P.cd[q][s]) < 1.0e18);
+    }
+  }
+  P.clo = clo * 1.0000002f;
+  for (int q = 0; q < 3; ++q) {
+    P.e[0][q] = fsub(t[3 + q], t[q]);
+    P.e[1][q] = fsub(t[6 + q], t[3 + q]);
+    P.e[2][q] = fsub(t[q], t[6 + q]);
+    for (int j = 0; j < 3; ++j) P.ae[j][q] = fabsf_(P.e[j][q]);
+  }
+  P.hd = k;
+  P.h = float(k);
+  ok = ok && (double(P.h) == k) && (k > 1.0e-30) && (k < 1.0e18);
+  P.fast = ok;
+}
+
+// One edge-axis test in fp32: reject (kTrue), keep (kFalse) or kUnknown.
+// p_i = sa*a*u_i - sb*b*w_i  for the two vertices i of the test;
+// V: bound on |t - c| over this box.
+SAT_HD Tri edge_test32(float a, float b, bool neg_a, float u0, float w0, float u1, float w1, float fa, float fb,
+                       float h, float clo, float V) {
+  // p = a*u - b*w, or (-a)*u + b*w for the Y tests; both are +-(a*u - b*w)
+  // up to the order of the two roundings, which the bound covers.
+  const float x0 = fmul(a, u0), y0 = fmul(b, w0);
+  const float x1 = fmul(a, u1), y1 = fmul(b, w1);
+  float p0 = fsub(x0, y0), p1 = fsub(x1, y1);
+  if (neg_a) { p0 = -p0; p1 = -p1; }
+  const float s0 = fadd(fabsf_(x0), fabsf_(y0));
+  const float s1 = fadd(fabsf_(x1), fabsf_(y1));
+  const float rad = fmul(fadd(fa, fb), h);
+  const float ab = fadd(fa, fb);
+  const float common = fadd(fadd(fmul(3.2f * kU32, rad), fmul(1.03f, fmul(ab, clo))),
+                            fadd(fmul(kD64, fadd(fmul(V, V), fmul(V, h))), kTiny));
+  const float tol0 = fadd(fmul(4.2f * kU32, s0), common);
+  const float tol1 = fadd(fmul(4.2f * kU32, s1), common);
+  // reject iff (p0 > rad && p1 > rad) || (p0 < -rad && p1 < -rad)
+  const Tri above = tri_and(gt(p0, rad, tol0), gt(p1, rad, tol1));
+  const Tri below = tri_and(gt(-rad, p0, tol0), gt(-rad, p1, tol1));
+  return tri_or(above, below);
+}
+
+// Overlap decision for child `ci` (index 4x+2y+z) of the pair.  Returns
+// true when the child box overlaps the triangle; `fallbacks` counts the
+// predicates that needed fp64.
+SAT_HD bool child_overlap(const Pair32& P, int ci, unsigned* fallbacks) {
+  const int sx = (ci >> 2) & 1, sy = (ci >> 1) & 1, sz = ci & 1;
+  const double c[3] = {P.cd[0][sx], P.cd[1][sy], P.cd[2][sz]};
+  if (!P.fast) {
+    if (fallbacks) ++*fallbacks;
+    return tri_box64(P.t, c, P.hd);
+  }
+  const float h = P.h;
+  const float clo = P.clo;
+  // fp32 vertex offsets v = t - fl32(c); |v_f - (t - c)| <= 1.01 u32 |v_f| + 1.01 clo
+  float v[3][3];
+  const float chi[3] = {P.chi[0][sx], P.chi[1][sy], P.chi[2][sz]};
+  float V = 0.f;
+  for (int i = 0; i < 3; ++i)
+    for (int q = 0; q < 3; ++q) {
+      v[i][q] = fsub(P.t[3 * i + q], chi[q]);
+      const float a = fabsf_(v[i][q]);
+      V = (a > V) ? a : V;
+    }
+  V = fadd(fmul(V, 1.0000003f), fmul(1.01f, clo));
+
+  Box64 b64;
+  bool have64 = false;
+  auto need64 = [&]() {
+    if (!have64) { box64(P.t, c, b64); have64 = true; }
+    if (fallbacks) ++*fallbacks;
+  };
+
+  // bounding-box tests (FINDMINMAX): v_d > h decided from v_f
+  for (int q = 0; q < 3; ++q) {
+    float mn = v[0][q], mx = v[0][q];
+    mn = (v[1][q] < mn) ? v[1][q] : mn;
+    mx = (v[1][q] > mx) ? v[1][q] : mx;
+    mn = (v[2][q] < mn) ? v[2][q] : mn;
+    mx = (v[2][q] > mx) ? v[2][q] : mx;
+    const float tmn = fadd(fadd(fmul(1.1f * kU32, fabsf_(mn)), fmul(1.02f, clo)), fadd(fmul(2.2e-16f, fadd(fabsf_(mn), h)), kTiny));
+    const float tmx = fadd(fadd(fmul(1.1f * kU32, fabsf_(mx)), fmul(1.02f, clo)), fadd(fmul(2.2e-16f, fadd(fabsf_(mx), h)), kTiny));
+    const Tri r = tri_or(gt(mn, h, tmn), gt(-h, mx, tmx));
+    if (r == kTrue) return false;
+    if (r == kUnknown) {
+      need64();
+      if (aabb_reject64(b64, q, P.hd)) return false;
+    }
+  }
+
+  // nine edge-axis tests (test_triangle_box.cpp:137-156)
+  const int X = 0, Y = 1, Z = 2;
+  for (int k = 0; k < 9; ++k) {
+    const int j = k / 3;
+    const float* e = P.e[j];
+    const float* ae = P.ae[j];
+    Tri r;
+    switch (k) {
+      case 0: case 3:  // X01: a=e.z, b=e.y over v0, v2 on (y, z)
+        r = edge_test32(e[Z], e[Y], false, v[0][Y], v[0][Z], v[2][Y], v[2][Z], ae[Z], ae[Y], h, clo, V); break;
+      case 1: case 4:  // Y02: -a*v.x + b*v.z, a=e.z, b=e.x over v0, v2
+        r = edge_test32(e[Z], e[X], true, v[0][X], v[0][Z], v[2][X], v[2][Z], ae[Z], ae[X], h, clo, V); break;
+      case 2: case 8:  // Z12: a=e.y, b=e.x over v1, v2 on (x, y)
+        r = edge_test32(e[Y], e[X], false, v[1][X], v[1][Y], v[2][X], v[2][Y], ae[Y], ae[X], h, clo, V); break;
+      case 5:          // Z0: over v0, v1
+        r = edge_test32(e[Y], e[X], false, v[0][X], v[0][Y], v[1][X], v[1][Y], ae[Y], ae[X], h, clo, V); break;
+      case 6:          // X2: over v0, v1
+        r = edge_test32(e[Z], e[Y], false, v[0][Y], v[0][Z], v[1][Y], v[1][Z], ae[Z], ae[Y], h, clo, V); break;
+      default:         // 7, Y1: over v0, v1
+        r = edge_test32(e[Z], e[X], true, v[0][X], v[0][Z], v[1][X], v[1][Z], ae[Z], ae[X], h, clo, V); break;
+    }
+    if (r == kTrue) return false;
+    if (r == kUnknown) {
+      need64();
+      if (edge_test64(b64, k, P.hd)) return false;
+    }
+  }
+
+  // plane test: normal = e0 x e1; vmin/vmax by the sign of each component.
+  const float* e0 = P.e[0];
+  const float* e1 = P.e[1];
+  const float m0 = fmul(e0[1], e1[2]), m1 = fmul(e0[2], e1[1]);
+  const float m2 = fmul(e0[2], e1[0]), m3 = fmul(e0[0], e1[2]);
+  const float m4 = fmul(e0[0], e1[1]), m5 = fmul(e0[1], e1[0]);
+  const float n[3] = {fsub(m0, m1), fsub(m2, m3), fsub(m4, m5)};
+  const float sn[3] = {fadd(fabsf_(m0), fabsf_(m1)), fadd(fabsf_(m2), fabsf_(m3)), fadd(fabsf_(m4), fabsf_(m5))};
+  bool plane_unknown = false;
+  float vmin[3], vmax[3], W[3];
+  for (int q = 0; q < 3; ++q) {
+    // |n_f - n*| <= 4.1 u32 sn; fp64 side <= 2^-47 V^2
+    const float tn = fadd(fadd(fmul(4.2f * kU32, sn[q]), fmul(kD64, fmul(V, V))), kTiny);
+    if (n[q] > tn) { vmin[q] = fsub(-h, v[0][q]); vmax[q] = fsub(h, v[0][q]); }
+    else if (n[q] < -tn) { vmin[q] = fsub(h, v[0][q]); vmax[q] = fsub(-h, v[0][q]); }
+    else { plane_unknown = true; break; }
+    W[q] = fmul(fadd(h, fabsf_(v[0][q])), 1.0000003f);
+  }
+  if (!plane_unknown) {
+    // |dot_f - dot*| <= 9.5 u32 sum sn_q (W_q + |v0_q|) + 1.1 clo sum sn_q; fp64 side <= 2^-42 V^2 (V + h)
+    float acc = 0.f, accs = 0.f;
+    for (int q = 0; q < 3; ++q) {
+      acc = fadd(acc, fmul(sn[q], fadd(W[q], fabsf_(v[0][q]))));
+      accs = fadd(accs, sn[q]);
+    }
+    const float td = fadd(fadd(fmul(9.6f * kU32, acc), fmul(1.1f, fmul(clo, accs))),
+                          fadd(fmul(32.f * kD64, fmul(fmul(V, V), fadd(V, h))), kTiny));
+    const float dmin = fadd(fadd(fmul(n[0], vmin[0]), fmul(n[1], vmin[1])), fmul(n[2], vmin[2]));
+    const Tri rmin = gt(dmin, 0.f, td);  // reference: dmin > 0 -> reject
+    if (rmin == kTrue) return false;
+    if (rmin == kFalse) {
+      const float dmax = fadd(fadd(fmul(n[0], vmax[0]), fmul(n[1], vmax[1])), fmul(n[2], vmax[2]));
+      const Tri rmax = gt(dmax, 0.f, td);  // reference: dmax >= 0 -> overlap
+      if (rmax == kTrue) return true;
+      if (rmax == kFalse) return false;
+    }
+  }
+  need64();
+  return !plane_reject64(b64, P.hd);
+}
+
+}  // namespace sat
+}  // namespace svdag

@@ -1,0 +1,145 @@
+// Host-side mirror of SymVox's GeomOctree build surface over the GPU C ABI
+// (include/svdag_gpu.h), plus the reference's node record and the encoders
+// of its output files.
+//
+// GeomOctree keeps the reference's method names and meaning
+// (src/symvox/geom_octree.hpp:106-157); geometry arguments are plain arrays
+// instead of SpaceLand types.  The node pool lives on the GPU and is copied
+// into the reference's NodeData form on the first getNodeData() after a build
+// step, so encoders and other consumers read it exactly as in the reference.
+#pragma once
+
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "svdag_gpu.h"
+
+namespace svdag {
+
+constexpr uint32_t kNullNode = 0xFFFFFFFEu;  // Octree::nullNode (src/symvox/octree.cpp:22)
+
+// Octree::Node + GeomOctree::Node fields (src/symvox/octree.hpp:57-85,
+// src/symvox/geom_octree.hpp:59-96).
+struct Node {
+  uint32_t children[8];
+  uint8_t childrenBitmask = 0;
+  uint32_t childLevels[8];
+  uint8_t childrenMirroredBitmask[3] = {0, 0, 0};
+  uint8_t invariantBitmask = 0;
+  uint8_t outsideMask = 0;
+  Node() {
+    for (int c = 0; c < 8; ++c) { children[c] = kNullNode; childLevels[c] = 0xFFFFFFFFu; }
+  }
+  bool existsChild(int c) const { return (childrenBitmask >> c) & 1u; }
+  bool existsChildPointer(int c) const { return children[c] != kNullNode; }
+  bool getChildMirrorBit(int axis, int c) const { return (childrenMirroredBitmask[axis] >> c) & 1u; }
+  unsigned getNChildren() const { return unsigned(__builtin_popcount(childrenBitmask)); }
+};
+
+typedef std::vector<std::vector<Node>> NodeData;
+
+enum State { S_EMPTY = 0, S_SVO = 1, S_DAG = 2, S_SDAG = 3 };
+
+struct Stats {
+  uint64_t nTotalVoxels = 0, nNodesSVO = 0, nNodesDAG = 0, nNodesSDAG = 0;
+  uint64_t nNodesLastLevSVO = 0, nNodesLastLevDAG = 0, nNodesLastLevSDAG = 0;
+  uint64_t simulatedEncodedSVOSize = 0, nCrossLevelMerged = 0, nMissingCorrespondences = 0;
+  double buildSVOTime = 0, toDAGTime = 0, toSDAGTime = 0, crossMergeTime = 0;  // milliseconds
+};
+
+class Scene;
+
+class GeomOctree {
+ public:
+  explicit GeomOctree(Scene* scene = nullptr, int device = 0);
+  GeomOctree(const GeomOctree& other);  // device-side deep copy
+  GeomOctree& operator=(const GeomOctree&) = delete;
+  ~GeomOctree();
+
+  void setScene(Scene* s) { scene_ = s; }
+  // buildSVO(levels, bbox) (geom_octree.cpp:171-280); bbox = {min xyz, max xyz}
+  void buildSVO(unsigned levels, const double bbox[6]);
+  // buildDAG(levels, stepLevel, bbox): the reference chunks the SVO build for
+  // memory; the GPU builds the whole SVO in HBM, whose reduction gives the same
+  // DAG node counts (geom_octree.cpp:289-435).
+  void buildDAG(unsigned levels, unsigned stepLevel, const double bbox[6]);
+  void toDAG();
+  void toSDAG();
+  unsigned mergeAcrossAllLevels();
+  void initChildLevels();
+  // GeomOctree(NodeData, bbox, rootSide, levels, stats) (geom_octree.cpp:49-60)
+  void importDAG(const NodeData& data, const float bbox[6], double rootSide, uint64_t nVoxels);
+
+  const NodeData& getNodeData() const;
+  Stats getStats() const;
+  State getState() const;
+  unsigned getLevels() const;
+  uint64_t getNVoxels() const;
+  uint64_t getNNodes() const;
+  const float* getSceneBBox() const { return bbox_; }
+  float getRootSide() const { return float(rootSide_); }
+  double getRootSideD() const { return rootSide_; }
+  // resizeSceneBbox (octree.hpp:101-105)
+  void resizeSceneBbox(const float bbox[6]);
+  svdag_ctx* handle() const { return ctx_; }
+
+ private:
+  void check(int status) const;
+  void invalidate() { cached_ = false; }
+  Scene* scene_ = nullptr;
+  svdag_ctx* ctx_ = nullptr;
+  float bbox_[6] = {0, 0, 0, 0, 0, 0};
+  double rootSide_ = 0;
+  mutable NodeData data_;
+  mutable bool cached_ = false;
+};
+
+// ---------------------------------------------------------------------------
+// Output files, byte-compatible with the reference's savers.
+
+// EncodedSVDAG (src/symvox/encoded_svdag.cpp:76-199): absolute u32 pointers,
+// child levels honoured (CSVDAG).
+struct EncodedSVDAG {
+  float bbox[6] = {0, 0, 0, 0, 0, 0};
+  float rootSide = 0;
+  uint32_t levels = 0;
+  uint64_t nNodes = 0;
+  uint32_t firstLeafPtr = 0;
+  std::vector<uint32_t> data;
+  bool encode(const NodeData& d, const float bbox[6], float rootSide, uint64_t nNodes, State st);
+  bool save(const std::string& path) const;
+  size_t getDataSize() const { return data.size() * 4; }
+};
+
+// EncodedUSSVDAG (src/symvox/encoded_ussvdag.cpp:60-170): SVDAG layout with the
+// three mirror masks packed into the node header word.
+struct EncodedUSSVDAG {
+  float bbox[6] = {0, 0, 0, 0, 0, 0};
+  float rootSide = 0;
+  uint32_t levels = 0;
+  uint64_t nNodes = 0;
+  uint32_t firstLeafPtr = 0;
+  std::vector<uint32_t> data;
+  bool encode(const NodeData& d, const float bbox[6], float rootSide, uint64_t nNodes, State st);
+  bool save(const std::string& path) const;
+  size_t getDataSize() const { return data.size() * 4; }
+};
+
+// EncodedSSVDAG (src/symvox/encoded_ssvdag.cpp:84-466): levels reordered by
+// reference count, 4^3 leaf bricks, 16/32-bit pointers with mirror bits.
+struct EncodedSSVDAG {
+  float bbox[6] = {0, 0, 0, 0, 0, 0};
+  float rootSide = 0;
+  uint32_t levels = 0;
+  uint64_t nNodes = 0;
+  std::vector<uint16_t> inner;
+  std::vector<uint8_t> leaves;
+  std::vector<uint32_t> levelOffsets;
+  bool encode(const NodeData& d, const float bbox[6], float rootSide, uint64_t nNodes, State st);
+  bool save(const std::string& path) const;
+  size_t getDataSize() const { return inner.size() * 2 + leaves.size() + levelOffsets.size() * 4; }
+};
+
+}  // namespace svdag

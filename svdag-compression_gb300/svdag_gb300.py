@@ -46,6 +46,8 @@ class _Stats(ctypes.Structure):
         ("sdag_ms", ctypes.c_double),
         ("csv_ms", ctypes.c_double),
         ("gpu_launches", ctypes.c_uint64),
+        ("frontier_pairs", ctypes.c_uint64),
+        ("sat_fallbacks", ctypes.c_uint64),
     ]
 
 
@@ -69,6 +71,10 @@ GPU_SYMBOLS = {
     "svdag_download_level": (_I, [_VP, _U32, _VP, _VP, _VP, _VP]),
     "svdag_get_stats": (_I, [_VP, ctypes.POINTER(_Stats)]),
     "svdag_level_device_ptrs": (_I, [_VP, _U32, _VP, _VP, _VP, _VP]),
+    "svdag_import_begin": (_I, [_VP, _U32, _VP, ctypes.c_double, _U64]),
+    "svdag_import_level": (_I, [_VP, _U32, _U64, _VP, _VP]),
+    "svdag_profile_enable": (_I, [_VP, _I]),
+    "svdag_profile_report": (_I, [_VP, ctypes.c_char_p, _U64]),
 }
 
 HOST_SYMBOLS = {
@@ -78,7 +84,10 @@ HOST_SYMBOLS = {
     "svdag_synth_terrain": (_I, [_U32, _U32, ctypes.c_double, _U64, _VP]),
     "svdag_synth_boxes": (_I, [_VP, _VP, _U64, _VP]),
     "svdag_write_obj": (_I, [ctypes.c_char_p, _VP, _U64, _I]),
+    "svdag_write_encoded": (_I, [ctypes.c_char_p, _I, _U32, _VP, _VP, _VP, ctypes.c_float, _U64, _I]),
 }
+
+FORMATS = {"svdag": 0, "ussvdag": 1, "ssvdag": 2}
 
 _gpu = None
 _host = None
@@ -158,6 +167,19 @@ def write_obj(path, tris, pin_unit_cube=True):
 UNIT_BOX = (0.0, 0.0, 0.0, 1.0, 1.0, 1.0)
 
 
+def write_encoded(path, fmt, pool, n_nodes, state, bbox=UNIT_BOX, root_side=1.0):
+    """Writes a node pool (list of REC arrays) in one of the reference's file
+    formats: "svdag", "ussvdag" or "ssvdag" (also .esvdag from a DAG)."""
+    h = load_host()
+    pool = [np.ascontiguousarray(l, REC) for l in pool]
+    counts = (ctypes.c_uint64 * len(pool))(*[len(l) for l in pool])
+    ptrs = (ctypes.c_void_p * len(pool))(*[l.ctypes.data for l in pool])
+    bb = (ctypes.c_float * 6)(*bbox)
+    r = h.svdag_write_encoded(path.encode(), FORMATS[fmt], len(pool), counts, ptrs, bb, root_side, n_nodes, state)
+    if r != 0:
+        raise SvdagError(r, "cannot encode %s to %s" % (fmt, path))
+
+
 # --------------------------------------------------------------------------
 class Octree:
     """GPU octree with the GeomOctree build surface."""
@@ -223,6 +245,20 @@ class Octree:
         self._check(self._lib.svdag_cross_level_merge(self._h))
         return self.stats()["n_cross_level_merged"]
 
+    def importDAG(self, pool, bbox=UNIT_BOX, root_side=1.0, n_total_voxels=0):
+        """GeomOctree(NodeData, bbox, rootSide, levels, stats): a DAG from host
+        pools (list of REC arrays, or (hdr, children) pairs per level)."""
+        bb = (ctypes.c_float * 6)(*bbox)
+        self._check(self._lib.svdag_import_begin(self._h, len(pool), bb, root_side, n_total_voxels))
+        for l, lev in enumerate(pool):
+            if isinstance(lev, np.ndarray) and lev.dtype == REC:
+                hdr = np.ascontiguousarray(lev["hdr"])
+                ch = np.ascontiguousarray(lev["ch"])
+            else:
+                hdr = np.ascontiguousarray(lev[0], np.uint32)
+                ch = np.ascontiguousarray(lev[1], np.uint32)
+            self._check(self._lib.svdag_import_level(self._h, l, len(hdr), hdr.ctypes.data, ch.ctypes.data))
+
     def clone(self):
         h = ctypes.c_void_p()
         self._check(self._lib.svdag_clone(self._h, ctypes.byref(h)))
@@ -259,3 +295,20 @@ class Octree:
 
     def pool(self):
         return [self.level(l) for l in range(self.getLevels())]
+
+    # per-kernel device timing
+    def profile(self, enable=True):
+        self._check(self._lib.svdag_profile_enable(self._h, 1 if enable else 0))
+
+    def profile_report(self):
+        """{kernel name: (launches, total_ms)} since the last report."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        self._check(self._lib.svdag_profile_report(self._h, buf, len(buf)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, n, ms = line.rsplit(";", 2)
+            out[name] = (int(n), float(ms))
+        return out
+
+    def handle(self):
+        return self._h.value

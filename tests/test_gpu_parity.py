@@ -49,6 +49,31 @@ def test_svo_dag_sdag_match_reference_digests(name):
     s.toSDAG()
     assert s.stats()["n_nodes_sdag"] == g["nNodesSDAG"]
     assert oracle_py.pool_digest(s.pool()) == g["sdag"]["digest"]
+    c = o.clone()
+    assert c.mergeAcrossAllLevels() == g["nCrossLevelMerged"]
+    assert c.stats()["n_nodes"] == g["nNodesCSVDAG"]
+    assert oracle_py.pool_digest(c.pool()) == g["csv"]["digest"]
+
+
+def test_imported_chunked_dag_reduces_like_reference():
+    """A DAG from the reference's chunked OpenMP build (buildDAG, restated by
+    the oracle and pinned by its golden digest) imported through the C ABI
+    (the GeomOctree(NodeData) route) gives the reference's SDAG and CSVDAG."""
+    g = G["terrain129_L9_step1"]
+    ref = oracle_py.OracleOctree()
+    ref.buildDAG(SCENES["terrain129_L9_step1"](), g["levels"], g["step_levels"])
+    ref.initChildLevels()
+    assert oracle_py.pool_digest(ref.pool()) == g["dag"]["digest"]
+    o = sv.Octree()
+    o.importDAG(ref.pool(), n_total_voxels=g["nTotalVoxels"])
+    o.initChildLevels()
+    assert oracle_py.pool_digest(o.pool()) == g["dag"]["digest"]
+    s = o.clone()
+    s.toSDAG()
+    assert oracle_py.pool_digest(s.pool()) == g["sdag"]["digest"]
+    c = o.clone()
+    c.mergeAcrossAllLevels()
+    assert oracle_py.pool_digest(c.pool()) == g["csv"]["digest"]
 
 
 @pytest.mark.parametrize("seed", [1, 2, 3])
@@ -76,6 +101,12 @@ def test_random_scenes_match_oracle(kind, seed):
     s.toSDAG()
     assert first_mismatch(s.pool(), rs.pool()) is None
     assert s.stats()["n_nodes_sdag"] == rs.stats()["n_nodes_sdag"]
+    rc, c = ref.clone(), o.clone()
+    rc.mergeAcrossAllLevels()
+    c.mergeAcrossAllLevels()
+    assert first_mismatch(c.pool(), rc.pool()) is None
+    assert c.stats()["n_cross_level_merged"] == rc.stats()["n_cross_level_merged"]
+    assert c.stats()["n_missing_correspondences"] == rc.stats()["n_missing_correspondences"]
 
 
 def _edge(tris, levels):
@@ -87,6 +118,12 @@ def _edge(tris, levels):
     ref.toDAG()
     o.toDAG()
     assert first_mismatch(o.pool(), ref.pool()) is None
+    ref.initChildLevels()
+    o.initChildLevels()
+    rc, c = ref.clone(), o.clone()
+    rc.mergeAcrossAllLevels()
+    c.mergeAcrossAllLevels()
+    assert first_mismatch(c.pool(), rc.pool()) is None
     ref.toSDAG()
     o.toSDAG()
     assert first_mismatch(o.pool(), ref.pool()) is None
