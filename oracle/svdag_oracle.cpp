@@ -434,7 +434,10 @@ int merge_across_levels(ora_octree* o, uint64_t* n_missing) {
   rebuild(cur_depth);
 
   std::set<uint32_t> check, next;
-  for (uint32_t i = 0; i < o->d[1].size(); ++i) check.insert(i);
+  // (a one-level tree has no level 1; the reference indexes past its levels
+  // there, so the restatement merges nothing)
+  if (L >= 2)
+    for (uint32_t i = 0; i < o->d[1].size(); ++i) check.insert(i);
   std::vector<std::map<uint32_t, std::pair<uint32_t, uint32_t>>> corr(L), visited(L);
   for (uint32_t levA = 1; levA < L; ++levA) {
     uint32_t max_depth = L - levA - 1;

@@ -25,7 +25,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["api.cu", "voxelize.cu", "reduce.cu", "csvdag.cu"]
-HOST_SOURCES = ["synth.cpp", "encoders.cpp"]
+HOST_SOURCES = ["synth.cpp", "encoders.cpp", "scene.cpp", "geom_octree.cpp"]
 
 
 def _run(cmd, cwd=None):
@@ -67,11 +67,23 @@ def build_gpu(jobs=8):
 def build_host():
     os.makedirs(LIB, exist_ok=True)
     srcs = [os.path.join(PKG, "host", s) for s in HOST_SOURCES]
-    hdrs = [os.path.join(PKG, "host", h) for h in os.listdir(os.path.join(PKG, "host")) if h.endswith(".h")]
+    hdrs = [os.path.join(PKG, "host", h) for h in os.listdir(os.path.join(PKG, "host")) if h.endswith((".h", ".hpp"))]
     out = os.path.join(LIB, "libsvdag_host.so")
-    if not _newer(out, srcs + hdrs):
+    if not _newer(out, srcs + hdrs + [os.path.join(LIB, "libsvdag_gpu.so")]):
         _run([CXX, "-O2", "-std=gnu++17", "-fPIC", "-shared", "-ffp-contract=off", "-I", INC,
-              "-I", os.path.join(PKG, "host")] + srcs + ["-o", out])
+              "-I", os.path.join(PKG, "host")] + srcs + ["-L", LIB, "-lsvdag_gpu", "-Wl,-rpath,$ORIGIN", "-o", out])
+    return out
+
+
+def build_cli(gpu_lib):
+    """svbuilder executable (the reference CLI over the GPU path)."""
+    os.makedirs(os.path.join(PKG, "bin"), exist_ok=True)
+    srcs = [os.path.join(PKG, "host", s) for s in HOST_SOURCES + ["svbuilder.cpp"]]
+    hdrs = [os.path.join(PKG, "host", h) for h in os.listdir(os.path.join(PKG, "host")) if h.endswith((".h", ".hpp"))]
+    out = os.path.join(PKG, "bin", "svbuilder")
+    if not _newer(out, srcs + hdrs + [gpu_lib]):
+        _run([CXX, "-O2", "-std=gnu++17", "-ffp-contract=off", "-I", INC, "-I", os.path.join(PKG, "host")] + srcs +
+             ["-L", LIB, "-lsvdag_gpu", "-Wl,-rpath,$ORIGIN/../lib", "-o", out])
     return out
 
 
@@ -97,10 +109,12 @@ def build_reference():
 def build_all(with_reference=True):
     with ThreadPoolExecutor(4) as ex:
         fg = ex.submit(build_gpu)
+        fg.result()
         fh = ex.submit(build_host)
         fo = ex.submit(build_oracle)
         fr = ex.submit(build_reference) if with_reference else None
         res = {"gpu": fg.result(), "host": fh.result(), "oracle": fo.result()}
+        res["cli"] = build_cli(res["gpu"])
         if fr is not None:
             res["reference"] = fr.result()
     return res

@@ -15,6 +15,7 @@ namespace svdag {
 //   inv[n]      : invariant mask (SDAG only; empty otherwise)
 //   clev[8n]    : child levels (CSVDAG only; empty otherwise)
 //   ctr[3n]     : fp64 node centre (SVO build only)
+//   nbox[8n]    : fp32 child-box centres of the node (SVO build only)
 struct Level {
   uint64_t n = 0;
   DBuf<uint32_t> hdr;
@@ -22,6 +23,7 @@ struct Level {
   DBuf<uint8_t> inv;
   DBuf<uint8_t> clev;
   DBuf<double> ctr;
+  DBuf<float> nbox;
 };
 
 struct Ctx {

@@ -169,17 +169,42 @@ SAT_HD bool tri_box64(const float t[9], const double c[3], double h) {
 // ---------------------------------------------------------------------------
 // fp32 filter.
 
+// Per node: the centres of its 8 child boxes, c_q + (+-k) per axis, as the
+// fp32 head of each coordinate and the largest tail.  Computed once per node
+// in fp64 (the reference's child-centre values, geom_octree.cpp:222-230).
+struct NodeBoxes {
+  float chi[6];  // index 2*q + s: fl32(c_q + (s ? k : -k))
+  float clo;     // max |(c_q +- k) - chi|, inflated
+  float ok;      // 1 when the fp32 path may be used for this node
+};
+
+SAT_HD void node_boxes(const double c[3], double k, NodeBoxes& nb) {
+  float clo = 0.f;
+  bool ok = (k > 1.0e-30) && (k < 1.0e18) && (double(float(k)) == k);
+  for (int q = 0; q < 3; ++q) {
+    for (int s = 0; s < 2; ++s) {
+      const double cd = dadd(c[q], s ? k : -k);
+      const float hi = float(cd);
+      nb.chi[2 * q + s] = hi;
+      const float alo = float(fabs_(dsub(cd, double(hi))));
+      clo = (alo > clo) ? alo : clo;
+      ok = ok && (fabs_(cd) < 1.0e18);
+    }
+  }
+  nb.clo = clo * 1.0000002f;
+  nb.ok = ok ? 1.f : 0.f;
+}
+
 // Per (triangle, parent node) data shared by the 8 children.
 struct Pair32 {
   float t[9];        // triangle (exact)
   float e[3][3];     // fp32 edges  t1-t0, t2-t1, t0-t2 (edge, axis)
   float ae[3][3];    // |e|
-  double cd[3][2];   // child centre coordinate per axis and side (fp64, reference values)
-  float chi[3][2];   // fl32(cd)
-  float clo;         // max |cd - chi| over axes and sides
-  float h;           // child half side (exact in fp32)
-  double hd;
+  NodeBoxes nb;
+  float h;           // child half side (exact in fp32 when nb.ok)
   bool fast;         // fp32 path usable (finite, moderate magnitudes)
+  const double* c;   // parent centre (fp64), for predicates decided in fp64
+  double k;          // child half side (fp64)
 };
 
 // Decides x > y from fp32 values with a tolerance; kUnknown inside it.
@@ -201,36 +226,25 @@ SAT_HD Tri tri_or(Tri a, Tri b) {
   return kUnknown;
 }
 
-// Builds the per-pair data; c = parent centre, k = child half side.
-SAT_HD void pair_setup(const float t[9], const double c[3], double k, Pair32& P) {
-  for (int i = 0; i < 9; ++i) P.t[i] = t[i];
-  bool ok = true;
-  for (int i = 0; i < 9; ++i) ok = ok && (fabsf_(t[i]) < 1.0e18f);  // also false for NaN
-  float clo = 0.f;
-  for (int q = 0; q < 3; ++q) {
-    // child centre = parent centre + (+-k), as geom_octree.cpp:222-230
-    P.cd[q][0] = dadd(c[q], -k);
-    P.cd[q][1] = dadd(c[q], k);
-    for (int s = 0; s < 2; ++s) {
-      const float hi = float(P.cd[q][s]);
-      P.chi[q][s] = hi;
-      const double lo = dsub(P.cd[q][s], double(hi));
-      const float alo = float(fabs_(lo));
-      clo = (alo > clo) ? alo : clo;
-      ok = ok && (fabs_(P.cd[q][s]) < 1.0e18);
-    }
+// Builds the per-pair data; c = parent centre (fp64, kept by pointer),
+// nb = the node's child boxes, k = child half side.
+SAT_HD void pair_setup(const float t[9], const double* c, const NodeBoxes& nb, double k, Pair32& P) {
+  bool ok = nb.ok != 0.f;
+  for (int i = 0; i < 9; ++i) {
+    P.t[i] = t[i];
+    ok = ok && (fabsf_(t[i]) < 1.0e18f);  // also false for NaN
   }
-  P.clo = clo * 1.0000002f;
   for (int q = 0; q < 3; ++q) {
     P.e[0][q] = fsub(t[3 + q], t[q]);
     P.e[1][q] = fsub(t[6 + q], t[3 + q]);
     P.e[2][q] = fsub(t[q], t[6 + q]);
     for (int j = 0; j < 3; ++j) P.ae[j][q] = fabsf_(P.e[j][q]);
   }
-  P.hd = k;
+  P.nb = nb;
   P.h = float(k);
-  ok = ok && (double(P.h) == k) && (k > 1.0e-30) && (k < 1.0e18);
   P.fast = ok;
+  P.c = c;
+  P.k = k;
 }
 
 // One edge-axis test in fp32: reject (kTrue), keep (kFalse) or kUnknown.
@@ -262,17 +276,23 @@ SAT_HD Tri edge_test32(float a, float b, bool neg_a, float u0, float w0, float u
 // true when the child box overlaps the triangle; `fallbacks` counts the
 // predicates that needed fp64.
 SAT_HD bool child_overlap(const Pair32& P, int ci, unsigned* fallbacks) {
-  const int sx = (ci >> 2) & 1, sy = (ci >> 1) & 1, sz = ci & 1;
-  const double c[3] = {P.cd[0][sx], P.cd[1][sy], P.cd[2][sz]};
+  const bool sx = (ci >> 2) & 1, sy = (ci >> 1) & 1, sz = ci & 1;
+  auto centre64 = [&](double c[3]) {
+    c[0] = dadd(P.c[0], sx ? P.k : -P.k);
+    c[1] = dadd(P.c[1], sy ? P.k : -P.k);
+    c[2] = dadd(P.c[2], sz ? P.k : -P.k);
+  };
   if (!P.fast) {
     if (fallbacks) ++*fallbacks;
-    return tri_box64(P.t, c, P.hd);
+    double c[3];
+    centre64(c);
+    return tri_box64(P.t, c, P.k);
   }
   const float h = P.h;
-  const float clo = P.clo;
+  const float clo = P.nb.clo;
   // fp32 vertex offsets v = t - fl32(c); |v_f - (t - c)| <= 1.01 u32 |v_f| + 1.01 clo
   float v[3][3];
-  const float chi[3] = {P.chi[0][sx], P.chi[1][sy], P.chi[2][sz]};
+  const float chi[3] = {sx ? P.nb.chi[1] : P.nb.chi[0], sy ? P.nb.chi[3] : P.nb.chi[2], sz ? P.nb.chi[5] : P.nb.chi[4]};
   float V = 0.f;
   for (int i = 0; i < 3; ++i)
     for (int q = 0; q < 3; ++q) {
@@ -285,7 +305,12 @@ SAT_HD bool child_overlap(const Pair32& P, int ci, unsigned* fallbacks) {
   Box64 b64;
   bool have64 = false;
   auto need64 = [&]() {
-    if (!have64) { box64(P.t, c, b64); have64 = true; }
+    if (!have64) {
+      double c[3];
+      centre64(c);
+      box64(P.t, c, b64);
+      have64 = true;
+    }
     if (fallbacks) ++*fallbacks;
   };
 
@@ -302,7 +327,7 @@ SAT_HD bool child_overlap(const Pair32& P, int ci, unsigned* fallbacks) {
     if (r == kTrue) return false;
     if (r == kUnknown) {
       need64();
-      if (aabb_reject64(b64, q, P.hd)) return false;
+      if (aabb_reject64(b64, q, P.k)) return false;
     }
   }
 
@@ -330,7 +355,7 @@ SAT_HD bool child_overlap(const Pair32& P, int ci, unsigned* fallbacks) {
     if (r == kTrue) return false;
     if (r == kUnknown) {
       need64();
-      if (edge_test64(b64, k, P.hd)) return false;
+      if (edge_test64(b64, k, P.k)) return false;
     }
   }
 
@@ -372,7 +397,7 @@ SAT_HD bool child_overlap(const Pair32& P, int ci, unsigned* fallbacks) {
     }
   }
   need64();
-  return !plane_reject64(b64, P.hd);
+  return !plane_reject64(b64, P.k);
 }
 
 }  // namespace sat

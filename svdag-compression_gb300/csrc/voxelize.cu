@@ -45,7 +45,7 @@ __host__ __device__ __forceinline__ double child_half_side(double root_side, uin
 __global__ void __launch_bounds__(256) k_expand(VoxParams P, const float* __restrict__ tris,
                                                 const uint32_t* __restrict__ f_tri, const uint32_t* __restrict__ f_node,
                                                 uint64_t F, const double* __restrict__ ctr,
-                                                uint32_t* __restrict__ hdr, uint32_t* __restrict__ firstq,
+                                                const float* __restrict__ nbox, uint32_t* __restrict__ hdr, uint32_t* __restrict__ firstq,
                                                 uint8_t* __restrict__ hits_out, unsigned long long* __restrict__ n_fallback) {
   const double k = child_half_side(P.root_side, P.level);
   const bool leaf = (P.level == P.leaf_level);
@@ -57,9 +57,15 @@ __global__ void __launch_bounds__(256) k_expand(VoxParams P, const float* __rest
     const float* tp = tris + 9ull * t;
 #pragma unroll
     for (int j = 0; j < 9; ++j) tri[j] = tp[j];
-    const double c[3] = {ctr[3ull * node], ctr[3ull * node + 1], ctr[3ull * node + 2]};
+    sat::NodeBoxes nb;
+    {
+      const float4* p = reinterpret_cast<const float4*>(nbox + 8ull * node);
+      const float4 a = p[0], b = p[1];
+      nb.chi[0] = a.x; nb.chi[1] = a.y; nb.chi[2] = a.z; nb.chi[3] = a.w;
+      nb.chi[4] = b.x; nb.chi[5] = b.y; nb.clo = b.z; nb.ok = b.w;
+    }
     sat::Pair32 PP;
-    sat::pair_setup(tri, c, k, PP);
+    sat::pair_setup(tri, ctr + 3ull * node, nb, k, PP);
     uint32_t h = 0;
 #pragma unroll 1
     for (int i = 7; i >= 0; --i)
@@ -109,7 +115,8 @@ struct U64to32Out {
 // parent centre + (+-k) per axis (geom_octree.cpp:222-230).
 __global__ void k_assign_children(const uint32_t* __restrict__ firstq, uint64_t slots, const uint32_t* __restrict__ bitmap,
                                   const uint32_t* __restrict__ woff, const double* __restrict__ ctr, double k,
-                                  uint32_t* __restrict__ ch, double* __restrict__ child_ctr) {
+                                  double k_next, uint32_t* __restrict__ ch, double* __restrict__ child_ctr,
+                                  float* __restrict__ child_nbox) {
   for (uint64_t s = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; s < slots; s += uint64_t(gridDim.x) * blockDim.x) {
     const uint32_t fq = firstq[s];
     if (fq == kNone) { ch[s] = kNull; continue; }
@@ -119,9 +126,16 @@ __global__ void k_assign_children(const uint32_t* __restrict__ firstq, uint64_t 
     ch[s] = rank;
     const uint64_t p = s >> 3;
     const uint32_t i = uint32_t(s & 7);
-    child_ctr[3ull * rank + 0] = __dadd_rn(ctr[3 * p + 0], (i & 4) ? k : -k);
-    child_ctr[3ull * rank + 1] = __dadd_rn(ctr[3 * p + 1], (i & 2) ? k : -k);
-    child_ctr[3ull * rank + 2] = __dadd_rn(ctr[3 * p + 2], (i & 1) ? k : -k);
+    const double cc[3] = {__dadd_rn(ctr[3 * p + 0], (i & 4) ? k : -k), __dadd_rn(ctr[3 * p + 1], (i & 2) ? k : -k),
+                          __dadd_rn(ctr[3 * p + 2], (i & 1) ? k : -k)};
+    child_ctr[3ull * rank + 0] = cc[0];
+    child_ctr[3ull * rank + 1] = cc[1];
+    child_ctr[3ull * rank + 2] = cc[2];
+    sat::NodeBoxes nb;
+    sat::node_boxes(cc, k_next, nb);
+    float4* q = reinterpret_cast<float4*>(child_nbox + 8ull * rank);
+    q[0] = make_float4(nb.chi[0], nb.chi[1], nb.chi[2], nb.chi[3]);
+    q[1] = make_float4(nb.chi[4], nb.chi[5], nb.clo, nb.ok);
   }
 }
 
@@ -203,8 +217,19 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
   c.lev[0].n = 1;
   c.lev[0].hdr.alloc(1, st);
   c.lev[0].ctr.alloc(3, st);
+  c.lev[0].nbox.alloc(8, st);
   SVDAG_CUDA(cudaMemsetAsync(c.lev[0].hdr.get(), 0, 4, st));
   SVDAG_CUDA(cudaMemcpyAsync(c.lev[0].ctr.get(), P.root_c, 24, cudaMemcpyHostToDevice, st));
+  {
+    sat::NodeBoxes nb;
+    sat::node_boxes(P.root_c, child_half_side(c.root_side, 0), nb);
+    static thread_local float root_nb[8];
+    for (int k = 0; k < 6; ++k) root_nb[k] = nb.chi[k];
+    root_nb[6] = nb.clo;
+    root_nb[7] = nb.ok;
+    SVDAG_CUDA(cudaMemcpyAsync(c.lev[0].nbox.get(), root_nb, 32, cudaMemcpyHostToDevice, st));
+    SVDAG_CUDA(cudaStreamSynchronize(st));
+  }
 
   DBuf<uint32_t> f_tri, f_node;  // frontier; empty at level 0 (implicit (t, root))
   uint64_t F = c.n_tris;
@@ -227,7 +252,7 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
     }
     if (F)
       SVDAG_LAUNCH(ex, k_expand, grid_for(ex, F, 256, 32), 256, 0, P, c.tris, f_tri.get(), f_node.get(), F,
-                   L.ctr.get(), L.hdr.get(), firstq.get(), hits.get(), d_fb.get());
+                   L.ctr.get(), L.nbox.get(), L.hdr.get(), firstq.get(), hits.get(), d_fb.get());
     if (leaf) break;
 
     // --- create level l+1 in reference creation order
@@ -244,9 +269,11 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
     L.ch.alloc(slots, st);
     N.hdr.alloc(n_next ? n_next : 1, st);
     N.ctr.alloc(3 * (n_next ? n_next : 1), st);
+    N.nbox.alloc(8 * (n_next ? n_next : 1), st);
     SVDAG_CUDA(cudaMemsetAsync(N.hdr.get(), 0, 4 * (n_next ? n_next : 1), st));
     SVDAG_LAUNCH(ex, k_assign_children, grid_for(ex, slots, 256), 256, 0, firstq.get(), slots, bitmap.get(),
-                 woff.get(), L.ctr.get(), child_half_side(c.root_side, l), L.ch.get(), N.ctr.get());
+                 woff.get(), L.ctr.get(), child_half_side(c.root_side, l), child_half_side(c.root_side, l + 1),
+                 L.ch.get(), N.ctr.get(), N.nbox.get());
     firstq.release();
     bitmap.release();
     woff.release();
@@ -274,7 +301,10 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
       SVDAG_LAUNCH(ex, k_clean_empty, grid_for(ex, P_.n, 256), 256, 0, P_.hdr.get(), P_.ch.get(), P_.n,
                    c.lev[lev].hdr.get());
   }
-  for (auto& L : c.lev) L.ctr.release();
+  for (auto& L : c.lev) {
+    L.ctr.release();
+    L.nbox.release();
+  }
 
   SVDAG_CUDA(cudaMemsetAsync(d_vox.get(), 0, 8, st));
   const Level& LL = c.lev[levels - 1];

@@ -91,6 +91,72 @@ bool EncodedSVDAG::save(const std::string& path) const {
   return bool(f);
 }
 
+bool EncodedSVDAG::load(const std::string& path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) return false;
+  uint32_t nn = 0, count = 0;
+  f.read(reinterpret_cast<char*>(bbox), 12);
+  f.read(reinterpret_cast<char*>(bbox + 3), 12);
+  f.read(reinterpret_cast<char*>(&rootSide), 4);
+  f.read(reinterpret_cast<char*>(&levels), 4);
+  f.read(reinterpret_cast<char*>(&nn), 4);
+  f.read(reinterpret_cast<char*>(&firstLeafPtr), 4);
+  f.read(reinterpret_cast<char*>(&count), 4);
+  nNodes = nn;
+  data.resize(count);
+  f.read(reinterpret_cast<char*>(data.data()), std::streamsize(4) * count);
+  return bool(f) && levels >= 1;
+}
+
+NodeData EncodedSVDAG::decode() const {
+  NodeData d(levels);
+  // pass 1: walk the stream; a level ends where the smallest child pointer
+  // of the level above begins; remember the pointer words before each node
+  std::vector<uint64_t> level_start(levels, ~0ull);
+  level_start[0] = 0;
+  std::vector<std::vector<std::pair<uint32_t, uint32_t>>> ptrs_before(levels);  // (position, pointers before)
+  uint32_t lev = 0;
+  uint32_t nptr = 0;
+  for (uint64_t i = 0; i < data.size(); ++i) {
+    if (lev + 1 < levels && i == level_start[lev + 1]) { ++lev; nptr = 0; }
+    Node n;
+    n.childrenBitmask = uint8_t(data[i]);
+    ptrs_before[lev].push_back(std::make_pair(uint32_t(i), nptr));
+    if (lev + 1 < levels) {
+      int k = 0;
+      for (int c = 7; c >= 0; --c)
+        if (n.existsChild(c)) {
+          n.children[c] = data[i + 1 + k];
+          ++k;
+          if (n.children[c] < level_start[lev + 1]) level_start[lev + 1] = n.children[c];
+        }
+      i += k;
+      nptr += k;
+    }
+    d[lev].push_back(n);
+  }
+  // pass 2: absolute positions -> per-level indices
+  uint64_t start = 0;
+  for (uint32_t l = 0; l + 1 < levels; ++l) {
+    start += d[l].size();
+    for (const Node& n : d[l]) start += n.getNChildren();
+    const auto& pb = ptrs_before[l + 1];
+    for (Node& n : d[l]) {
+      for (int c = 0; c < 8; ++c) {
+        if (!n.existsChild(c)) { n.children[c] = kNullNode; continue; }
+        const uint32_t pos = n.children[c];
+        auto it = std::lower_bound(pb.begin(), pb.end(), std::make_pair(pos, 0u),
+                                   [](const std::pair<uint32_t, uint32_t>& a, const std::pair<uint32_t, uint32_t>& b) {
+                                     return a.first < b.first;
+                                   });
+        const uint32_t before = (it != pb.end() && it->first == pos) ? it->second : 0u;
+        n.children[c] = uint32_t(pos - start - before);
+      }
+    }
+  }
+  return d;
+}
+
 bool EncodedUSSVDAG::encode(const NodeData& d, const float bb[6], float rs, uint64_t nn, State st) {
   if (st != S_SDAG) return false;  // encoded_ussvdag.cpp:90-93
   std::memcpy(bbox, bb, sizeof(bbox));

@@ -111,6 +111,11 @@ struct EncodedSVDAG {
   bool encode(const NodeData& d, const float bbox[6], float rootSide, uint64_t nNodes, State st);
   bool save(const std::string& path) const;
   size_t getDataSize() const { return data.size() * 4; }
+  // EncodedSVDAG::load / decode (encoded_svdag.cpp:44-74, 217-281): the
+  // stream back into per-level nodes (same-level pointers only, as the
+  // reference's decoder).
+  bool load(const std::string& path);
+  NodeData decode() const;
 };
 
 // EncodedUSSVDAG (src/symvox/encoded_ussvdag.cpp:60-170): SVDAG layout with the

@@ -18,8 +18,10 @@ static uint64_t g_cases = 0, g_mis = 0, g_hits = 0;
 static unsigned g_fb = 0;
 
 static void check(const float t[9], const double pc[3], double k) {
+  NodeBoxes nb;
+  node_boxes(pc, k, nb);
   Pair32 P;
-  pair_setup(t, pc, k, P);
+  pair_setup(t, pc, nb, k, P);
   for (int ci = 0; ci < 8; ++ci) {
     const double c[3] = {pc[0] + ((ci & 4) ? k : -k), pc[1] + ((ci & 2) ? k : -k), pc[2] + ((ci & 1) ? k : -k)};
     const bool want = ora_tri_box(c, k, t) != 0;

@@ -120,10 +120,11 @@ def _edge(tris, levels):
     assert first_mismatch(o.pool(), ref.pool()) is None
     ref.initChildLevels()
     o.initChildLevels()
-    rc, c = ref.clone(), o.clone()
-    rc.mergeAcrossAllLevels()
-    c.mergeAcrossAllLevels()
-    assert first_mismatch(c.pool(), rc.pool()) is None
+    if levels >= 2:  # the reference's merge indexes level 1, which a 1-level tree lacks
+        rc, c = ref.clone(), o.clone()
+        rc.mergeAcrossAllLevels()
+        c.mergeAcrossAllLevels()
+        assert first_mismatch(c.pool(), rc.pool()) is None
     ref.toSDAG()
     o.toSDAG()
     assert first_mismatch(o.pool(), ref.pool()) is None
