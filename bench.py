@@ -251,6 +251,7 @@ def run_ours(args, rank, local, world):
                    "nodes_sdag": int(sst["n_nodes_sdag"]),
                    "nodes_csvdag": int(cst["n_nodes"]) if cst else None,
                    "csvdag_in_step": bool(have_csv),
+                   "frontier_pairs": int(info["frontier"][0]), "sat_fp64_fallbacks": int(info["sat_fallbacks"]),
                    "l2": "inputs larger than L2 (triangles 302 MB, node pools > 129 MB)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clk, "gpu_launches": int(launches), "roofline": roof, "e2e": e2e,
@@ -269,11 +270,12 @@ def level_info(sv, base, s_last, levels):
     o.buildSVO(levels)
     svo = [o.level_count(l) for l in range(levels)]
     pairs = o.stats()["frontier_pairs"]
+    fallbacks = o.stats()["sat_fallbacks"]
     o.toDAG()
     dag = [o.level_count(l) for l in range(levels)]
     o.close()
     return {"svo": svo, "dag": dag, "svo_inner": svo[1:-1], "dag_inner": dag[1:-1], "frontier": [pairs],
-            "sdag": [s_last.level_count(l) for l in range(levels)]}
+            "sdag": [s_last.level_count(l) for l in range(levels)], "sat_fallbacks": fallbacks}
 
 
 def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):

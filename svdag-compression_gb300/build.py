@@ -24,6 +24,8 @@ REFERENCE = "/root/reference"
 NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# extra nvcc flags (e.g. tuning macros), whitespace separated
+EXTRA_NVCC = os.environ.get("SVDAG_NVCC_FLAGS", "").split()
 CU_SOURCES = ["api.cu", "voxelize.cu", "reduce.cu", "csvdag.cu"]
 HOST_SOURCES = ["synth.cpp", "encoders.cpp", "scene.cpp", "geom_octree.cpp"]
 
@@ -48,7 +50,7 @@ def _cu_object(src):
     deps = [s] + [os.path.join(PKG, "csrc", h) for h in os.listdir(os.path.join(PKG, "csrc")) if h.endswith(".cuh")]
     deps.append(os.path.join(INC, "svdag_gpu.h"))
     if not _newer(o, deps):
-        _run([NVCC] + ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC,
+        _run([NVCC] + ARCH + EXTRA_NVCC + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC,
                               "-I", os.path.join(PKG, "csrc"), "-c", s, "-o", o])
     return o
 

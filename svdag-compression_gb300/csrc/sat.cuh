@@ -34,8 +34,15 @@
 
 #if defined(__CUDACC__)
 #define SAT_HD __host__ __device__ __forceinline__
+#define SAT_COLD __host__ __device__ __noinline__
 #else
 #define SAT_HD inline
+#define SAT_COLD inline
+#endif
+
+// Optional per-predicate fallback hook (profiling builds); no-op by default.
+#ifndef SVDAG_FB_HOOK
+#define SVDAG_FB_HOOK(which) ((void)0)
 #endif
 
 namespace svdag {
@@ -50,6 +57,7 @@ SAT_HD double dsub(double a, double b) { return __dsub_rn(a, b); }
 SAT_HD double dmul(double a, double b) { return __dmul_rn(a, b); }
 SAT_HD float fabsf_(float a) { return fabsf(a); }
 SAT_HD double fabs_(double a) { return fabs(a); }
+SAT_HD float ffma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 #else
 SAT_HD float fadd(float a, float b) { return a + b; }
 SAT_HD float fsub(float a, float b) { return a - b; }
@@ -59,6 +67,7 @@ SAT_HD double dsub(double a, double b) { return a - b; }
 SAT_HD double dmul(double a, double b) { return a * b; }
 SAT_HD float fabsf_(float a) { return std::fabs(a); }
 SAT_HD double fabs_(double a) { return std::fabs(a); }
+SAT_HD float ffma(float a, float b, float c) { return std::fma(a, b, c); }
 #endif
 
 constexpr float kU32 = 5.9604644775390625e-08f;  // 2^-24
@@ -166,6 +175,165 @@ SAT_HD bool tri_box64(const float t[9], const double c[3], double h) {
   return !plane_reject64(b, h);
 }
 
+// One predicate of child `ci` of a pair in fp64, from scratch (rare path):
+// which = 0..2 bounding-box axis, 3..11 edge-axis test which-3, 12 plane,
+// -1 the whole test (returns !overlap).  Returns "reject".
+SAT_COLD bool pred64(const float* t, const double* pc, double k, int ci, int which) {
+  const double c[3] = {dadd(pc[0], (ci & 4) ? k : -k), dadd(pc[1], (ci & 2) ? k : -k),
+                       dadd(pc[2], (ci & 1) ? k : -k)};
+  float tt[9];
+  for (int i = 0; i < 9; ++i) tt[i] = t[i];
+  if (which < 0) return !tri_box64(tt, c, k);
+  Box64 b;
+  box64(tt, c, b);
+  if (which < 3) return aabb_reject64(b, which, k);
+  if (which < 12) return edge_test64(b, which - 3, k);
+  return plane_reject64(b, k);
+}
+
+// ---------------------------------------------------------------------------
+// Exact-arithmetic tier.  A predicate the error bound leaves undecided is
+// re-evaluated in fp32 with error-free transformations: TwoSum gives the
+// exact rounding error of an addition, an FMA residual that of a product.
+// When every operation of the predicate is exact, the fp32 value is the real
+// value of the expression on the exact inputs; the reference's fp64
+// evaluation of the same expression then rounds nothing either (every fp32
+// value is an fp64 value), so both make the same comparison of the same real
+// numbers.  Typical case: triangles lying on octree grid planes (ties).
+
+SAT_HD bool xsub(float a, float b, float& s) {  // s = fl(a - b); exact?
+  s = fsub(a, b);
+  const float bv = fsub(s, a);
+  const float av = fsub(s, bv);
+  return fadd(fsub(a, av), fsub(-b, bv)) == 0.f;
+}
+SAT_HD bool xmul(float a, float b, float& p) {  // p = fl(a * b); exact?
+  p = fmul(a, b);
+  if (p == 0.f) return a == 0.f || b == 0.f;
+  if (fabsf_(p) < 1.0e-30f) return false;  // keep the residual out of the subnormal range
+  return ffma(a, b, -p) == 0.f;
+}
+
+// which = 0..2 bounding-box axis, 3..11 edge-axis test which-3, 12 plane.
+// kTrue = the reference rejects the box, kFalse = it does not, kUnknown = some
+// operation was inexact.  c = the child centre, exact in fp32.
+SAT_COLD int exact32(const float* tg, float cx, float cy, float cz, float h, int which) {
+  float t[9];
+  for (int i = 0; i < 9; ++i) t[i] = tg[i];
+  const float c[3] = {cx, cy, cz};
+  float v[3][3];
+  bool ok = true;
+  if (which < 3) {  // one axis only
+    const int q = which;
+    for (int i = 0; i < 3; ++i) ok = xsub(t[3 * i + q], c[q], v[i][q]) && ok;
+    if (!ok) return kUnknown;
+    float mn = v[0][q], mx = v[0][q];
+    for (int i = 1; i < 3; ++i) { mn = (v[i][q] < mn) ? v[i][q] : mn; mx = (v[i][q] > mx) ? v[i][q] : mx; }
+    return (mn > h || mx < -h) ? kTrue : kFalse;
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int q = 0; q < 3; ++q) ok = xsub(t[3 * i + q], c[q], v[i][q]) && ok;
+  if (!ok) return kUnknown;
+  // edges from the vertex offsets, as the reference forms them (e0 = v1 - v0, ...)
+  float e[3][3];
+  for (int q = 0; q < 3; ++q) {
+    ok = xsub(v[1][q], v[0][q], e[0][q]) && ok;
+    ok = xsub(v[2][q], v[1][q], e[1][q]) && ok;
+    ok = xsub(v[0][q], v[2][q], e[2][q]) && ok;
+  }
+  if (!ok) return kUnknown;
+  if (which < 12) {
+    const int k = which - 3, j = k / 3;
+    // (a axis, b axis, u axis, w axis, vertex pair, negated) per test, as
+    // AXISTEST_X01/X2 (a=e.z b=e.y on y,z), Y02/Y1 (-a*x + b*z, a=e.z b=e.x),
+    // Z12/Z0 (a=e.y b=e.x on x,y)
+    int aa, bb, ua, wa, i0, i1;
+    bool neg = false;
+    switch (k) {
+      case 0: case 3: aa = 2; bb = 1; ua = 1; wa = 2; i0 = 0; i1 = 2; break;
+      case 1: case 4: aa = 2; bb = 0; ua = 0; wa = 2; i0 = 0; i1 = 2; neg = true; break;
+      case 2: case 8: aa = 1; bb = 0; ua = 0; wa = 1; i0 = 1; i1 = 2; break;
+      case 5: aa = 1; bb = 0; ua = 0; wa = 1; i0 = 0; i1 = 1; break;
+      case 6: aa = 2; bb = 1; ua = 1; wa = 2; i0 = 0; i1 = 1; break;
+      default: aa = 2; bb = 0; ua = 0; wa = 2; i0 = 0; i1 = 1; neg = true; break;
+    }
+    const float a = e[j][aa], b = e[j][bb];
+    float x0, y0, x1, y1, p0, p1, sab, rad;
+    ok = xmul(a, v[i0][ua], x0) && ok;
+    ok = xmul(b, v[i0][wa], y0) && ok;
+    ok = xmul(a, v[i1][ua], x1) && ok;
+    ok = xmul(b, v[i1][wa], y1) && ok;
+    ok = xsub(x0, y0, p0) && ok;
+    ok = xsub(x1, y1, p1) && ok;
+    ok = xsub(fabsf_(a), -fabsf_(b), sab) && ok;
+    ok = xmul(sab, h, rad) && ok;
+    if (!ok) return kUnknown;
+    if (neg) { p0 = -p0; p1 = -p1; }
+    return ((p0 > rad && p1 > rad) || (p0 < -rad && p1 < -rad)) ? kTrue : kFalse;
+  }
+  // plane test: n = e0 x e1, box corners by the sign of n, two dot products
+  float m[6], n[3];
+  ok = xmul(e[0][1], e[1][2], m[0]) && ok;
+  ok = xmul(e[0][2], e[1][1], m[1]) && ok;
+  ok = xmul(e[0][2], e[1][0], m[2]) && ok;
+  ok = xmul(e[0][0], e[1][2], m[3]) && ok;
+  ok = xmul(e[0][0], e[1][1], m[4]) && ok;
+  ok = xmul(e[0][1], e[1][0], m[5]) && ok;
+  ok = xsub(m[0], m[1], n[0]) && ok;
+  ok = xsub(m[2], m[3], n[1]) && ok;
+  ok = xsub(m[4], m[5], n[2]) && ok;
+  if (!ok) return kUnknown;
+  float vmin[3], vmax[3];
+  for (int q = 0; q < 3; ++q) {
+    if (n[q] > 0.f) { ok = xsub(-h, v[0][q], vmin[q]) && ok; ok = xsub(h, v[0][q], vmax[q]) && ok; }
+    else            { ok = xsub(h, v[0][q], vmin[q]) && ok; ok = xsub(-h, v[0][q], vmax[q]) && ok; }
+  }
+  float d[3], s1, dmin, dmax;
+  for (int q = 0; q < 3; ++q) ok = xmul(n[q], vmin[q], d[q]) && ok;
+  ok = xsub(d[0], -d[1], s1) && ok;
+  ok = xsub(s1, -d[2], dmin) && ok;
+  if (!ok) return kUnknown;
+  if (dmin > 0.f) return kTrue;
+  for (int q = 0; q < 3; ++q) ok = xmul(n[q], vmax[q], d[q]) && ok;
+  ok = xsub(d[0], -d[1], s1) && ok;
+  ok = xsub(s1, -d[2], dmax) && ok;
+  if (!ok) return kUnknown;
+  return (dmax >= 0.f) ? kFalse : kTrue;
+}
+
+// Edge tangency.  Edge-axis test k projects vertices i0, i1 onto
+// p = a*u - b*w (Y tests: -a*u + b*w) with a = e_A, b = e_B of edge j and
+// u = v_U, w = v_W.  When a is an exact zero (the edge's endpoints share
+// coordinate A, so the reference's e_A = v - v = 0) and |w| = h exactly for
+// one of the two vertices, the reference computes |p| = fl(|b|*h) = rad for
+// that vertex: it lies on the slab boundary and the test cannot reject.  The
+// same holds with b and u exchanged, and when a = b = 0 (p = rad = 0).
+// Returns true when the rule proves test k passes for box centre c.
+SAT_HD bool edge_tangent(const float* t, const float c[3], float h, int k) {
+  int aa, bb, ua, wa, i0, i1;
+  switch (k) {
+    case 0: case 3: aa = 2; bb = 1; ua = 1; wa = 2; i0 = 0; i1 = 2; break;
+    case 1: case 4: aa = 2; bb = 0; ua = 0; wa = 2; i0 = 0; i1 = 2; break;
+    case 2: case 8: aa = 1; bb = 0; ua = 0; wa = 1; i0 = 1; i1 = 2; break;
+    case 5: aa = 1; bb = 0; ua = 0; wa = 1; i0 = 0; i1 = 1; break;
+    case 6: aa = 2; bb = 1; ua = 1; wa = 2; i0 = 0; i1 = 1; break;
+    default: aa = 2; bb = 0; ua = 0; wa = 2; i0 = 0; i1 = 1; break;
+  }
+  const int j = k / 3;                       // e0 = v1 - v0, e1 = v2 - v1, e2 = v0 - v2
+  const int ea = (j + 1) % 3, eb = j;        // endpoints of edge j
+  const bool a0 = t[3 * ea + aa] == t[3 * eb + aa];
+  const bool b0 = t[3 * ea + bb] == t[3 * eb + bb];
+  if (a0 && b0) return true;
+  if (!a0 && !b0) return false;
+  const int q = a0 ? wa : ua;                // the component multiplied by the non-zero coefficient
+  for (int r = 0; r < 2; ++r) {
+    const int i = r ? i1 : i0;
+    float vq;
+    if (xsub(t[3 * i + q], c[q], vq) && fabsf_(vq) == h) return true;
+  }
+  return false;
+}
+
 // ---------------------------------------------------------------------------
 // fp32 filter.
 
@@ -195,6 +363,18 @@ SAT_HD void node_boxes(const double c[3], double k, NodeBoxes& nb) {
   nb.ok = ok ? 1.f : 0.f;
 }
 
+// Where the triangle's extent on one axis lies against one child slab
+// [c - h, c + h]:
+//   out    : the reference's bounding-box test rejects (certain)
+//   in     : strictly inside, margin >= 2^-21 h (certain pass, see below)
+//   cross  : the bounding-box test passes (certain), not strictly inside
+//   unsure : the bounding-box predicate needs fp64
+// A triangle strictly inside a box by a margin d passes all 13 fp64 tests of
+// the reference when d exceeds their rounding errors (<= 2^-40 h): every
+// edge-axis projection lies within rad - d(|a|+|b|), and the plane test gives
+// dmin <= -|n|_1 d < 0 <= |n|_1 d <= dmax (both zero when n = 0).
+enum Slab : uint32_t { kSlabOut = 0, kSlabIn = 1, kSlabCross = 2, kSlabUnsure = 3 };
+
 // Per (triangle, parent node) data shared by the 8 children.
 struct Pair32 {
   float t[9];        // triangle (exact)
@@ -203,6 +383,10 @@ struct Pair32 {
   NodeBoxes nb;
   float h;           // child half side (exact in fp32 when nb.ok)
   bool fast;         // fp32 path usable (finite, moderate magnitudes)
+  uint32_t slab;     // 2 bits per (axis q, side s) at bit 2*(2q+s)
+  uint32_t tang;     // bit 2q+s: grid-plane tangency on axis q, side s (see pair_slabs)
+  float vmax[6];     // max_i |fl32(t_iq - chi)| per (axis, side)
+  const float* tp;   // the triangle in its source buffer (fp64 predicates reload it)
   const double* c;   // parent centre (fp64), for predicates decided in fp64
   double k;          // child half side (fp64)
 };
@@ -228,7 +412,10 @@ SAT_HD Tri tri_or(Tri a, Tri b) {
 
 // Builds the per-pair data; c = parent centre (fp64, kept by pointer),
 // nb = the node's child boxes, k = child half side.
-SAT_HD void pair_setup(const float t[9], const double* c, const NodeBoxes& nb, double k, Pair32& P) {
+// Triangle, node and edge data of a pair (no slab classification).
+SAT_HD void pair_basic(const float t[9], const float* tp, const double* c, const NodeBoxes& nb, double k,
+                       Pair32& P) {
+  P.tp = tp;
   bool ok = nb.ok != 0.f;
   for (int i = 0; i < 9; ++i) {
     P.t[i] = t[i];
@@ -245,6 +432,73 @@ SAT_HD void pair_setup(const float t[9], const double* c, const NodeBoxes& nb, d
   P.fast = ok;
   P.c = c;
   P.k = k;
+  P.slab = 0;
+  P.tang = 0;
+}
+
+// Slab classification of the pair (see Slab).
+SAT_HD void pair_slabs(Pair32& P) {
+  if (!P.fast) return;
+  const float* t = P.t;
+  const NodeBoxes& nb = P.nb;
+  // per axis: vertex extent; fl32(t - chi) is monotone in t, so the extreme
+  // offsets are the offsets of the extreme coordinates
+  const float h = P.h, clo = nb.clo;
+  const float thr_in = fsub(fmul(h, 0.99999904632568359375f), fmul(1.02f, clo));
+  uint32_t slab = 0;
+  for (int q = 0; q < 3; ++q) {
+    float tmn = t[q], tmx = t[q];
+    tmn = (t[3 + q] < tmn) ? t[3 + q] : tmn;
+    tmx = (t[3 + q] > tmx) ? t[3 + q] : tmx;
+    tmn = (t[6 + q] < tmn) ? t[6 + q] : tmn;
+    tmx = (t[6 + q] > tmx) ? t[6 + q] : tmx;
+    for (int sd = 0; sd < 2; ++sd) {
+      const float chi = nb.chi[2 * q + sd];
+      const float mn = fsub(tmn, chi), mx = fsub(tmx, chi);
+      // FINDMINMAX reject: min v > h or max v < -h, with |v_f - v*| <= 1.01 u32 |v_f| + clo
+      // and a one-ulp fp64 margin
+      const float tl = fadd(fadd(fmul(1.1f * kU32, fabsf_(mn)), fmul(1.02f, clo)),
+                            fadd(fmul(2.2e-16f, fadd(fabsf_(mn), h)), kTiny));
+      const float tu = fadd(fadd(fmul(1.1f * kU32, fabsf_(mx)), fmul(1.02f, clo)),
+                            fadd(fmul(2.2e-16f, fadd(fabsf_(mx), h)), kTiny));
+      const Tri r = tri_or(gt(mn, h, tl), gt(-h, mx, tu));
+      const float am = (fabsf_(mn) > fabsf_(mx)) ? fabsf_(mn) : fabsf_(mx);
+      P.vmax[2 * q + sd] = am;
+      uint32_t cls;
+      if (r == kTrue) cls = kSlabOut;
+      else if (r == kUnknown) cls = kSlabUnsure;
+      else cls = (am <= thr_in) ? kSlabIn : kSlabCross;
+      slab |= cls << (2 * (2 * q + sd));
+    }
+  }
+  P.slab = slab;
+  // Grid-plane tangency.  When the three vertices share coordinate q
+  // (t_q constant) and the child face lies exactly on that plane
+  // (t_q - c_q = +-h exactly, c_q an fp32 value), the reference's fp64
+  // predicates that involve axis q all pass: the bounding-box test on q
+  // compares +-h with h; every edge of the triangle has e_q = 0 exactly, so an
+  // edge-axis test whose projection uses v_q computes p = fl(e'*(+-h)) (the
+  // e_q*v term is an exact zero) against rad = fl(|e'|*h), i.e. |p| = rad,
+  // which rejects nothing; and the plane test's normal has only its q
+  // component non-zero with box corner offsets {0, +-2h} on q, giving
+  // dmin <= 0 <= dmax.
+  uint32_t tang = 0;
+  if (clo == 0.f) {
+    for (int q = 0; q < 3; ++q) {
+      if (!(t[q] == t[3 + q] && t[q] == t[6 + q])) continue;
+      for (int sd = 0; sd < 2; ++sd) {
+        float vq;
+        if (xsub(t[q], nb.chi[2 * q + sd], vq) && fabsf_(vq) == h) tang |= 1u << (2 * q + sd);
+      }
+    }
+  }
+  P.tang = tang;
+}
+
+SAT_HD void pair_setup(const float t[9], const float* tp, const double* c, const NodeBoxes& nb, double k,
+                       Pair32& P) {
+  pair_basic(t, tp, c, nb, k, P);
+  pair_slabs(P);
 }
 
 // One edge-axis test in fp32: reject (kTrue), keep (kFalse) or kUnknown.
@@ -272,68 +526,71 @@ SAT_HD Tri edge_test32(float a, float b, bool neg_a, float u0, float w0, float u
   return tri_or(above, below);
 }
 
-// Overlap decision for child `ci` (index 4x+2y+z) of the pair.  Returns
-// true when the child box overlaps the triangle; `fallbacks` counts the
-// predicates that needed fp64.
-SAT_HD bool child_overlap(const Pair32& P, int ci, unsigned* fallbacks) {
+// Decision from the slab classes alone: 0 no overlap, 1 overlap, 2 the
+// full test is needed.
+SAT_HD int child_fast(const Pair32& P, int ci) {
+  if (!P.fast) return 2;
+  const uint32_t cx = (P.slab >> (2 * (0 + ((ci >> 2) & 1)))) & 3u;
+  const uint32_t cy = (P.slab >> (2 * (2 + ((ci >> 1) & 1)))) & 3u;
+  const uint32_t cz = (P.slab >> (2 * (4 + (ci & 1)))) & 3u;
+  if (cx == kSlabOut || cy == kSlabOut || cz == kSlabOut) return 0;
+  if (cx == kSlabIn && cy == kSlabIn && cz == kSlabIn) return 1;
+  return 2;
+}
+
+// The full test of child `ci` for a child child_fast() left undecided.
+SAT_HD bool child_full(const Pair32& P, int ci, unsigned* fallbacks) {
   const bool sx = (ci >> 2) & 1, sy = (ci >> 1) & 1, sz = ci & 1;
-  auto centre64 = [&](double c[3]) {
-    c[0] = dadd(P.c[0], sx ? P.k : -P.k);
-    c[1] = dadd(P.c[1], sy ? P.k : -P.k);
-    c[2] = dadd(P.c[2], sz ? P.k : -P.k);
-  };
   if (!P.fast) {
     if (fallbacks) ++*fallbacks;
-    double c[3];
-    centre64(c);
-    return tri_box64(P.t, c, P.k);
+    SVDAG_FB_HOOK(-1);
+    return !pred64(P.tp, P.c, P.k, ci, -1);
   }
+  const uint32_t cx = (P.slab >> (2 * (0 + sx))) & 3u;
+  const uint32_t cy = (P.slab >> (2 * (2 + sy))) & 3u;
+  const uint32_t cz = (P.slab >> (2 * (4 + sz))) & 3u;
   const float h = P.h;
   const float clo = P.nb.clo;
   // fp32 vertex offsets v = t - fl32(c); |v_f - (t - c)| <= 1.01 u32 |v_f| + 1.01 clo
   float v[3][3];
   const float chi[3] = {sx ? P.nb.chi[1] : P.nb.chi[0], sy ? P.nb.chi[3] : P.nb.chi[2], sz ? P.nb.chi[5] : P.nb.chi[4]};
-  float V = 0.f;
   for (int i = 0; i < 3; ++i)
-    for (int q = 0; q < 3; ++q) {
-      v[i][q] = fsub(P.t[3 * i + q], chi[q]);
-      const float a = fabsf_(v[i][q]);
-      V = (a > V) ? a : V;
-    }
+    for (int q = 0; q < 3; ++q) v[i][q] = fsub(P.t[3 * i + q], chi[q]);
+  float V = sx ? P.vmax[1] : P.vmax[0];
+  const float vy = sy ? P.vmax[3] : P.vmax[2], vz = sz ? P.vmax[5] : P.vmax[4];
+  V = (vy > V) ? vy : V;
+  V = (vz > V) ? vz : V;
   V = fadd(fmul(V, 1.0000003f), fmul(1.01f, clo));
 
-  Box64 b64;
-  bool have64 = false;
-  auto need64 = [&]() {
-    if (!have64) {
-      double c[3];
-      centre64(c);
-      box64(P.t, c, b64);
-      have64 = true;
+  // undecided predicate: exact fp32 tier when the box centre is an fp32
+  // value, else (or when inexact) the reference's fp64 evaluation
+  auto need64 = [&](int which) {
+    if (clo == 0.f && which >= 3 && which < 12 && edge_tangent(P.t, chi, h, which - 3)) return false;
+    if (clo == 0.f) {
+      const int r = exact32(P.tp, chi[0], chi[1], chi[2], h, which);
+      if (r != kUnknown) return r == kTrue;
     }
     if (fallbacks) ++*fallbacks;
+    SVDAG_FB_HOOK(which);
+    return pred64(P.tp, P.c, P.k, ci, which);
   };
 
-  // bounding-box tests (FINDMINMAX): v_d > h decided from v_f
-  for (int q = 0; q < 3; ++q) {
-    float mn = v[0][q], mx = v[0][q];
-    mn = (v[1][q] < mn) ? v[1][q] : mn;
-    mx = (v[1][q] > mx) ? v[1][q] : mx;
-    mn = (v[2][q] < mn) ? v[2][q] : mn;
-    mx = (v[2][q] > mx) ? v[2][q] : mx;
-    const float tmn = fadd(fadd(fmul(1.1f * kU32, fabsf_(mn)), fmul(1.02f, clo)), fadd(fmul(2.2e-16f, fadd(fabsf_(mn), h)), kTiny));
-    const float tmx = fadd(fadd(fmul(1.1f * kU32, fabsf_(mx)), fmul(1.02f, clo)), fadd(fmul(2.2e-16f, fadd(fabsf_(mx), h)), kTiny));
-    const Tri r = tri_or(gt(mn, h, tmn), gt(-h, mx, tmx));
-    if (r == kTrue) return false;
-    if (r == kUnknown) {
-      need64();
-      if (aabb_reject64(b64, q, P.k)) return false;
-    }
-  }
+  // grid-plane tangency (pair_slabs): the predicates on a tangent axis pass
+  const bool tx = (P.tang >> (0 + sx)) & 1u, ty = (P.tang >> (2 + sy)) & 1u, tz = (P.tang >> (4 + sz)) & 1u;
+  const bool passX = ty || tz, passY = tx || tz, passZ = tx || ty;  // X-, Y-, Z-axis edge tests
+
+  // bounding-box tests (FINDMINMAX): decided per slab in pair_setup
+  if (cx == kSlabUnsure && !tx && need64(0)) return false;
+  if (cy == kSlabUnsure && !ty && need64(1)) return false;
+  if (cz == kSlabUnsure && !tz && need64(2)) return false;
 
   // nine edge-axis tests (test_triangle_box.cpp:137-156)
   const int X = 0, Y = 1, Z = 2;
+#pragma unroll
   for (int k = 0; k < 9; ++k) {
+    if ((k == 0 || k == 3 || k == 6) && passX) continue;
+    if ((k == 1 || k == 4 || k == 7) && passY) continue;
+    if ((k == 2 || k == 5 || k == 8) && passZ) continue;
     const int j = k / 3;
     const float* e = P.e[j];
     const float* ae = P.ae[j];
@@ -353,11 +610,10 @@ SAT_HD bool child_overlap(const Pair32& P, int ci, unsigned* fallbacks) {
         r = edge_test32(e[Z], e[X], true, v[0][X], v[0][Z], v[1][X], v[1][Z], ae[Z], ae[X], h, clo, V); break;
     }
     if (r == kTrue) return false;
-    if (r == kUnknown) {
-      need64();
-      if (edge_test64(b64, k, P.k)) return false;
-    }
+    if (r == kUnknown && need64(3 + k)) return false;
   }
+
+  if (tx || ty || tz) return true;  // the plane test passes on a tangent grid plane
 
   // plane test: normal = e0 x e1; vmin/vmax by the sign of each component.
   const float* e0 = P.e[0];
@@ -396,8 +652,16 @@ SAT_HD bool child_overlap(const Pair32& P, int ci, unsigned* fallbacks) {
       if (rmax == kFalse) return false;
     }
   }
-  need64();
-  return !plane_reject64(b64, P.k);
+  return !need64(12);
+}
+
+// Overlap decision for child `ci` (index 4x+2y+z) of the pair: true when the
+// child box overlaps the triangle exactly as the reference decides it;
+// `fallbacks` counts the predicates that needed fp64.
+SAT_HD bool child_overlap(const Pair32& P, int ci, unsigned* fallbacks) {
+  const int f = child_fast(P, ci);
+  if (f != 2) return f == 1;
+  return child_full(P, ci, fallbacks);
 }
 
 }  // namespace sat

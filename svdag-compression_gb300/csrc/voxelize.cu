@@ -41,47 +41,116 @@ __host__ __device__ __forceinline__ double child_half_side(double root_side, uin
   return root_side / double(1ull << (l + 2));
 }
 
-// One thread per frontier pair: the 8 child boxes against the triangle.
-__global__ void __launch_bounds__(256) k_expand(VoxParams P, const float* __restrict__ tris,
-                                                const uint32_t* __restrict__ f_tri, const uint32_t* __restrict__ f_node,
-                                                uint64_t F, const double* __restrict__ ctr,
-                                                const float* __restrict__ nbox, uint32_t* __restrict__ hdr, uint32_t* __restrict__ firstq,
-                                                uint8_t* __restrict__ hits_out, unsigned long long* __restrict__ n_fallback) {
+// Expansion of one frontier tile per block, in two phases so the expensive
+// box tests run with full warps:
+//   1. one thread per pair loads the triangle and the node's child boxes,
+//      classifies the triangle's extent against the 6 child slabs and decides
+//      every child the slabs settle (certain miss / certain overlap);
+//   2. the (pair, child) items left undecided are queued in shared memory and
+//      the whole block works through the queue, one item per thread, with the
+//      full certified test.
+// Then each pair publishes its hit mask: OR into the node mask, first-pair
+// index per created child, and the mask for the next frontier.
+constexpr int kExpandThreads = 256;
+
+__global__ void __launch_bounds__(kExpandThreads) k_expand(VoxParams P, const float* __restrict__ tris,
+                                                           const uint32_t* __restrict__ f_tri,
+                                                           const uint32_t* __restrict__ f_node, uint64_t F,
+                                                           const double* __restrict__ ctr, const float* __restrict__ nbox,
+                                                           uint32_t* __restrict__ hdr, uint32_t* __restrict__ firstq,
+                                                           uint8_t* __restrict__ hits_out,
+                                                           unsigned long long* __restrict__ n_fallback) {
+  __shared__ float s_t[9][kExpandThreads];
+  __shared__ float s_nb[8][kExpandThreads];
+  __shared__ float s_vmax[6][kExpandThreads];
+  __shared__ uint32_t s_tri[kExpandThreads], s_node[kExpandThreads], s_slab[kExpandThreads];
+  __shared__ uint32_t s_hits[kExpandThreads];
+  __shared__ uint16_t s_queue[8 * kExpandThreads];
+  __shared__ uint32_t s_qn;
   const double k = child_half_side(P.root_side, P.level);
   const bool leaf = (P.level == P.leaf_level);
+  const int tid = threadIdx.x;
   unsigned fb = 0;
-  for (uint64_t q = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; q < F; q += uint64_t(gridDim.x) * blockDim.x) {
-    const uint32_t t = f_tri ? f_tri[q] : uint32_t(q);
-    const uint32_t node = f_node ? f_node[q] : 0u;
-    float tri[9];
-    const float* tp = tris + 9ull * t;
+  for (uint64_t base = uint64_t(blockIdx.x) * kExpandThreads; base < F; base += uint64_t(gridDim.x) * kExpandThreads) {
+    const uint64_t q = base + tid;
+    if (tid == 0) s_qn = 0;
+    __syncthreads();
+    uint32_t hits = 0;
+    if (q < F) {
+      const uint32_t t = f_tri ? f_tri[q] : uint32_t(q);
+      const uint32_t node = f_node ? f_node[q] : 0u;
+      const float* tp = tris + 9ull * t;
+      float tri[9];
 #pragma unroll
-    for (int j = 0; j < 9; ++j) tri[j] = tp[j];
-    sat::NodeBoxes nb;
-    {
-      const float4* p = reinterpret_cast<const float4*>(nbox + 8ull * node);
-      const float4 a = p[0], b = p[1];
+      for (int j = 0; j < 9; ++j) tri[j] = tp[j];
+      sat::NodeBoxes nb;
+      const float4* np = reinterpret_cast<const float4*>(nbox + 8ull * node);
+      const float4 a = np[0], b = np[1];
       nb.chi[0] = a.x; nb.chi[1] = a.y; nb.chi[2] = a.z; nb.chi[3] = a.w;
       nb.chi[4] = b.x; nb.chi[5] = b.y; nb.clo = b.z; nb.ok = b.w;
+      sat::Pair32 PP;
+      sat::pair_setup(tri, tp, ctr + 3ull * node, nb, k, PP);
+      for (int ci = 7; ci >= 0; --ci) {
+        const int f = sat::child_fast(PP, ci);
+        if (f == 1) {
+          hits |= 1u << ci;
+        } else if (f == 2) {
+          const uint32_t slot = atomicAdd(&s_qn, 1u);
+          s_queue[slot] = uint16_t((tid << 3) | ci);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 9; ++j) s_t[j][tid] = tri[j];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) { s_nb[j][tid] = nb.chi[j]; s_vmax[j][tid] = PP.vmax[j]; }
+      s_nb[6][tid] = nb.clo;
+      s_nb[7][tid] = nb.ok;
+      s_tri[tid] = t;
+      s_node[tid] = node;
+      s_slab[tid] = PP.slab | (PP.tang << 16);  // slab classes (12 bits) + tangency (6 bits)
     }
-    sat::Pair32 PP;
-    sat::pair_setup(tri, ctr + 3ull * node, nb, k, PP);
-    uint32_t h = 0;
-#pragma unroll 1
-    for (int i = 7; i >= 0; --i)
-      if (sat::child_overlap(PP, i, &fb)) h |= 1u << i;
-    if (h) atomicOr(&hdr[node], h);
-    if (!leaf) {
-      hits_out[q] = uint8_t(h);
-      for (uint32_t m = h; m; m &= m - 1) {
-        const int i = __ffs(m) - 1;
-        atomicMin(&firstq[8ull * node + i], uint32_t(q));
+    s_hits[tid] = hits;
+    __syncthreads();
+    const uint32_t nq = s_qn;
+    for (uint32_t i = tid; i < nq; i += kExpandThreads) {
+      const uint32_t item = s_queue[i];
+      const uint32_t slot = item >> 3;
+      const int ci = int(item & 7u);
+      float tri[9];
+#pragma unroll
+      for (int j = 0; j < 9; ++j) tri[j] = s_t[j][slot];
+      sat::NodeBoxes nb;
+#pragma unroll
+      for (int j = 0; j < 6; ++j) nb.chi[j] = s_nb[j][slot];
+      nb.clo = s_nb[6][slot];
+      nb.ok = s_nb[7][slot];
+      const uint32_t node = s_node[slot];
+      sat::Pair32 PP;
+      sat::pair_basic(tri, tris + 9ull * s_tri[slot], ctr + 3ull * node, nb, k, PP);
+      PP.slab = s_slab[slot] & 0xFFFFu;
+      PP.tang = s_slab[slot] >> 16;
+#pragma unroll
+      for (int j = 0; j < 6; ++j) PP.vmax[j] = s_vmax[j][slot];
+      if (sat::child_full(PP, ci, &fb)) atomicOr(&s_hits[slot], 1u << ci);
+    }
+    __syncthreads();
+    if (q < F) {
+      const uint32_t h = s_hits[tid];
+      const uint32_t node = s_node[tid];
+      if (h) atomicOr(&hdr[node], h);
+      if (!leaf) {
+        hits_out[q] = uint8_t(h);
+        for (uint32_t m = h; m; m &= m - 1) {
+          const int i = __ffs(m) - 1;
+          atomicMin(&firstq[8ull * node + i], uint32_t(q));
+        }
       }
     }
+    __syncthreads();
   }
-  unsigned long long s = fb;
-  for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, o);
-  if ((threadIdx.x & 31) == 0 && s) atomicAdd(n_fallback, s);
+  unsigned long long sum = fb;
+  for (int o = 16; o; o >>= 1) sum += __shfl_down_sync(0xFFFFFFFFu, sum, o);
+  if ((threadIdx.x & 31) == 0 && sum) atomicAdd(n_fallback, sum);
 }
 
 // Creation key of each created child: firstq * 8 + (7 - child).
@@ -251,7 +320,7 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
       hits.alloc(F, st);
     }
     if (F)
-      SVDAG_LAUNCH(ex, k_expand, grid_for(ex, F, 256, 32), 256, 0, P, c.tris, f_tri.get(), f_node.get(), F,
+      SVDAG_LAUNCH(ex, k_expand, grid_for(ex, F, kExpandThreads, 8), kExpandThreads, 0, P, c.tris, f_tri.get(), f_node.get(), F,
                    L.ctr.get(), L.nbox.get(), L.hdr.get(), firstq.get(), hits.get(), d_fb.get());
     if (leaf) break;
 

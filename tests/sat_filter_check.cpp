@@ -21,7 +21,7 @@ static void check(const float t[9], const double pc[3], double k) {
   NodeBoxes nb;
   node_boxes(pc, k, nb);
   Pair32 P;
-  pair_setup(t, pc, nb, k, P);
+  pair_setup(t, t, pc, nb, k, P);
   for (int ci = 0; ci < 8; ++ci) {
     const double c[3] = {pc[0] + ((ci & 4) ? k : -k), pc[1] + ((ci & 2) ? k : -k), pc[2] + ((ci & 1) ? k : -k)};
     const bool want = ora_tri_box(c, k, t) != 0;
