@@ -255,6 +255,7 @@ def run_ours(args, rank, local, world):
                    "l2": "inputs larger than L2 (triangles 302 MB, node pools > 129 MB)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clk, "gpu_launches": int(launches), "roofline": roof, "e2e": e2e,
+        "kernel_ms_per_step": sum(v[1] for v in prof.values()) / args.steps,
         "kernels": {k: {"launches": v[0], "ms_per_step": v[1] / args.steps} for k, v in
                     sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]},
     }

@@ -98,6 +98,12 @@ int svdag_create(svdag_ctx** out, int device, void* stream) {
     }
     int sms = 0;
     SVDAG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    // keep freed blocks of the stream-ordered allocator cached between builds
+    // (a process-local attribute of this device's default pool)
+    cudaMemPool_t pool;
+    SVDAG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t keep = ~0ull;
+    SVDAG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
     c.ex.stream = c.stream;
     c.ex.sm_count = sms;
     c.ex.launches = &c.launches;

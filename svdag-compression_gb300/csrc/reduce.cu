@@ -350,7 +350,6 @@ void phase_reduce_dag(Ctx& c) {
       slot_of.release();
       device_exclusive_scan<uint32_t>(ex, RepFlagIn{rep.get()}, n, U32Out{newid.get()}, d_cnt.get());
       const uint64_t d = read_scalar(ex, d_cnt.get());
-      check_err(ex, d_err.get(), "toDAG");
       DBuf<uint32_t> out_hdr(d ? d : 1, st), out_ch(8 * (d ? d : 1), st);
       if (n)
         SVDAG_LAUNCH(ex, k_compact_dag, grid_for(ex, n, 256), 256, 0, L.hdr.get(), L.ch.get(), n, rep.get(),
@@ -363,6 +362,7 @@ void phase_reduce_dag(Ctx& c) {
     }
     nnodes += L.n;
   }
+  check_err(ex, d_err.get(), "toDAG");
   c.st.n_nodes_dag = nnodes;
   c.st.n_nodes = nnodes;
   c.state = SVDAG_S_DAG;
@@ -413,7 +413,6 @@ void phase_reduce_sdag(Ctx& c) {
     slot_of.release();
     device_exclusive_scan<uint32_t>(ex, UniqueFlagIn{state.get()}, n, U32Out{newid.get()}, d_cnt.get());
     const uint64_t s = read_scalar(ex, d_cnt.get());
-    check_err(ex, d_err.get(), "toSDAG");
     DBuf<uint32_t> out_hdr(s ? s : 1, st), out_ch(ch ? 8 * (s ? s : 1) : 0, st), corr_id(n ? n : 1, st);
     DBuf<uint8_t> out_inv(s ? s : 1, st), corr_m(n ? n : 1, st);
     if (n)
@@ -429,6 +428,7 @@ void phase_reduce_sdag(Ctx& c) {
     child_inv = L.inv.get();
     nnodes += s;
   }
+  check_err(ex, d_err.get(), "toSDAG");
   c.st.n_nodes_sdag = nnodes;
   c.st.n_nodes = nnodes;
   c.state = SVDAG_S_SDAG;

@@ -70,6 +70,21 @@ SAT_HD double fabs_(double a) { return std::fabs(a); }
 SAT_HD float ffma(float a, float b, float c) { return std::fma(a, b, c); }
 #endif
 
+// Two independent fp32 operations (one packed instruction on sm_100+; each
+// lane is the ordinary IEEE-rounded operation, so host and device agree).
+struct F2 {
+  float x, y;
+};
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000)
+SAT_HD F2 f2add(F2 a, F2 b) { const float2 r = __fadd2_rn(make_float2(a.x, a.y), make_float2(b.x, b.y)); return {r.x, r.y}; }
+SAT_HD F2 f2mul(F2 a, F2 b) { const float2 r = __fmul2_rn(make_float2(a.x, a.y), make_float2(b.x, b.y)); return {r.x, r.y}; }
+#else
+SAT_HD F2 f2add(F2 a, F2 b) { return {fadd(a.x, b.x), fadd(a.y, b.y)}; }
+SAT_HD F2 f2mul(F2 a, F2 b) { return {fmul(a.x, b.x), fmul(a.y, b.y)}; }
+#endif
+SAT_HD float fmin_(float a, float b) { return (b < a) ? b : a; }
+SAT_HD float fmax_(float a, float b) { return (a < b) ? b : a; }
+
 constexpr float kU32 = 5.9604644775390625e-08f;  // 2^-24
 constexpr float kTiny = 7.8886090522101181e-31f; // 2^-100 absolute slack
 constexpr float kD64 = 7.105427357601002e-15f;   // 2^-47 (fp64-side factor)
@@ -309,7 +324,10 @@ SAT_COLD int exact32(const float* tg, float cx, float cy, float cz, float h, int
 // that vertex: it lies on the slab boundary and the test cannot reject.  The
 // same holds with b and u exchanged, and when a = b = 0 (p = rad = 0).
 // Returns true when the rule proves test k passes for box centre c.
-SAT_HD bool edge_tangent(const float* t, const float c[3], float h, int k) {
+SAT_COLD bool edge_tangent(const float* tg, float cx, float cy, float cz, float h, int k) {
+  float t[9];
+  for (int i = 0; i < 9; ++i) t[i] = tg[i];
+  const float c[3] = {cx, cy, cz};
   int aa, bb, ua, wa, i0, i1;
   switch (k) {
     case 0: case 3: aa = 2; bb = 1; ua = 1; wa = 2; i0 = 0; i1 = 2; break;
@@ -455,13 +473,23 @@ SAT_HD void pair_slabs(Pair32& P) {
     for (int sd = 0; sd < 2; ++sd) {
       const float chi = nb.chi[2 * q + sd];
       const float mn = fsub(tmn, chi), mx = fsub(tmx, chi);
-      // FINDMINMAX reject: min v > h or max v < -h, with |v_f - v*| <= 1.01 u32 |v_f| + clo
-      // and a one-ulp fp64 margin
-      const float tl = fadd(fadd(fmul(1.1f * kU32, fabsf_(mn)), fmul(1.02f, clo)),
-                            fadd(fmul(2.2e-16f, fadd(fabsf_(mn), h)), kTiny));
-      const float tu = fadd(fadd(fmul(1.1f * kU32, fabsf_(mx)), fmul(1.02f, clo)),
-                            fadd(fmul(2.2e-16f, fadd(fabsf_(mx), h)), kTiny));
-      const Tri r = tri_or(gt(mn, h, tl), gt(-h, mx, tu));
+      // FINDMINMAX reject: min v > h or max v < -h.
+      Tri r;
+      if (clo == 0.f) {
+        // c is an fp32 value: v_f = fl32(v*) and v_d = fl64(v*) round the same
+        // exact v*, and h is an fp32 value, so v_f > h implies v* > h + ulp32/2,
+        // hence v_d > h (likewise for <); only equality stays open
+        if (mn > h || mx < -h) r = kTrue;
+        else if (mn < h && mx > -h) r = kFalse;
+        else r = kUnknown;
+      } else {
+        // |v_f - v*| <= 1.01 u32 |v_f| + clo, plus a one-ulp fp64 margin
+        const float tl = fadd(fadd(fmul(1.1f * kU32, fabsf_(mn)), fmul(1.02f, clo)),
+                              fadd(fmul(2.2e-16f, fadd(fabsf_(mn), h)), kTiny));
+        const float tu = fadd(fadd(fmul(1.1f * kU32, fabsf_(mx)), fmul(1.02f, clo)),
+                              fadd(fmul(2.2e-16f, fadd(fabsf_(mx), h)), kTiny));
+        r = tri_or(gt(mn, h, tl), gt(-h, mx, tu));
+      }
       const float am = (fabsf_(mn) > fabsf_(mx)) ? fabsf_(mn) : fabsf_(mx);
       P.vmax[2 * q + sd] = am;
       uint32_t cls;
@@ -502,28 +530,29 @@ SAT_HD void pair_setup(const float t[9], const float* tp, const double* c, const
 }
 
 // One edge-axis test in fp32: reject (kTrue), keep (kFalse) or kUnknown.
-// p_i = sa*a*u_i - sb*b*w_i  for the two vertices i of the test;
-// V: bound on |t - c| over this box.
+// p_i = a*u_i - b*w_i (negated for the Y tests) for the two vertices of the
+// test; cd = the fp64-side and absolute error terms of the box.
+// The reference rejects iff min p > rad or max p < -rad.  With tol covering
+// |p_f - p*| + |rad_f - rad*| + the fp64 errors, and the roundings of
+// rad +- tol (at most u32 (rad + tol), absorbed by the 4.6 / 4.3 factors):
+//   min p > rad + tol or max p < -(rad + tol)   -> certain reject
+//   min p < rad - tol and max p > -(rad - tol)  -> certain keep
 SAT_HD Tri edge_test32(float a, float b, bool neg_a, float u0, float w0, float u1, float w1, float fa, float fb,
-                       float h, float clo, float V) {
-  // p = a*u - b*w, or (-a)*u + b*w for the Y tests; both are +-(a*u - b*w)
-  // up to the order of the two roundings, which the bound covers.
-  const float x0 = fmul(a, u0), y0 = fmul(b, w0);
-  const float x1 = fmul(a, u1), y1 = fmul(b, w1);
-  float p0 = fsub(x0, y0), p1 = fsub(x1, y1);
-  if (neg_a) { p0 = -p0; p1 = -p1; }
-  const float s0 = fadd(fabsf_(x0), fabsf_(y0));
-  const float s1 = fadd(fabsf_(x1), fabsf_(y1));
-  const float rad = fmul(fadd(fa, fb), h);
+                       float h, float clo, float cd) {
+  const F2 x = f2mul(F2{a, a}, F2{u0, u1});
+  const F2 y = f2mul(F2{b, b}, F2{w0, w1});
+  F2 p = f2add(x, F2{-y.x, -y.y});
+  if (neg_a) p = F2{-p.x, -p.y};
+  const F2 sv = f2add(F2{fabsf_(x.x), fabsf_(x.y)}, F2{fabsf_(y.x), fabsf_(y.y)});
   const float ab = fadd(fa, fb);
-  const float common = fadd(fadd(fmul(3.2f * kU32, rad), fmul(1.03f, fmul(ab, clo))),
-                            fadd(fmul(kD64, fadd(fmul(V, V), fmul(V, h))), kTiny));
-  const float tol0 = fadd(fmul(4.2f * kU32, s0), common);
-  const float tol1 = fadd(fmul(4.2f * kU32, s1), common);
-  // reject iff (p0 > rad && p1 > rad) || (p0 < -rad && p1 < -rad)
-  const Tri above = tri_and(gt(p0, rad, tol0), gt(p1, rad, tol1));
-  const Tri below = tri_and(gt(-rad, p0, tol0), gt(-rad, p1, tol1));
-  return tri_or(above, below);
+  const float rad = fmul(ab, h);
+  const float smax = fmax_(sv.x, sv.y);
+  const float tol = ffma(4.6f * kU32, smax, ffma(4.3f * kU32, rad, ffma(1.04f * clo, ab, cd)));
+  const float mn = fmin_(p.x, p.y), mx = fmax_(p.x, p.y);
+  const float hi = fadd(rad, tol), lo = fsub(rad, tol);
+  if (mn > hi || mx < -hi) return kTrue;
+  if (mn < lo && mx > -lo) return kFalse;
+  return kUnknown;
 }
 
 // Decision from the slab classes alone: 0 no overlap, 1 overlap, 2 the
@@ -561,11 +590,13 @@ SAT_HD bool child_full(const Pair32& P, int ci, unsigned* fallbacks) {
   V = (vy > V) ? vy : V;
   V = (vz > V) ? vz : V;
   V = fadd(fmul(V, 1.0000003f), fmul(1.01f, clo));
+  // fp64-side and absolute error terms of the edge tests: 2^-47 (V^2 + V h) + 2^-100
+  const float cd = ffma(kD64, fmul(V, fadd(V, h)), kTiny);
 
   // undecided predicate: exact fp32 tier when the box centre is an fp32
   // value, else (or when inexact) the reference's fp64 evaluation
   auto need64 = [&](int which) {
-    if (clo == 0.f && which >= 3 && which < 12 && edge_tangent(P.t, chi, h, which - 3)) return false;
+    if (clo == 0.f && which >= 3 && which < 12 && edge_tangent(P.tp, chi[0], chi[1], chi[2], h, which - 3)) return false;
     if (clo == 0.f) {
       const int r = exact32(P.tp, chi[0], chi[1], chi[2], h, which);
       if (r != kUnknown) return r == kTrue;
@@ -597,17 +628,17 @@ SAT_HD bool child_full(const Pair32& P, int ci, unsigned* fallbacks) {
     Tri r;
     switch (k) {
       case 0: case 3:  // X01: a=e.z, b=e.y over v0, v2 on (y, z)
-        r = edge_test32(e[Z], e[Y], false, v[0][Y], v[0][Z], v[2][Y], v[2][Z], ae[Z], ae[Y], h, clo, V); break;
+        r = edge_test32(e[Z], e[Y], false, v[0][Y], v[0][Z], v[2][Y], v[2][Z], ae[Z], ae[Y], h, clo, cd); break;
       case 1: case 4:  // Y02: -a*v.x + b*v.z, a=e.z, b=e.x over v0, v2
-        r = edge_test32(e[Z], e[X], true, v[0][X], v[0][Z], v[2][X], v[2][Z], ae[Z], ae[X], h, clo, V); break;
+        r = edge_test32(e[Z], e[X], true, v[0][X], v[0][Z], v[2][X], v[2][Z], ae[Z], ae[X], h, clo, cd); break;
       case 2: case 8:  // Z12: a=e.y, b=e.x over v1, v2 on (x, y)
-        r = edge_test32(e[Y], e[X], false, v[1][X], v[1][Y], v[2][X], v[2][Y], ae[Y], ae[X], h, clo, V); break;
+        r = edge_test32(e[Y], e[X], false, v[1][X], v[1][Y], v[2][X], v[2][Y], ae[Y], ae[X], h, clo, cd); break;
       case 5:          // Z0: over v0, v1
-        r = edge_test32(e[Y], e[X], false, v[0][X], v[0][Y], v[1][X], v[1][Y], ae[Y], ae[X], h, clo, V); break;
+        r = edge_test32(e[Y], e[X], false, v[0][X], v[0][Y], v[1][X], v[1][Y], ae[Y], ae[X], h, clo, cd); break;
       case 6:          // X2: over v0, v1
-        r = edge_test32(e[Z], e[Y], false, v[0][Y], v[0][Z], v[1][Y], v[1][Z], ae[Z], ae[Y], h, clo, V); break;
+        r = edge_test32(e[Z], e[Y], false, v[0][Y], v[0][Z], v[1][Y], v[1][Z], ae[Z], ae[Y], h, clo, cd); break;
       default:         // 7, Y1: over v0, v1
-        r = edge_test32(e[Z], e[X], true, v[0][X], v[0][Z], v[1][X], v[1][Z], ae[Z], ae[X], h, clo, V); break;
+        r = edge_test32(e[Z], e[X], true, v[0][X], v[0][Z], v[1][X], v[1][Z], ae[Z], ae[X], h, clo, cd); break;
     }
     if (r == kTrue) return false;
     if (r == kUnknown && need64(3 + k)) return false;

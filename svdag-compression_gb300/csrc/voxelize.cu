@@ -63,11 +63,13 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(VoxParams P, const fl
   __shared__ float s_t[9][kExpandThreads];
   __shared__ float s_nb[8][kExpandThreads];
   __shared__ float s_vmax[6][kExpandThreads];
+  __shared__ float s_e[9][kExpandThreads];
   __shared__ uint32_t s_tri[kExpandThreads], s_node[kExpandThreads], s_slab[kExpandThreads];
   __shared__ uint32_t s_hits[kExpandThreads];
   __shared__ uint16_t s_queue[8 * kExpandThreads];
   __shared__ uint32_t s_qn;
   const double k = child_half_side(P.root_side, P.level);
+  const float hf = float(k);
   const bool leaf = (P.level == P.leaf_level);
   const int tid = threadIdx.x;
   unsigned fb = 0;
@@ -90,15 +92,18 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(VoxParams P, const fl
       nb.chi[4] = b.x; nb.chi[5] = b.y; nb.clo = b.z; nb.ok = b.w;
       sat::Pair32 PP;
       sat::pair_setup(tri, tp, ctr + 3ull * node, nb, k, PP);
+      uint32_t full = 0;
       for (int ci = 7; ci >= 0; --ci) {
         const int f = sat::child_fast(PP, ci);
-        if (f == 1) {
-          hits |= 1u << ci;
-        } else if (f == 2) {
-          const uint32_t slot = atomicAdd(&s_qn, 1u);
-          s_queue[slot] = uint16_t((tid << 3) | ci);
-        }
+        if (f == 1) hits |= 1u << ci;
+        else if (f == 2) full |= 1u << ci;
       }
+      if (full) {  // this pair's undecided children in consecutive queue slots
+        uint32_t slot = atomicAdd(&s_qn, uint32_t(__popc(full)));
+        for (uint32_t m = full; m; m &= m - 1) s_queue[slot++] = uint16_t((tid << 3) | (__ffs(m) - 1));
+      }
+#pragma unroll
+      for (int j = 0; j < 9; ++j) s_e[j][tid] = PP.e[j / 3][j % 3];
 #pragma unroll
       for (int j = 0; j < 9; ++j) s_t[j][tid] = tri[j];
 #pragma unroll
@@ -107,7 +112,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(VoxParams P, const fl
       s_nb[7][tid] = nb.ok;
       s_tri[tid] = t;
       s_node[tid] = node;
-      s_slab[tid] = PP.slab | (PP.tang << 16);  // slab classes (12 bits) + tangency (6 bits)
+      s_slab[tid] = PP.slab | (PP.tang << 16) | (PP.fast ? 0x80000000u : 0u);  // classes, tangency, fp32 path
     }
     s_hits[tid] = hits;
     __syncthreads();
@@ -125,10 +130,22 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(VoxParams P, const fl
       nb.clo = s_nb[6][slot];
       nb.ok = s_nb[7][slot];
       const uint32_t node = s_node[slot];
+      const uint32_t word = s_slab[slot];
       sat::Pair32 PP;
-      sat::pair_basic(tri, tris + 9ull * s_tri[slot], ctr + 3ull * node, nb, k, PP);
-      PP.slab = s_slab[slot] & 0xFFFFu;
-      PP.tang = s_slab[slot] >> 16;
+#pragma unroll
+      for (int j = 0; j < 9; ++j) {
+        PP.t[j] = tri[j];
+        PP.e[j / 3][j % 3] = s_e[j][slot];
+        PP.ae[j / 3][j % 3] = fabsf(PP.e[j / 3][j % 3]);
+      }
+      PP.nb = nb;
+      PP.h = hf;
+      PP.fast = (word >> 31) != 0u;
+      PP.slab = word & 0xFFFFu;
+      PP.tang = (word >> 16) & 0x3Fu;
+      PP.tp = tris + 9ull * s_tri[slot];
+      PP.c = ctr + 3ull * node;
+      PP.k = k;
 #pragma unroll
       for (int j = 0; j < 6; ++j) PP.vmax[j] = s_vmax[j][slot];
       if (sat::child_full(PP, ci, &fb)) atomicOr(&s_hits[slot], 1u << ci);
@@ -324,7 +341,7 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
                    L.ctr.get(), L.nbox.get(), L.hdr.get(), firstq.get(), hits.get(), d_fb.get());
     if (leaf) break;
 
-    // --- create level l+1 in reference creation order
+    // --- counts of level l+1 and of the next frontier (one host sync)
     const uint64_t slots = 8 * L.n;
     const uint64_t words = (8 * F + 31) / 32;
     DBuf<uint32_t> bitmap(words ? words : 1, st), woff(words ? words : 1, st);
@@ -332,7 +349,17 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
     SVDAG_LAUNCH(ex, k_mark_keys, grid_for(ex, slots, 256), 256, 0, firstq.get(), slots, bitmap.get());
     DBuf<uint32_t> d_n32(1, st);
     device_exclusive_scan<uint32_t>(ex, PopcIn{bitmap.get()}, words, U32Out{woff.get()}, d_n32.get());
-    const uint64_t n_next = read_scalar(ex, d_n32.get());
+    DBuf<uint32_t> off(F ? F : 1, st);
+    device_exclusive_scan<uint64_t>(ex, PopcU8In{hits.get()}, F, U64to32Out{off.get()}, d_total.get());
+    uint64_t F_next = 0;
+    uint32_t n32 = 0;
+    SVDAG_CUDA(cudaMemcpyAsync(&n32, d_n32.get(), 4, cudaMemcpyDeviceToHost, st));
+    SVDAG_CUDA(cudaMemcpyAsync(&F_next, d_total.get(), 8, cudaMemcpyDeviceToHost, st));
+    SVDAG_CUDA(cudaStreamSynchronize(st));
+    if (F_next >= (1ull << 32)) throw Error(SVDAG_ERR_OVERFLOW, "voxelize: frontier exceeds 2^32 pairs");
+
+    // --- create level l+1 in reference creation order
+    const uint64_t n_next = n32;
     Level& N = c.lev[l + 1];
     N.n = n_next;
     L.ch.alloc(slots, st);
@@ -348,10 +375,6 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
     woff.release();
 
     // --- next frontier
-    DBuf<uint32_t> off(F ? F : 1, st);
-    device_exclusive_scan<uint64_t>(ex, PopcU8In{hits.get()}, F, U64to32Out{off.get()}, d_total.get());
-    const uint64_t F_next = read_scalar(ex, d_total.get());
-    if (F_next >= (1ull << 32)) throw Error(SVDAG_ERR_OVERFLOW, "voxelize: frontier exceeds 2^32 pairs");
     DBuf<uint32_t> nf_tri(F_next ? F_next : 1, st), nf_node(F_next ? F_next : 1, st);
     if (F)
       SVDAG_LAUNCH(ex, k_emit_frontier, grid_for(ex, F, 256), 256, 0, f_tri.get(), f_node.get(), F, hits.get(),
