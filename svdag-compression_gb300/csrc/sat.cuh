@@ -82,6 +82,11 @@ SAT_HD F2 f2mul(F2 a, F2 b) { const float2 r = __fmul2_rn(make_float2(a.x, a.y),
 SAT_HD F2 f2add(F2 a, F2 b) { return {fadd(a.x, b.x), fadd(a.y, b.y)}; }
 SAT_HD F2 f2mul(F2 a, F2 b) { return {fmul(a.x, b.x), fmul(a.y, b.y)}; }
 #endif
+#if defined(__CUDA_ARCH__)
+SAT_HD int __builtin_ctz_(uint32_t m) { return __ffs(int(m)) - 1; }
+#else
+SAT_HD int __builtin_ctz_(uint32_t m) { return __builtin_ctz(m); }
+#endif
 SAT_HD float fmin_(float a, float b) { return (b < a) ? b : a; }
 SAT_HD float fmax_(float a, float b) { return (a < b) ? b : a; }
 
@@ -404,6 +409,8 @@ struct Pair32 {
   uint32_t slab;     // 2 bits per (axis q, side s) at bit 2*(2q+s)
   uint32_t tang;     // bit 2q+s: grid-plane tangency on axis q, side s (see pair_slabs)
   float vmax[6];     // max_i |fl32(t_iq - chi)| per (axis, side)
+  float n[3], sn[3]; // plane normal e0 x e1 in fp32 and |m1| + |m2| per component
+  float nh;          // fl32(|n|_1 h)
   const float* tp;   // the triangle in its source buffer (fp64 predicates reload it)
   const double* c;   // parent centre (fp64), for predicates decided in fp64
   double k;          // child half side (fp64)
@@ -430,6 +437,21 @@ SAT_HD Tri tri_or(Tri a, Tri b) {
 
 // Builds the per-pair data; c = parent centre (fp64, kept by pointer),
 // nb = the node's child boxes, k = child half side.
+// Plane constants of a pair: n = e0 x e1 (fp32), sn_q = |m1| + |m2| of
+// component q, nh = fl32(|n|_1 h).
+SAT_HD void pair_plane(Pair32& P, float h) {
+  const float* e0 = P.e[0];
+  const float* e1 = P.e[1];
+  const float m0 = fmul(e0[1], e1[2]), m1 = fmul(e0[2], e1[1]);
+  const float m2 = fmul(e0[2], e1[0]), m3 = fmul(e0[0], e1[2]);
+  const float m4 = fmul(e0[0], e1[1]), m5 = fmul(e0[1], e1[0]);
+  P.n[0] = fsub(m0, m1); P.n[1] = fsub(m2, m3); P.n[2] = fsub(m4, m5);
+  P.sn[0] = fadd(fabsf_(m0), fabsf_(m1));
+  P.sn[1] = fadd(fabsf_(m2), fabsf_(m3));
+  P.sn[2] = fadd(fabsf_(m4), fabsf_(m5));
+  P.nh = fmul(fadd(fadd(fabsf_(P.n[0]), fabsf_(P.n[1])), fabsf_(P.n[2])), h);
+}
+
 // Triangle, node and edge data of a pair (no slab classification).
 SAT_HD void pair_basic(const float t[9], const float* tp, const double* c, const NodeBoxes& nb, double k,
                        Pair32& P) {
@@ -445,6 +467,7 @@ SAT_HD void pair_basic(const float t[9], const float* tp, const double* c, const
     P.e[2][q] = fsub(t[q], t[6 + q]);
     for (int j = 0; j < 3; ++j) P.ae[j][q] = fabsf_(P.e[j][q]);
   }
+  pair_plane(P, float(k));
   P.nb = nb;
   P.h = float(k);
   P.fast = ok;
@@ -555,6 +578,27 @@ SAT_HD Tri edge_test32(float a, float b, bool neg_a, float u0, float w0, float u
   return kUnknown;
 }
 
+// Edge-axis test with box-level thresholds: 1 reject, 0 keep, 2 unknown.
+// ab = fl(|a| + |b|), hW = fl(h + Wp), hmW = fl(h - Wp).  With
+// Wp >= 4.7 u32 V + 4.4 u32 h + 1.05 clo the thresholds
+//   hi = fl(ab hW + cd) >= rad* + (|a|+|b|)(4.1 u32 V + 1.02 clo) + fp64 errors,
+//   lo = fl(ab hmW - cd) <= rad* - (the same)
+// hold after every rounding (|a*|+|b*| <= ab (1 + 2.02 u32)), so
+//   min p > hi or max p < -hi -> certain reject,
+//   min p < lo and max p > -lo -> certain keep.
+SAT_HD int edge_test_box(float a, float b, bool neg_a, float u0, float w0, float u1, float w1, float ab, float hW,
+                         float hmW, float cd) {
+  const F2 x = f2mul(F2{a, a}, F2{u0, u1});
+  const F2 y = f2mul(F2{b, b}, F2{w0, w1});
+  F2 p = f2add(x, F2{-y.x, -y.y});
+  if (neg_a) p = F2{-p.x, -p.y};
+  const float mn = fmin_(p.x, p.y), mx = fmax_(p.x, p.y);
+  const float hi = ffma(ab, hW, cd), lo = ffma(ab, hmW, -cd);
+  if (mn > hi || mx < -hi) return 1;
+  if (mn < lo && mx > -lo) return 0;
+  return 2;
+}
+
 // Decision from the slab classes alone: 0 no overlap, 1 overlap, 2 the
 // full test is needed.
 SAT_HD int child_fast(const Pair32& P, int ci) {
@@ -585,16 +629,17 @@ SAT_HD bool child_full(const Pair32& P, int ci, unsigned* fallbacks) {
   const float chi[3] = {sx ? P.nb.chi[1] : P.nb.chi[0], sy ? P.nb.chi[3] : P.nb.chi[2], sz ? P.nb.chi[5] : P.nb.chi[4]};
   for (int i = 0; i < 3; ++i)
     for (int q = 0; q < 3; ++q) v[i][q] = fsub(P.t[3 * i + q], chi[q]);
+  // V >= |t - c| and >= |v_f| over this box
   float V = sx ? P.vmax[1] : P.vmax[0];
-  const float vy = sy ? P.vmax[3] : P.vmax[2], vz = sz ? P.vmax[5] : P.vmax[4];
-  V = (vy > V) ? vy : V;
-  V = (vz > V) ? vz : V;
-  V = fadd(fmul(V, 1.0000003f), fmul(1.01f, clo));
-  // fp64-side and absolute error terms of the edge tests: 2^-47 (V^2 + V h) + 2^-100
+  V = fmax_(V, sy ? P.vmax[3] : P.vmax[2]);
+  V = fmax_(V, sz ? P.vmax[5] : P.vmax[4]);
+  V = ffma(V, 1.0000003f, 1.01f * clo);
+  // fp64-side and absolute error terms: 2^-47 (V^2 + V h) + 2^-100
   const float cd = ffma(kD64, fmul(V, fadd(V, h)), kTiny);
 
-  // undecided predicate: exact fp32 tier when the box centre is an fp32
-  // value, else (or when inexact) the reference's fp64 evaluation
+  // undecided predicate: tangency rule, then the exact fp32 tier when the box
+  // centre is an fp32 value, else (or when inexact) the reference's fp64
+  // evaluation
   auto need64 = [&](int which) {
     if (clo == 0.f && which >= 3 && which < 12 && edge_tangent(P.tp, chi[0], chi[1], chi[2], h, which - 3)) return false;
     if (clo == 0.f) {
@@ -615,8 +660,14 @@ SAT_HD bool child_full(const Pair32& P, int ci, unsigned* fallbacks) {
   if (cy == kSlabUnsure && !ty && need64(1)) return false;
   if (cz == kSlabUnsure && !tz && need64(2)) return false;
 
-  // nine edge-axis tests (test_triangle_box.cpp:137-156)
+  // nine edge-axis tests (test_triangle_box.cpp:137-156).  Per box:
+  //   |p_f - p*| + |rad_f - rad*| <= (|a| + |b|)(4.1 u32 V + 3.1 u32 h + 1.02 clo)
+  // so the thresholds are ab (h +- Wp) +- cd with Wp covering that and the
+  // roundings of the thresholds themselves (see edge_test_box).
+  const float Wp = ffma(4.7f * kU32, V, ffma(4.4f * kU32, h, 1.05f * clo));
+  const float hW = fadd(h, Wp), hmW = fsub(h, Wp);
   const int X = 0, Y = 1, Z = 2;
+  uint32_t rej = 0, unk = 0;
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     if ((k == 0 || k == 3 || k == 6) && passX) continue;
@@ -625,62 +676,53 @@ SAT_HD bool child_full(const Pair32& P, int ci, unsigned* fallbacks) {
     const int j = k / 3;
     const float* e = P.e[j];
     const float* ae = P.ae[j];
-    Tri r;
+    int r;
     switch (k) {
       case 0: case 3:  // X01: a=e.z, b=e.y over v0, v2 on (y, z)
-        r = edge_test32(e[Z], e[Y], false, v[0][Y], v[0][Z], v[2][Y], v[2][Z], ae[Z], ae[Y], h, clo, cd); break;
+        r = edge_test_box(e[Z], e[Y], false, v[0][Y], v[0][Z], v[2][Y], v[2][Z], fadd(ae[Z], ae[Y]), hW, hmW, cd); break;
       case 1: case 4:  // Y02: -a*v.x + b*v.z, a=e.z, b=e.x over v0, v2
-        r = edge_test32(e[Z], e[X], true, v[0][X], v[0][Z], v[2][X], v[2][Z], ae[Z], ae[X], h, clo, cd); break;
+        r = edge_test_box(e[Z], e[X], true, v[0][X], v[0][Z], v[2][X], v[2][Z], fadd(ae[Z], ae[X]), hW, hmW, cd); break;
       case 2: case 8:  // Z12: a=e.y, b=e.x over v1, v2 on (x, y)
-        r = edge_test32(e[Y], e[X], false, v[1][X], v[1][Y], v[2][X], v[2][Y], ae[Y], ae[X], h, clo, cd); break;
+        r = edge_test_box(e[Y], e[X], false, v[1][X], v[1][Y], v[2][X], v[2][Y], fadd(ae[Y], ae[X]), hW, hmW, cd); break;
       case 5:          // Z0: over v0, v1
-        r = edge_test32(e[Y], e[X], false, v[0][X], v[0][Y], v[1][X], v[1][Y], ae[Y], ae[X], h, clo, cd); break;
+        r = edge_test_box(e[Y], e[X], false, v[0][X], v[0][Y], v[1][X], v[1][Y], fadd(ae[Y], ae[X]), hW, hmW, cd); break;
       case 6:          // X2: over v0, v1
-        r = edge_test32(e[Z], e[Y], false, v[0][Y], v[0][Z], v[1][Y], v[1][Z], ae[Z], ae[Y], h, clo, cd); break;
+        r = edge_test_box(e[Z], e[Y], false, v[0][Y], v[0][Z], v[1][Y], v[1][Z], fadd(ae[Z], ae[Y]), hW, hmW, cd); break;
       default:         // 7, Y1: over v0, v1
-        r = edge_test32(e[Z], e[X], true, v[0][X], v[0][Z], v[1][X], v[1][Z], ae[Z], ae[X], h, clo, cd); break;
+        r = edge_test_box(e[Z], e[X], true, v[0][X], v[0][Z], v[1][X], v[1][Z], fadd(ae[Z], ae[X]), hW, hmW, cd); break;
     }
-    if (r == kTrue) return false;
-    if (r == kUnknown && need64(3 + k)) return false;
+    rej |= uint32_t(r == 1) << k;
+    unk |= uint32_t(r == 2) << k;
   }
+  if (rej) return false;  // one certain reject decides the AND of the 13 tests
+  for (uint32_t m = unk; m; m &= m - 1)
+    if (need64(3 + (__builtin_ctz_(m)))) return false;
 
   if (tx || ty || tz) return true;  // the plane test passes on a tangent grid plane
 
-  // plane test: normal = e0 x e1; vmin/vmax by the sign of each component.
-  const float* e0 = P.e[0];
-  const float* e1 = P.e[1];
-  const float m0 = fmul(e0[1], e1[2]), m1 = fmul(e0[2], e1[1]);
-  const float m2 = fmul(e0[2], e1[0]), m3 = fmul(e0[0], e1[2]);
-  const float m4 = fmul(e0[0], e1[1]), m5 = fmul(e0[1], e1[0]);
-  const float n[3] = {fsub(m0, m1), fsub(m2, m3), fsub(m4, m5)};
-  const float sn[3] = {fadd(fabsf_(m0), fabsf_(m1)), fadd(fabsf_(m2), fabsf_(m3)), fadd(fabsf_(m4), fabsf_(m5))};
-  bool plane_unknown = false;
-  float vmin[3], vmax[3], W[3];
-  for (int q = 0; q < 3; ++q) {
-    // |n_f - n*| <= 4.1 u32 sn; fp64 side <= 2^-47 V^2
-    const float tn = fadd(fadd(fmul(4.2f * kU32, sn[q]), fmul(kD64, fmul(V, V))), kTiny);
-    if (n[q] > tn) { vmin[q] = fsub(-h, v[0][q]); vmax[q] = fsub(h, v[0][q]); }
-    else if (n[q] < -tn) { vmin[q] = fsub(h, v[0][q]); vmax[q] = fsub(-h, v[0][q]); }
-    else { plane_unknown = true; break; }
-    W[q] = fmul(fadd(h, fabsf_(v[0][q])), 1.0000003f);
-  }
-  if (!plane_unknown) {
-    // |dot_f - dot*| <= 9.5 u32 sum sn_q (W_q + |v0_q|) + 1.1 clo sum sn_q; fp64 side <= 2^-42 V^2 (V + h)
-    float acc = 0.f, accs = 0.f;
-    for (int q = 0; q < 3; ++q) {
-      acc = fadd(acc, fmul(sn[q], fadd(W[q], fabsf_(v[0][q]))));
-      accs = fadd(accs, sn[q]);
-    }
-    const float td = fadd(fadd(fmul(9.6f * kU32, acc), fmul(1.1f, fmul(clo, accs))),
-                          fadd(fmul(32.f * kD64, fmul(fmul(V, V), fadd(V, h))), kTiny));
-    const float dmin = fadd(fadd(fmul(n[0], vmin[0]), fmul(n[1], vmin[1])), fmul(n[2], vmin[2]));
-    const Tri rmin = gt(dmin, 0.f, td);  // reference: dmin > 0 -> reject
-    if (rmin == kTrue) return false;
-    if (rmin == kFalse) {
-      const float dmax = fadd(fadd(fmul(n[0], vmax[0]), fmul(n[1], vmax[1])), fmul(n[2], vmax[2]));
-      const Tri rmax = gt(dmax, 0.f, td);  // reference: dmax >= 0 -> overlap
-      if (rmax == kTrue) return true;
-      if (rmax == kFalse) return false;
+  // plane test with the pair's normal n = e0 x e1 (pair constants n, sn, nh):
+  //   dmin* = -(|n|_1 h + n.v0),  dmax* = |n|_1 h - n.v0
+  // once every component's sign is certain (the reference picks each box
+  // corner by sign(n_q)).
+  //   |n_f - n*| <= 4.1 u32 sn_q;  |nh_f - nh*| <= 7.2 u32 h sum sn
+  //   |d_f - d*| <= 8.2 u32 h sum sn + 9.2 u32 sum sn_q |v0_q| + clo sum sn
+  //   fp64 side <= 2^-42 V^2 (V + h)
+  const float tn0 = ffma(kD64, fmul(V, V), kTiny);
+  bool sure = true;
+  for (int q = 0; q < 3; ++q) sure = sure && (fabsf_(P.n[q]) > ffma(4.2f * kU32, P.sn[q], tn0));
+  if (sure) {
+    const float nd = fadd(fadd(fmul(P.n[0], v[0][0]), fmul(P.n[1], v[0][1])), fmul(P.n[2], v[0][2]));
+    const float dmin = -fadd(P.nh, nd);
+    const float dmax = fsub(P.nh, nd);
+    const float snsum = fadd(fadd(P.sn[0], P.sn[1]), P.sn[2]);
+    const float snv = ffma(P.sn[0], fabsf_(v[0][0]), ffma(P.sn[1], fabsf_(v[0][1]), fmul(P.sn[2], fabsf_(v[0][2]))));
+    const float td = ffma(8.7f * kU32 * h, snsum,
+                          ffma(9.7f * kU32, snv, ffma(1.06f * clo, snsum,
+                                                     ffma(32.f * kD64, fmul(fmul(V, V), fadd(V, h)), kTiny))));
+    if (dmin > td) return false;                 // reference: dmin > 0 -> reject
+    if (dmin < -td) {
+      if (dmax > td) return true;                // dmax >= 0 -> overlap
+      if (dmax < -td) return false;
     }
   }
   return !need64(12);

@@ -64,6 +64,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(VoxParams P, const fl
   __shared__ float s_nb[8][kExpandThreads];
   __shared__ float s_vmax[6][kExpandThreads];
   __shared__ float s_e[9][kExpandThreads];
+  __shared__ float s_pl[7][kExpandThreads];  // plane normal, |m1|+|m2| per component, |n|_1 h
   __shared__ uint32_t s_tri[kExpandThreads], s_node[kExpandThreads], s_slab[kExpandThreads];
   __shared__ uint32_t s_hits[kExpandThreads];
   __shared__ uint16_t s_queue[8 * kExpandThreads];
@@ -110,6 +111,9 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(VoxParams P, const fl
       for (int j = 0; j < 6; ++j) { s_nb[j][tid] = nb.chi[j]; s_vmax[j][tid] = PP.vmax[j]; }
       s_nb[6][tid] = nb.clo;
       s_nb[7][tid] = nb.ok;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) { s_pl[j][tid] = PP.n[j]; s_pl[3 + j][tid] = PP.sn[j]; }
+      s_pl[6][tid] = PP.nh;
       s_tri[tid] = t;
       s_node[tid] = node;
       s_slab[tid] = PP.slab | (PP.tang << 16) | (PP.fast ? 0x80000000u : 0u);  // classes, tangency, fp32 path
@@ -148,6 +152,9 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(VoxParams P, const fl
       PP.k = k;
 #pragma unroll
       for (int j = 0; j < 6; ++j) PP.vmax[j] = s_vmax[j][slot];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) { PP.n[j] = s_pl[j][slot]; PP.sn[j] = s_pl[3 + j][slot]; }
+      PP.nh = s_pl[6][slot];
       if (sat::child_full(PP, ci, &fb)) atomicOr(&s_hits[slot], 1u << ci);
     }
     __syncthreads();
