@@ -129,6 +129,38 @@ int svdag_level_device_ptrs(const svdag_ctx* ctx, uint32_t level, const uint32_t
 int svdag_profile_enable(svdag_ctx* ctx, int enable);
 int svdag_profile_report(svdag_ctx* ctx, char* buf, uint64_t capacity);
 
+/* toDAG without allocating (no counterpart in the reference, whose toDAG,
+ * src/symvox/geom_octree.cpp:462-548, works in host containers).
+ *
+ * Same result as svdag_reduce_dag, but every temporary (hash table, scan
+ * sums, compacted level) lives in one file-scope __device__ array of
+ * SVDAG_NOALLOC_SCRATCH_BYTES per device, and each reduced level is copied
+ * back into the front of the buffers it already has.  No cudaMalloc,
+ * cudaMallocAsync, cudaFree or allocating library call is made.  For callers
+ * that must not allocate device memory in the middle of their work: a
+ * renderer or streaming system that has already committed the GPU's memory
+ * to its own pools (an allocation there fails with out-of-memory, or grows
+ * a pool the caller accounts for), or a caller whose memory budget is
+ * enforced outside the CUDA allocator.
+ *
+ * Limit: every inner level (not the root, not the leaves) must fit the
+ * scratch.  Levels of up to SVDAG_NOALLOC_MAX_LEVEL_NODES nodes always fit;
+ * somewhat larger ones may.  A tree that does not fit is rejected with
+ * SVDAG_ERR_OVERFLOW before any work is queued, the octree unchanged and
+ * svdag_last_error() naming the level; svdag_reduce_dag has no such limit.
+ *
+ * The array is shared by every context on a device: calls whose work
+ * overlaps in time (two threads, or two streams in flight at once) race on
+ * it and corrupt each other; serialise them.  Its contents need not be zero:
+ * each call clears what it reads first.  The first call on a device looks
+ * the array up (cudaGetSymbolAddress, which can load the module and commit
+ * its memory); make that first call before any stream capture begins.  Like
+ * svdag_reduce_dag, the call synchronises its stream once per level and on
+ * return.  Per-kernel profiling (svdag_profile_enable) does not cover it. */
+#define SVDAG_NOALLOC_SCRATCH_BYTES (64ull << 20)
+#define SVDAG_NOALLOC_MAX_LEVEL_NODES 1048576ull
+int svdag_reduce_dag_noalloc(svdag_ctx* ctx);
+
 #ifdef __cplusplus
 }
 #endif

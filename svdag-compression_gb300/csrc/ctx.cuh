@@ -56,6 +56,8 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bbox[6]);
 void phase_reduce_dag(Ctx& c);
 void phase_reduce_sdag(Ctx& c);
 void phase_cross_level_merge(Ctx& c);
+// toDAG with every temporary in caller-provided device scratch (no allocation).
+void phase_reduce_dag_scratch(Ctx& c, uint8_t* scratch, uint64_t capacity);
 
 }  // namespace svdag
 

@@ -21,6 +21,8 @@
 // undecided nodes resolve the dependency chains (the lowest undecided index
 // always resolves, so rounds terminate) and give exactly the sequential
 // result.
+#include <algorithm>
+
 #include "ctx.cuh"
 #include "dedup.cuh"
 
@@ -432,6 +434,145 @@ void phase_reduce_sdag(Ctx& c) {
   c.st.n_nodes_sdag = nnodes;
   c.st.n_nodes = nnodes;
   c.state = SVDAG_S_SDAG;
+}
+
+// ---------------------------------------------------------------------------
+// toDAG on caller-provided device scratch: the same kernels and the same
+// result as phase_reduce_dag, with every temporary placed in `scratch` and
+// each reduced level copied back to the front of its own buffers (a level
+// only shrinks), so nothing is allocated.
+//
+// Scratch layout (offsets 256-byte aligned):
+//   head [0, 4096):  error flag, level count, leaf first/rank/output tables
+//   inner level of n nodes, from 4096:
+//     A  max(8 * table slots, 32 n): hash table, then the compacted children
+//     B  4 n: slot per node, then the compacted headers
+//     rep, newid, corr: 4 n each;  tile sums and offsets of the scan
+// Nothing has to be zero beforehand: the error flag, the hash table and the
+// leaf first-occurrence table are cleared on the stream before their first
+// read, on every call.
+namespace {
+
+constexpr uint64_t kHeadErr = 0, kHeadCnt = 64, kHeadFirst = 256, kHeadRank = 1280, kHeadLeafOut = 2304;
+constexpr uint64_t kHeadBytes = 4096;
+
+inline uint64_t align256(uint64_t x) { return (x + 255) & ~uint64_t(255); }
+
+struct InnerLayout {
+  uint64_t slots, table, slot_of, rep, newid, corr, sums, offs, end;
+};
+
+InnerLayout inner_layout(uint64_t n) {
+  InnerLayout L;
+  const uint64_t m = n ? n : 1;
+  const uint64_t nb = (m + kScanTile - 1) / kScanTile;
+  L.slots = next_pow2(n < 16 ? 32 : 2 * n);
+  L.table = kHeadBytes;
+  L.slot_of = L.table + align256(std::max<uint64_t>(8 * L.slots, 32 * m));
+  L.rep = L.slot_of + align256(4 * m);
+  L.newid = L.rep + align256(4 * m);
+  L.corr = L.newid + align256(4 * m);
+  L.sums = L.corr + align256(4 * m);
+  L.offs = L.sums + align256(4 * nb);
+  L.end = L.offs + align256(4 * nb);
+  return L;
+}
+
+// Exclusive scan with the tile sums and offsets in scratch (n <= kScanTile^2).
+template <class T, class In, class Out>
+void scan_in_scratch(const Exec& ex, In in, uint64_t n, Out out, T* d_total, T* sums, T* offs) {
+  if (n == 0) {
+    SVDAG_CUDA(cudaMemsetAsync(d_total, 0, sizeof(T), ex.stream));
+    return;
+  }
+  const uint64_t nb = (n + kScanTile - 1) / kScanTile;
+  SVDAG_LAUNCH(ex, (k_scan_tile_sums<T, In>), unsigned(nb), kScanThreads, 0, in, n, sums);
+  if (nb == 1)
+    SVDAG_CUDA(cudaMemsetAsync(offs, 0, sizeof(T), ex.stream));
+  else
+    SVDAG_LAUNCH(ex, (k_scan_tile_emit<T, ArrayIn<T>, ArrayOut<T>>), 1, kScanThreads, 0, ArrayIn<T>{sums}, nb,
+                 (const T*)nullptr, ArrayOut<T>{offs});
+  SVDAG_LAUNCH(ex, (k_scan_tile_emit<T, In, Out>), unsigned(nb), kScanThreads, 0, in, n, (const T*)offs, out);
+  SVDAG_LAUNCH(ex, k_store_total<T>, 1, 32, 0, sums, offs, nb, d_total);
+}
+
+}  // namespace
+
+void phase_reduce_dag_scratch(Ctx& c, uint8_t* scratch, uint64_t capacity) {
+  if (c.state != SVDAG_S_SVO && c.state != SVDAG_S_DAG)
+    throw Error(SVDAG_ERR_INVALID_STATE, "toDAG: the octree is not an SVO or DAG");
+  // every level is checked against the scratch before any work is queued,
+  // so a rejected call leaves the octree untouched
+  for (uint32_t lev = 1; lev + 1 < c.levels; ++lev) {
+    const uint64_t n = c.lev[lev].n;
+    const uint64_t need = inner_layout(n).end;
+    if (need > capacity || (n + kScanTile - 1) / kScanTile > kScanTile)
+      throw Error(SVDAG_ERR_OVERFLOW, "toDAG with static scratch: level " + std::to_string(lev) + " has " +
+                                          std::to_string(n) + " nodes and needs " + std::to_string(need) +
+                                          " bytes of scratch, above the " + std::to_string(capacity) +
+                                          " bytes available (svdag_reduce_dag has no such limit)");
+  }
+  if (capacity < kHeadBytes) throw Error(SVDAG_ERR_OVERFLOW, "toDAG with static scratch: scratch too small");
+  Exec ex = c.ex;
+  ex.prof = nullptr;  // per-launch events would be created on demand
+  const cudaStream_t st = c.stream;
+  int* d_err = reinterpret_cast<int*>(scratch + kHeadErr);
+  uint32_t* d_cnt = reinterpret_cast<uint32_t*>(scratch + kHeadCnt);
+  SVDAG_CUDA(cudaMemsetAsync(d_err, 0, 4, st));
+  uint64_t nnodes = 1;
+  for (uint32_t lev = c.levels - 1; lev > 0; --lev) {
+    Level& L = c.lev[lev];
+    Level& P = c.lev[lev - 1];
+    const uint64_t n = L.n;
+    if (lev == c.levels - 1) {
+      uint32_t* first = reinterpret_cast<uint32_t*>(scratch + kHeadFirst);
+      uint32_t* rank = reinterpret_cast<uint32_t*>(scratch + kHeadRank);
+      uint32_t* out_hdr = reinterpret_cast<uint32_t*>(scratch + kHeadLeafOut);
+      fill<uint32_t>(ex, first, 256, kNone);
+      if (n) SVDAG_LAUNCH(ex, k_leaf_first, grid_for(ex, n, 256, 4), 256, 0, L.hdr.get(), n, first);
+      SVDAG_LAUNCH(ex, k_leaf_rank, 1, 256, 0, first, rank, out_hdr, d_cnt);
+      if (P.n)
+        SVDAG_LAUNCH(ex, k_remap_parents_leafrank, grid_for(ex, P.n, 256), 256, 0, P.hdr.get(), P.ch.get(), P.n,
+                     L.hdr.get(), rank);
+      const uint64_t d = read_scalar(ex, d_cnt);
+      if (d) SVDAG_CUDA(cudaMemcpyAsync(L.hdr.get(), out_hdr, 4 * d, cudaMemcpyDeviceToDevice, st));
+      L.n = d;
+    } else {
+      const InnerLayout Y = inner_layout(n);
+      unsigned long long* slots = reinterpret_cast<unsigned long long*>(scratch + Y.table);
+      uint32_t* slot_of = reinterpret_cast<uint32_t*>(scratch + Y.slot_of);
+      uint32_t* rep = reinterpret_cast<uint32_t*>(scratch + Y.rep);
+      uint32_t* newid = reinterpret_cast<uint32_t*>(scratch + Y.newid);
+      uint32_t* corr = reinterpret_cast<uint32_t*>(scratch + Y.corr);
+      SVDAG_CUDA(cudaMemsetAsync(slots, 0xFF, Y.slots * 8, st));
+      const Table T{slots, Y.slots - 1};
+      if (n) {
+        SVDAG_LAUNCH(ex, k_insert, grid_for(ex, n, 256), 256, 0, T, L.hdr.get(), L.ch.get(), n, slot_of, d_err);
+        SVDAG_LAUNCH(ex, k_rep, grid_for(ex, n, 256), 256, 0, T, slot_of, n, rep);
+      }
+      scan_in_scratch<uint32_t>(ex, RepFlagIn{rep}, n, U32Out{newid}, d_cnt, reinterpret_cast<uint32_t*>(scratch + Y.sums),
+                                reinterpret_cast<uint32_t*>(scratch + Y.offs));
+      const uint64_t d = read_scalar(ex, d_cnt);
+      // the table and the slots are dead after k_rep: their space takes the compacted level
+      uint32_t* out_ch = reinterpret_cast<uint32_t*>(scratch + Y.table);
+      uint32_t* out_hdr = slot_of;
+      if (n)
+        SVDAG_LAUNCH(ex, k_compact_dag, grid_for(ex, n, 256), 256, 0, L.hdr.get(), L.ch.get(), n, rep, newid, out_hdr,
+                     out_ch, corr);
+      if (P.n)
+        SVDAG_LAUNCH(ex, k_remap_parents, grid_for(ex, P.n, 256), 256, 0, P.hdr.get(), P.ch.get(), P.n, corr);
+      if (d) {
+        SVDAG_CUDA(cudaMemcpyAsync(L.hdr.get(), out_hdr, 4 * d, cudaMemcpyDeviceToDevice, st));
+        SVDAG_CUDA(cudaMemcpyAsync(L.ch.get(), out_ch, 32 * d, cudaMemcpyDeviceToDevice, st));
+      }
+      L.n = d;
+    }
+    nnodes += L.n;
+  }
+  check_err(ex, d_err, "toDAG");
+  c.st.n_nodes_dag = nnodes;
+  c.st.n_nodes = nnodes;
+  c.state = SVDAG_S_DAG;
 }
 
 }  // namespace svdag

@@ -75,6 +75,7 @@ GPU_SYMBOLS = {
     "svdag_import_level": (_I, [_VP, _U32, _U64, _VP, _VP]),
     "svdag_profile_enable": (_I, [_VP, _I]),
     "svdag_profile_report": (_I, [_VP, ctypes.c_char_p, _U64]),
+    "svdag_reduce_dag_noalloc": (_I, [_VP]),
 }
 
 HOST_SYMBOLS = {
@@ -234,6 +235,11 @@ class Octree:
 
     def toDAG(self):
         self._check(self._lib.svdag_reduce_dag(self._h))
+
+    def toDAG_noalloc(self):
+        """toDAG with the library's static device scratch (no allocation);
+        raises SvdagError (SVDAG_ERR_OVERFLOW) when a level does not fit."""
+        self._check(self._lib.svdag_reduce_dag_noalloc(self._h))
 
     def initChildLevels(self):
         self._check(self._lib.svdag_init_child_levels(self._h))

@@ -38,6 +38,7 @@ def test_status_strings_and_null_handles():
     assert lib.svdag_status_string(4) == b"out of device memory"
     assert lib.svdag_destroy(None) == 1
     assert lib.svdag_reduce_dag(None) == 1
+    assert lib.svdag_reduce_dag_noalloc(None) == 1
     assert lib.svdag_get_stats(None, None) == 1
 
 
