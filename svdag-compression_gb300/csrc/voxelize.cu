@@ -53,7 +53,10 @@ __host__ __device__ __forceinline__ double child_half_side(double root_side, uin
 // index per created child, and the mask for the next frontier.
 constexpr int kExpandThreads = 256;
 
-__global__ void __launch_bounds__(kExpandThreads) k_expand(VoxParams P, const float* __restrict__ tris,
+#ifndef SVDAG_EXPAND_MIN_BLOCKS
+#define SVDAG_EXPAND_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_expand(VoxParams P, const float* __restrict__ tris,
                                                            const uint32_t* __restrict__ f_tri,
                                                            const uint32_t* __restrict__ f_node, uint64_t F,
                                                            const double* __restrict__ ctr, const float* __restrict__ nbox,
@@ -158,17 +161,34 @@ __global__ void __launch_bounds__(kExpandThreads) k_expand(VoxParams P, const fl
       if (sat::child_full(PP, ci, &fb)) atomicOr(&s_hits[slot], 1u << ci);
     }
     __syncthreads();
-    if (q < F) {
-      const uint32_t h = s_hits[tid];
-      const uint32_t node = s_node[tid];
-      if (h) atomicOr(&hdr[node], h);
-      if (!leaf) {
-        hits_out[q] = uint8_t(h);
-        for (uint32_t m = h; m; m &= m - 1) {
-          const int i = __ffs(m) - 1;
-          atomicMin(&firstq[8ull * node + i], uint32_t(q));
+    {
+      // Publish per warp: lanes of the same node combine their hit masks and
+      // first pair indices (pair index = q - lane + lane', increasing with the
+      // lane), and one lane per node issues the atomics -- and only when the
+      // value does not already hold the result (both updates are monotone).
+      // On the upper levels thousands of pairs share a node, and unaggregated
+      // same-address atomics serialise.
+      const bool valid = q < F;
+      const uint32_t h = valid ? s_hits[tid] : 0u;
+      const uint32_t node = valid ? s_node[tid] : 0xFFFFFFFFu;
+      const int lane = tid & 31;
+      const unsigned grp = __match_any_sync(0xFFFFFFFFu, node);
+      const bool lead = valid && lane == __ffs(int(grp)) - 1;
+      uint32_t hg = 0;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const unsigned b = __ballot_sync(0xFFFFFFFFu, (h >> i) & 1u) & grp;
+        if (b) {
+          hg |= 1u << i;
+          if (lead && !leaf) {
+            uint32_t* fq = &firstq[8ull * node + i];
+            const uint32_t cand = uint32_t(q) - uint32_t(lane) + uint32_t(__ffs(int(b)) - 1);
+            if (__ldcg(fq) > cand) atomicMin(fq, cand);
+          }
         }
       }
+      if (lead && hg && (__ldcg(&hdr[node]) & hg) != hg) atomicOr(&hdr[node], hg);
+      if (valid && !leaf) hits_out[q] = uint8_t(h);
     }
     __syncthreads();
   }
