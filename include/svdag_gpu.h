@@ -81,7 +81,7 @@ const char* svdag_status_string(int status);
 int svdag_synchronize(svdag_ctx* ctx);
 
 /* Scene input: triangles as float[9] each (v0 v1 v2, xyz), the layout of
- * Scene::getTrianglePtr (src/symvox/scene.hpp:78).  upload copies from host
+ * Scene::getTrianglePtr (src/symvox/scene.hpp:90).  upload copies from host
  * memory; set_device borrows a device buffer that must outlive the build. */
 int svdag_upload_triangles(svdag_ctx* ctx, const float* host_tris, uint64_t n_tris);
 int svdag_set_device_triangles(svdag_ctx* ctx, const float* device_tris, uint64_t n_tris);

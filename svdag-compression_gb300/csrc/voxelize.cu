@@ -62,6 +62,7 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
                                                            const double* __restrict__ ctr, const float* __restrict__ nbox,
                                                            uint32_t* __restrict__ hdr, uint32_t* __restrict__ firstq,
                                                            uint8_t* __restrict__ hits_out,
+                                                           uint32_t* __restrict__ tile_hits,
                                                            unsigned long long* __restrict__ n_fallback) {
   __shared__ float s_t[9][kExpandThreads];
   __shared__ float s_nb[8][kExpandThreads];
@@ -72,6 +73,7 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
   __shared__ uint32_t s_hits[kExpandThreads];
   __shared__ uint16_t s_queue[8 * kExpandThreads];
   __shared__ uint32_t s_qn;
+  __shared__ uint32_t s_wsum[kExpandThreads / 32];
   const double k = child_half_side(P.root_side, P.level);
   const float hf = float(k);
   const bool leaf = (P.level == P.leaf_level);
@@ -188,9 +190,20 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
         }
       }
       if (lead && hg && (__ldcg(&hdr[node]) & hg) != hg) atomicOr(&hdr[node], hg);
-      if (valid && !leaf) hits_out[q] = uint8_t(h);
+      if (!leaf) {
+        if (valid) hits_out[q] = uint8_t(h);
+        // next-frontier entries of this tile (its offset comes from a scan of these)
+        const uint32_t wsum = __reduce_add_sync(0xFFFFFFFFu, uint32_t(__popc(h)));
+        if (lane == 0) s_wsum[tid >> 5] = wsum;
+      }
     }
     __syncthreads();
+    if (!leaf && tid == 0) {
+      uint32_t t = 0;
+#pragma unroll
+      for (int w = 0; w < kExpandThreads / 32; ++w) t += s_wsum[w];
+      tile_hits[base / kExpandThreads] = t;
+    }
   }
   unsigned long long sum = fb;
   for (int o = 16; o; o >>= 1) sum += __shfl_down_sync(0xFFFFFFFFu, sum, o);
@@ -211,9 +224,9 @@ struct PopcIn {
   const uint32_t* w;
   __device__ __forceinline__ uint32_t operator()(uint64_t i) const { return __popc(w[i]); }
 };
-struct PopcU8In {
-  const uint8_t* w;
-  __device__ __forceinline__ uint64_t operator()(uint64_t i) const { return __popc(uint32_t(w[i])); }
+struct U32toU64In {
+  const uint32_t* w;
+  __device__ __forceinline__ uint64_t operator()(uint64_t i) const { return w[i]; }
 };
 struct U32Out {
   uint32_t* a;
@@ -225,10 +238,15 @@ struct U64to32Out {
 };
 
 // Child ids = rank of the creation key; also the children's centres,
-// parent centre + (+-k) per axis (geom_octree.cpp:222-230).
+// parent centre + (+-k) per axis (geom_octree.cpp:222-230), and their child
+// boxes.  When the parent's child-box centres are exact fp32 values (tail 0),
+// the child's centre is one of them, and an fp32 sum whose TwoSum error is
+// zero is the fp64 sum too; then no fp64 arithmetic is needed.  Otherwise
+// (or when a sum is inexact) the centres are computed in fp64.
 __global__ void k_assign_children(const uint32_t* __restrict__ firstq, uint64_t slots, const uint32_t* __restrict__ bitmap,
-                                  const uint32_t* __restrict__ woff, const double* __restrict__ ctr, double k,
-                                  double k_next, uint32_t* __restrict__ ch, double* __restrict__ child_ctr,
+                                  const uint32_t* __restrict__ woff, const double* __restrict__ ctr,
+                                  const float* __restrict__ pnbox, double k, double k_next, bool k_next_f32,
+                                  uint32_t* __restrict__ ch, double* __restrict__ child_ctr,
                                   float* __restrict__ child_nbox) {
   for (uint64_t s = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; s < slots; s += uint64_t(gridDim.x) * blockDim.x) {
     const uint32_t fq = firstq[s];
@@ -239,6 +257,32 @@ __global__ void k_assign_children(const uint32_t* __restrict__ firstq, uint64_t 
     ch[s] = rank;
     const uint64_t p = s >> 3;
     const uint32_t i = uint32_t(s & 7);
+    float4* q = reinterpret_cast<float4*>(child_nbox + 8ull * rank);
+    if (k_next_f32) {
+      const float4* pb = reinterpret_cast<const float4*>(pnbox + 8ull * p);
+      const float4 a = pb[0], b = pb[1];
+      if (b.z == 0.f && b.w != 0.f) {
+        const float c3[3] = {(i & 4) ? a.y : a.x, (i & 2) ? a.w : a.z, (i & 1) ? b.y : b.x};
+        const float kf = float(k_next);
+        float chi[6];
+        bool exact = true;
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+          exact = sat::xsub(c3[ax], kf, chi[2 * ax]) && exact;
+          exact = sat::xsub(c3[ax], -kf, chi[2 * ax + 1]) && exact;
+        }
+#pragma unroll
+        for (int j = 0; j < 6; ++j) exact = exact && (fabsf(chi[j]) < 1.0e18f);
+        if (exact) {
+          child_ctr[3ull * rank + 0] = double(c3[0]);
+          child_ctr[3ull * rank + 1] = double(c3[1]);
+          child_ctr[3ull * rank + 2] = double(c3[2]);
+          q[0] = make_float4(chi[0], chi[1], chi[2], chi[3]);
+          q[1] = make_float4(chi[4], chi[5], 0.f, 1.f);
+          continue;
+        }
+      }
+    }
     const double cc[3] = {__dadd_rn(ctr[3 * p + 0], (i & 4) ? k : -k), __dadd_rn(ctr[3 * p + 1], (i & 2) ? k : -k),
                           __dadd_rn(ctr[3 * p + 2], (i & 1) ? k : -k)};
     child_ctr[3ull * rank + 0] = cc[0];
@@ -246,22 +290,28 @@ __global__ void k_assign_children(const uint32_t* __restrict__ firstq, uint64_t 
     child_ctr[3ull * rank + 2] = cc[2];
     sat::NodeBoxes nb;
     sat::node_boxes(cc, k_next, nb);
-    float4* q = reinterpret_cast<float4*>(child_nbox + 8ull * rank);
     q[0] = make_float4(nb.chi[0], nb.chi[1], nb.chi[2], nb.chi[3]);
     q[1] = make_float4(nb.chi[4], nb.chi[5], nb.clo, nb.ok);
   }
 }
 
-// Next frontier in (pair, child ascending) order.
-__global__ void k_emit_frontier(const uint32_t* __restrict__ f_tri, const uint32_t* __restrict__ f_node, uint64_t F,
-                                const uint8_t* __restrict__ hits, const uint32_t* __restrict__ off,
-                                const uint32_t* __restrict__ ch, uint32_t* __restrict__ nf_tri, uint32_t* __restrict__ nf_node) {
-  for (uint64_t q = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; q < F; q += uint64_t(gridDim.x) * blockDim.x) {
-    uint32_t h = hits[q];
+// Next frontier in (pair, child ascending) order, one 256-pair tile of the
+// expansion per block: a block scan of the hit counts plus the tile's offset.
+__global__ void __launch_bounds__(kExpandThreads) k_emit_frontier(const uint32_t* __restrict__ f_tri,
+                                                                  const uint32_t* __restrict__ f_node, uint64_t F,
+                                                                  const uint8_t* __restrict__ hits,
+                                                                  const uint32_t* __restrict__ tile_off,
+                                                                  const uint32_t* __restrict__ ch,
+                                                                  uint32_t* __restrict__ nf_tri,
+                                                                  uint32_t* __restrict__ nf_node) {
+  for (uint64_t tile = blockIdx.x; tile * kExpandThreads < F; tile += gridDim.x) {
+    const uint64_t q = tile * kExpandThreads + threadIdx.x;
+    uint32_t h = (q < F) ? hits[q] : 0u;
+    uint32_t tot;
+    uint32_t o = tile_off[tile] + block_excl_scan<uint32_t>(uint32_t(__popc(h)), &tot);
     if (!h) continue;
     const uint32_t t = f_tri ? f_tri[q] : uint32_t(q);
     const uint32_t node = f_node ? f_node[q] : 0u;
-    uint32_t o = off[q];
     for (; h; h &= h - 1) {
       const int i = __ffs(h) - 1;
       nf_tri[o] = t;
@@ -358,14 +408,17 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
     const bool leaf = (l == levels - 1);
     DBuf<uint32_t> firstq;
     DBuf<uint8_t> hits;
+    DBuf<uint32_t> tile_hits;
+    const uint64_t tiles = (F + kExpandThreads - 1) / kExpandThreads;
     if (!leaf) {
       firstq.alloc(8 * L.n, st);
       fill<uint32_t>(ex, firstq.get(), 8 * L.n, kNone);
       hits.alloc(F, st);
+      tile_hits.alloc(tiles ? tiles : 1, st);
     }
     if (F)
       SVDAG_LAUNCH(ex, k_expand, grid_for(ex, F, kExpandThreads, 8), kExpandThreads, 0, P, c.tris, f_tri.get(), f_node.get(), F,
-                   L.ctr.get(), L.nbox.get(), L.hdr.get(), firstq.get(), hits.get(), d_fb.get());
+                   L.ctr.get(), L.nbox.get(), L.hdr.get(), firstq.get(), hits.get(), tile_hits.get(), d_fb.get());
     if (leaf) break;
 
     // --- counts of level l+1 and of the next frontier (one host sync)
@@ -376,8 +429,8 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
     SVDAG_LAUNCH(ex, k_mark_keys, grid_for(ex, slots, 256), 256, 0, firstq.get(), slots, bitmap.get());
     DBuf<uint32_t> d_n32(1, st);
     device_exclusive_scan<uint32_t>(ex, PopcIn{bitmap.get()}, words, U32Out{woff.get()}, d_n32.get());
-    DBuf<uint32_t> off(F ? F : 1, st);
-    device_exclusive_scan<uint64_t>(ex, PopcU8In{hits.get()}, F, U64to32Out{off.get()}, d_total.get());
+    DBuf<uint32_t> tile_off(tiles ? tiles : 1, st);
+    device_exclusive_scan<uint64_t>(ex, U32toU64In{tile_hits.get()}, tiles, U64to32Out{tile_off.get()}, d_total.get());
     uint64_t F_next = 0;
     uint32_t n32 = 0;
     SVDAG_CUDA(cudaMemcpyAsync(&n32, d_n32.get(), 4, cudaMemcpyDeviceToHost, st));
@@ -394,8 +447,11 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
     N.ctr.alloc(3 * (n_next ? n_next : 1), st);
     N.nbox.alloc(8 * (n_next ? n_next : 1), st);
     SVDAG_CUDA(cudaMemsetAsync(N.hdr.get(), 0, 4 * (n_next ? n_next : 1), st));
+    // the fp32 path of node_boxes needs an fp32-exact half side in range
+    const double k_next = child_half_side(c.root_side, l + 1);
+    const bool k_next_f32 = k_next > 1.0e-30 && k_next < 1.0e18 && double(float(k_next)) == k_next;
     SVDAG_LAUNCH(ex, k_assign_children, grid_for(ex, slots, 256), 256, 0, firstq.get(), slots, bitmap.get(),
-                 woff.get(), L.ctr.get(), child_half_side(c.root_side, l), child_half_side(c.root_side, l + 1),
+                 woff.get(), L.ctr.get(), L.nbox.get(), child_half_side(c.root_side, l), k_next, k_next_f32,
                  L.ch.get(), N.ctr.get(), N.nbox.get());
     firstq.release();
     bitmap.release();
@@ -404,8 +460,9 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
     // --- next frontier
     DBuf<uint32_t> nf_tri(F_next ? F_next : 1, st), nf_node(F_next ? F_next : 1, st);
     if (F)
-      SVDAG_LAUNCH(ex, k_emit_frontier, grid_for(ex, F, 256), 256, 0, f_tri.get(), f_node.get(), F, hits.get(),
-                   off.get(), L.ch.get(), nf_tri.get(), nf_node.get());
+      SVDAG_LAUNCH(ex, k_emit_frontier, unsigned(tiles < uint64_t(ex.sm_count) * 8 ? tiles : uint64_t(ex.sm_count) * 8),
+                   kExpandThreads, 0, f_tri.get(), f_node.get(), F, hits.get(), tile_off.get(), L.ch.get(),
+                   nf_tri.get(), nf_node.get());
     f_tri = std::move(nf_tri);
     f_node = std::move(nf_node);
     F = F_next;
