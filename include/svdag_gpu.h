@@ -89,6 +89,13 @@ int svdag_set_device_triangles(svdag_ctx* ctx, const float* device_tris, uint64_
 /* GeomOctree::buildSVO(levels, bbox) (src/symvox/geom_octree.cpp:171-280):
  * bbox = {minx, miny, minz, maxx, maxy, maxz} in double, 1 <= levels <= 21. */
 int svdag_voxelize(svdag_ctx* ctx, uint32_t levels, const double bbox[6]);
+/* GeomOctree::buildDAG(levels, stepLevel, bbox) (src/symvox/geom_octree.cpp:289-435):
+ * the chunked build svbuilder runs for numBuildSteps > 0
+ * (src/svbuilder/main.cpp:158-175) -- a top SVO of stepLevel+1 levels, one
+ * sub-octree (buildSVO + toDAG) per top-level voxel, joined in the
+ * reference's order and reduced by one toDAG; leaves the octree in DAG state
+ * with the reference's node order.  1 <= stepLevel < levels - 1. */
+int svdag_build_dag(svdag_ctx* ctx, uint32_t levels, uint32_t step_level, const double bbox[6]);
 /* GeomOctree::toDAG (src/symvox/geom_octree.cpp:462-548) */
 int svdag_reduce_dag(svdag_ctx* ctx);
 /* GeomOctree::initChildLevels (src/symvox/geom_octree_extension.cpp:21-30) */

@@ -182,6 +182,14 @@ int svdag_voxelize(svdag_ctx* h, uint32_t levels, const double bbox[6]) {
   return guarded(h, [&](Ctx& c) { c.st.svo_ms = timed(c, [&] { svdag::phase_voxelize(c, levels, bbox); }); });
 }
 
+int svdag_build_dag(svdag_ctx* h, uint32_t levels, uint32_t step_level, const double bbox[6]) {
+  if (!bbox) return fail(h, SVDAG_ERR_INVALID_ARG, "build_dag: null bbox");
+  return guarded(h, [&](Ctx& c) {
+    c.st.svo_ms = timed(c, [&] { svdag::phase_build_dag(c, levels, step_level, bbox); });
+    c.st.dag_ms = 0.0;
+  });
+}
+
 int svdag_reduce_dag(svdag_ctx* h) {
   return guarded(h, [&](Ctx& c) { c.st.dag_ms = timed(c, [&] { svdag::phase_reduce_dag(c); }); });
 }

@@ -52,7 +52,11 @@ struct Ctx {
 };
 
 // Phases (each throws svdag::Error on failure).
-void phase_voxelize(Ctx& c, uint32_t levels, const double bbox[6]);
+// tri_list (optional, device, ascending ids): voxelize only these triangles
+void phase_voxelize(Ctx& c, uint32_t levels, const double bbox[6], const uint32_t* tri_list = nullptr,
+                    uint64_t n_list = 0);
+// GeomOctree::buildDAG: chunked build joined and reduced to a DAG
+void phase_build_dag(Ctx& c, uint32_t levels, uint32_t step_level, const double bbox[6]);
 void phase_reduce_dag(Ctx& c);
 void phase_reduce_sdag(Ctx& c);
 void phase_cross_level_merge(Ctx& c);

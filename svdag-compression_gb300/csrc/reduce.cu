@@ -103,7 +103,9 @@ __global__ void k_leaf_rank(const uint32_t* __restrict__ first, uint32_t* __rest
     rank[m] = r;
     out_hdr[r] = uint32_t(m);
   } else {
-    rank[m] = kNone;
+    // a pointer to an empty node (only a joined chunk root can be one) maps to
+    // 0, the reference's default correspondence (geom_octree.cpp:493-496)
+    rank[m] = (m == 0) ? 0u : kNone;
   }
   __syncthreads();
   if (m == 0) {

@@ -350,7 +350,7 @@ __global__ void k_count_voxels(const uint32_t* __restrict__ hdr, uint64_t n, uns
 
 }  // namespace
 
-void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
+void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6], const uint32_t* tri_list, uint64_t n_list) {
   const Exec& ex = c.ex;
   const cudaStream_t st = c.stream;
   if (!c.tris && c.n_tris) throw Error(SVDAG_ERR_INVALID_STATE, "voxelize: no triangles set");
@@ -394,8 +394,11 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
     SVDAG_CUDA(cudaStreamSynchronize(st));
   }
 
-  DBuf<uint32_t> f_tri, f_node;  // frontier; empty at level 0 (implicit (t, root))
-  uint64_t F = c.n_tris;
+  // frontier; at level 0 the pairs (t, root) for every triangle, or for the
+  // triangles of tri_list (ascending ids) when one is given
+  DBuf<uint32_t> f_tri, f_node;
+  const uint32_t* ft = tri_list;
+  uint64_t F = tri_list ? n_list : c.n_tris;
   DBuf<uint64_t> d_total(1, st);
   DBuf<unsigned long long> d_vox(1, st), d_fb(1, st);
   SVDAG_CUDA(cudaMemsetAsync(d_fb.get(), 0, 8, st));
@@ -417,7 +420,7 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
       tile_hits.alloc(tiles ? tiles : 1, st);
     }
     if (F)
-      SVDAG_LAUNCH(ex, k_expand, grid_for(ex, F, kExpandThreads, 8), kExpandThreads, 0, P, c.tris, f_tri.get(), f_node.get(), F,
+      SVDAG_LAUNCH(ex, k_expand, grid_for(ex, F, kExpandThreads, 8), kExpandThreads, 0, P, c.tris, ft, f_node.get(), F,
                    L.ctr.get(), L.nbox.get(), L.hdr.get(), firstq.get(), hits.get(), tile_hits.get(), d_fb.get());
     if (leaf) break;
 
@@ -461,10 +464,11 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6]) {
     DBuf<uint32_t> nf_tri(F_next ? F_next : 1, st), nf_node(F_next ? F_next : 1, st);
     if (F)
       SVDAG_LAUNCH(ex, k_emit_frontier, unsigned(tiles < uint64_t(ex.sm_count) * 8 ? tiles : uint64_t(ex.sm_count) * 8),
-                   kExpandThreads, 0, f_tri.get(), f_node.get(), F, hits.get(), tile_off.get(), L.ch.get(),
+                   kExpandThreads, 0, ft, f_node.get(), F, hits.get(), tile_off.get(), L.ch.get(),
                    nf_tri.get(), nf_node.get());
     f_tri = std::move(nf_tri);
     f_node = std::move(nf_node);
+    ft = f_tri.get();
     F = F_next;
   }
   f_tri.release();

@@ -38,9 +38,13 @@ void GeomOctree::buildSVO(unsigned levels, const double bb[6]) {
 }
 
 void GeomOctree::buildDAG(unsigned levels, unsigned stepLevel, const double bb[6]) {
-  (void)stepLevel;
-  buildSVO(levels, bb);
-  toDAG();
+  if (!scene_) throw std::runtime_error("GeomOctree::buildDAG: no scene");
+  check(svdag_upload_triangles(ctx_, scene_->triangles().data(), scene_->nTriangles()));
+  check(svdag_build_dag(ctx_, levels, stepLevel, bb));
+  float b[6];
+  for (int k = 0; k < 6; ++k) b[k] = float(bb[k]);
+  resizeSceneBbox(b);
+  invalidate();
 }
 
 void GeomOctree::toDAG() {

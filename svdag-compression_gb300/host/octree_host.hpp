@@ -61,9 +61,8 @@ class GeomOctree {
   void setScene(Scene* s) { scene_ = s; }
   // buildSVO(levels, bbox) (geom_octree.cpp:171-280); bbox = {min xyz, max xyz}
   void buildSVO(unsigned levels, const double bbox[6]);
-  // buildDAG(levels, stepLevel, bbox): the reference chunks the SVO build for
-  // memory; the GPU builds the whole SVO in HBM, whose reduction gives the same
-  // DAG node counts (geom_octree.cpp:289-435).
+  // buildDAG(levels, stepLevel, bbox) (geom_octree.cpp:289-435): chunked
+  // build, same node order as the reference.
   void buildDAG(unsigned levels, unsigned stepLevel, const double bbox[6]);
   void toDAG();
   void toSDAG();

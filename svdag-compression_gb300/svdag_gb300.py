@@ -63,6 +63,7 @@ GPU_SYMBOLS = {
     "svdag_upload_triangles": (_I, [_VP, _VP, _U64]),
     "svdag_set_device_triangles": (_I, [_VP, _VP, _U64]),
     "svdag_voxelize": (_I, [_VP, _U32, _VP]),
+    "svdag_build_dag": (_I, [_VP, _U32, _U32, _VP]),
     "svdag_reduce_dag": (_I, [_VP]),
     "svdag_init_child_levels": (_I, [_VP]),
     "svdag_reduce_sdag": (_I, [_VP]),
@@ -232,6 +233,11 @@ class Octree:
     def buildSVO(self, levels, bbox=UNIT_BOX):
         bb = (ctypes.c_double * 6)(*bbox)
         self._check(self._lib.svdag_voxelize(self._h, levels, bb))
+
+    def buildDAG(self, levels, step_level, bbox=UNIT_BOX):
+        """GeomOctree::buildDAG: chunked build, DAG state, reference node order."""
+        bb = (ctypes.c_double * 6)(*bbox)
+        self._check(self._lib.svdag_build_dag(self._h, levels, step_level, bb))
 
     def toDAG(self):
         self._check(self._lib.svdag_reduce_dag(self._h))

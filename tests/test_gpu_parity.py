@@ -153,3 +153,57 @@ def test_single_and_degenerate_triangles():
 def test_duplicate_triangles():
     t = sv.icosphere(2, 0.4, 0.08, 8)
     _edge(np.concatenate([t, t[::-1]]), 6)
+
+
+def test_build_dag_matches_reference_digests():
+    """GeomOctree::buildDAG (chunked, step level 1) through the C ABI: the
+    reference's node order, counts and pools."""
+    name = "terrain129_L9_step1"
+    g = G[name]
+    o = sv.Octree()
+    o.upload_triangles(SCENES[name]())
+    o.buildDAG(g["levels"], g["step_levels"])
+    st = o.stats()
+    assert st["state_name"] == "S_DAG"
+    assert st["n_total_voxels"] == g["nTotalVoxels"]
+    assert st["n_nodes_svo"] == g["nNodesSVO"]
+    assert st["n_nodes_dag"] == g["nNodesDAG"]
+    o.initChildLevels()
+    assert oracle_py.pool_digest(o.pool()) == g["dag"]["digest"]
+    s = o.clone()
+    s.toSDAG()
+    assert oracle_py.pool_digest(s.pool()) == g["sdag"]["digest"]
+    c = o.clone()
+    c.mergeAcrossAllLevels()
+    assert oracle_py.pool_digest(c.pool()) == g["csv"]["digest"]
+
+
+@pytest.mark.parametrize("step", [1, 2])
+@pytest.mark.parametrize("kind", ["ico", "terrain", "boxes"])
+def test_build_dag_random_scenes_match_oracle(kind, step):
+    if kind == "ico":
+        tris, levels = sv.icosphere(4, 0.33, 0.08, 70 + step), 8
+    elif kind == "terrain":
+        tris, levels = sv.terrain(65, 8, 0.3, 90 + step), 8
+    else:
+        from _scenes import box_scene
+
+        tris, levels = box_scene(120, 7, 30 + step), 7
+    ref = oracle_py.OracleOctree()
+    ref.buildDAG(tris, levels, step)
+    o = sv.Octree()
+    o.upload_triangles(tris)
+    o.buildDAG(levels, step)
+    assert first_mismatch(o.pool(), ref.pool()) is None
+    rs, st = ref.stats(), o.stats()
+    for k in ("n_total_voxels", "n_nodes_svo", "n_nodes_last_lev_svo", "n_nodes_dag"):
+        assert st[k] == rs[k], k
+
+
+def test_build_dag_rejects_bad_step_levels():
+    o = sv.Octree()
+    o.upload_triangles(sv.icosphere(2, 0.4, 0.08, 3))
+    for step in (0, 5, 6):
+        with pytest.raises(sv.SvdagError) as e:
+            o.buildDAG(6, step)
+        assert e.value.status == 1
