@@ -4,9 +4,10 @@
 //             [output.{svdag,ussvdag,ssvdag,esvdag}]
 //
 // Same argument contract, output names (<dir>/<base>_<levels>[infix].ext),
-// result printout and stats.txt append as the reference.  numBuildSteps is
-// accepted for compatibility: the GPU builds the whole SVO in HBM, which gives
-// the same DAG as the reference's chunked build.  -l (lossy LSVDAG) and -h
+// result printout and stats.txt append as the reference.  numBuildSteps = 0
+// builds the SVO and reduces it (buildSVO + toDAG); numBuildSteps > 0 runs the
+// chunked buildDAG with that step level (src/svbuilder/main.cpp:158-175), so
+// the node order is the reference's in both cases.  -l (lossy LSVDAG) and -h
 // (hidden-geometry DAG, work in progress in the reference) are reported as
 // unavailable in this build.
 #include <cmath>
@@ -30,7 +31,7 @@ void usage() {
       "Where:\n"
       "      input_model.obj: a 3D model in ASCII OBJ format OR a pre-built SVDAG file\n"
       "      numLevels: levels of the octree to build (i.e. 10->1K^3, 13->8K^3...)\n"
-      "      numBuildSteps: accepted for compatibility (the GPU builds the full octree at once)\n\n");
+      "      numBuildSteps: 0 = build the whole SVO, then reduce it; n > 0 = chunked build with step level n\n\n");
 }
 
 std::string dir_of(const std::string& p) {
@@ -102,8 +103,12 @@ int main(int argc, char** argv) {
     }
     const float* b = scene.bbox();
     const double bb[6] = {b[0], b[1], b[2], b[3], b[4], b[5]};
-    octree.buildSVO(unsigned(nLevels), bb);
-    octree.toDAG();
+    if (levelStep == 0) {
+      octree.buildSVO(unsigned(nLevels), bb);
+      octree.toDAG();
+    } else {
+      octree.buildDAG(unsigned(nLevels), unsigned(levelStep), bb);
+    }
     // bounding boxes outside [0.1, 1e5] are rescaled for rendering (main.cpp:178-193)
     const double dx = double(b[3]) - b[0], dy = double(b[4]) - b[1], dz = double(b[5]) - b[2];
     const float size = float(std::sqrt(dx * dx + dy * dy + dz * dz));
