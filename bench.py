@@ -40,13 +40,44 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--grid", type=int, default=2048)
-    ap.add_argument("--levels", type=int, default=12)
-    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--workload", choices=["terrain", "city"], default="terrain",
+                    help="terrain: 2048^2 fBm terrain at depth 12 (the headline); city: 4096^2 terrain + 200,000 "
+                         "boxes at depth 15, chunked build with step level 1")
+    ap.add_argument("--grid", type=int, default=None)
+    ap.add_argument("--levels", type=int, default=None)
+    ap.add_argument("--step-level", type=int, default=None, help="buildDAG step level (0 = buildSVO + toDAG)")
+    ap.add_argument("--boxes", type=int, default=200000)
+    ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-json", default="")
-    return ap.parse_args()
+    a = ap.parse_args()
+    city = a.workload == "city"
+    if a.grid is None:
+        a.grid = 4096 if city else 2048
+    if a.levels is None:
+        a.levels = 15 if city else 12
+    if a.step_level is None:
+        a.step_level = 1 if city else 0
+    if a.seed is None:
+        a.seed = 15 if city else 7
+    return a
+
+
+def scene(args, sv):
+    if args.workload == "city":
+        return sv.city(args.grid, args.boxes, args.levels, args.seed)
+    return sv.terrain(args.grid, 8, 0.3, args.seed)
+
+
+def workload_name(args):
+    if args.workload == "city":
+        return ("city: %dx%d fBm terrain + %d boxes (footprints 8-256 voxels, log-normal heights, median 64), "
+                "depth %d (%d^3), chunked buildDAG step level %d -> SVDAG -> SSVDAG + CSVDAG"
+                % (args.grid, args.grid, args.boxes, args.levels, 2 ** args.levels, args.step_level))
+    return ("terrain %dx%d fBm (8 octaves) + skirts, depth %d (%d^3): voxelize -> SVDAG -> SSVDAG + CSVDAG"
+            % (args.grid, args.grid, args.levels, 2 ** args.levels)
+            + (", chunked buildDAG step level %d" % args.step_level if args.step_level else ""))
 
 
 def rank_info():
@@ -137,9 +168,9 @@ KERNEL_DRAM_BYTES_PER_LAUNCH = {}
 
 def model_bytes(info, T):
     N, D, S, C = info["svo"], info["dag"], info["sdag"], info["csv"]
-    L = len(N)
-    b_vox = 36 * T + 36 * sum(N)
-    b_dag = sum((R + 4) * N[l] + R * D[l] + 64 * N[l - 1] for l in range(1, L))
+    L = len(D)
+    b_vox = 36 * T + 36 * info["svo_total"]
+    b_dag = sum((R + 4) * N[l] + R * D[l] + 64 * N[l - 1] for l in range(1, L)) if N else None
     b_sdag = sum((R + 13) * D[l] + R * S[l] + (64 * D[l - 1] if l else 0) for l in range(L))
     b_csv = sum((R + 16) * D[l] + R * C[l] for l in range(L)) if C else None
     return {"k_expand": b_vox, "vox": b_vox, "dag": b_dag, "sdag": b_sdag, "csv": b_csv}
@@ -153,7 +184,7 @@ def run_ours(args, rank, local, world):
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    tris = sv.terrain(args.grid, 8, 0.3, args.seed)
+    tris = scene(args, sv)
     T = tris.shape[0]
     d_tris = torch.from_numpy(tris).to(dev)
     stream = torch.cuda.Stream(device=dev)
@@ -171,10 +202,15 @@ def run_ours(args, rank, local, world):
 
     def step(octree, profile=False):
         nonlocal have_csv
-        octree.buildSVO(args.levels)
-        if profile:
-            collect("voxelize", octree)
-        octree.toDAG()
+        if args.step_level:
+            octree.buildDAG(args.levels, args.step_level)
+            if profile:
+                collect("voxelize", octree)
+        else:
+            octree.buildSVO(args.levels)
+            if profile:
+                collect("voxelize", octree)
+            octree.toDAG()
         octree.initChildLevels()
         if profile:
             collect("dag", octree)
@@ -262,7 +298,7 @@ def run_ours(args, rank, local, world):
     sst = s_last.stats()
     cst = c_last.stats() if c_last is not None else None
     # level sizes for the algorithmic-byte model (one extra instrumented build)
-    info = level_info(sv, base, s_last, args.levels)
+    info = level_info(sv, base, s_last, args)
 
     # --- roofline of the dominant kernel (live CUDA-event durations)
     hbm_peak, peak_src = peaks()
@@ -292,7 +328,7 @@ def run_ours(args, rank, local, world):
     # over the kernel time of those phases
     red = None
     red_ms = sum(ms for ph in ("dag", "sdag", "csv") for _, ms in phase_prof.get(ph, {}).values()) / args.steps
-    if red_ms > 0:
+    if red_ms > 0 and B["dag"] is not None:
         rb = B["dag"] + B["sdag"] + (B["csv"] or 0)
         red = {"bound": "hbm", "achieved": rb / (red_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                "frac": rb / (red_ms / 1e3) / 1e9 / hbm_peak, "bytes_per_step": rb, "kernel_ms_per_step": red_ms,
@@ -308,15 +344,14 @@ def run_ours(args, rank, local, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64-exact SAT (certified fp32 filter) + u32 keys", "data": "synthetic",
-        "config": {"workload": "terrain %dx%d fBm (8 octaves) + skirts, depth %d (%d^3): voxelize -> SVDAG -> "
-                               "SSVDAG + CSVDAG" % (args.grid, args.grid, args.levels, 2 ** args.levels),
+        "config": {"workload": workload_name(args),
                    "triangles": int(T), "levels": args.levels, "voxels": int(voxels),
                    "nodes_svo": int(st["n_nodes_svo"]), "nodes_dag": int(st["n_nodes_dag"]),
                    "nodes_sdag": int(sst["n_nodes_sdag"]),
                    "nodes_csvdag": int(cst["n_nodes"]) if cst else None,
                    "csvdag_in_step": bool(have_csv),
                    "frontier_pairs": int(info["frontier"][0]), "sat_fp64_fallbacks": int(info["sat_fallbacks"]),
-                   "l2": "inputs larger than L2 (triangles 302 MB, node pools > 129 MB)",
+                   "l2": "inputs larger than L2 (triangles %d MB, node pools > 129 MB)" % (36 * T // 10**6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clk, "gpu_launches": int(launches), "roofline": roof, "reduction_roofline": red, "e2e": e2e,
         "kernel_events_region_ms_per_step": ms_events / args.steps,
@@ -330,18 +365,24 @@ def run_ours(args, rank, local, world):
     return res
 
 
-def level_info(sv, base, s_last, levels):
-    """Frontier and level sizes of one build (for the byte model)."""
+def level_info(sv, base, s_last, args):
+    """Frontier and level sizes of one build (for the byte model).  The
+    chunked build exposes only its totals (its SVO never exists whole)."""
+    levels = args.levels
     o = base.clone()
-    o.buildSVO(levels)
-    svo = [o.level_count(l) for l in range(levels)]
-    pairs = o.stats()["frontier_pairs"]
-    fallbacks = o.stats()["sat_fallbacks"]
-    o.toDAG()
+    if args.step_level:
+        o.buildDAG(levels, args.step_level)
+        svo = None
+    else:
+        o.buildSVO(levels)
+        svo = [o.level_count(l) for l in range(levels)]
+    st = o.stats()
+    if not args.step_level:
+        o.toDAG()
     dag = [o.level_count(l) for l in range(levels)]
     o.close()
-    return {"svo": svo, "dag": dag, "svo_inner": svo[1:-1], "dag_inner": dag[1:-1], "frontier": [pairs],
-            "sdag": [s_last.level_count(l) for l in range(levels)], "sat_fallbacks": fallbacks}
+    return {"svo": svo, "svo_total": st["n_nodes_svo"], "dag": dag, "frontier": [st["frontier_pairs"]],
+            "sdag": [s_last.level_count(l) for l in range(levels)], "sat_fallbacks": st["sat_fallbacks"]}
 
 
 def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
@@ -425,17 +466,17 @@ def cpu_sample(args, frac_rows):
 
     import svdag_gb300 as sv
 
-    tris = sv.terrain(args.grid, 8, 0.3, args.seed)
+    tris = scene(args, sv)  # the terrain rows come first (the city's boxes follow them)
     g = args.grid - 1
     rows = max(1, int(g * frac_rows))
     return np.ascontiguousarray(tris[: 2 * g * rows]), rows
 
 
-def cpu_build(oracle_py, tris, levels, chunked, threads):
+def cpu_build(oracle_py, tris, levels, chunked, threads, step_level=2):
     o = oracle_py.OracleOctree()
     t0 = time.perf_counter()
     if chunked:
-        o.buildDAG(tris, levels, 2, threads=threads)
+        o.buildDAG(tris, levels, step_level, threads=threads)
     else:
         o.buildSVO(tris, levels)
         o.toDAG()
@@ -452,7 +493,7 @@ def run_cpu_baseline(args):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
 
-    frac = 1.0 / 8
+    frac = 1.0 / 256 if args.workload == "city" else 1.0 / 8
     tris, rows = cpu_sample(args, frac)
     vox, dt = cpu_build(oracle_py, tris, args.levels, chunked=False, threads=1)
     return {"value": vox / dt / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
@@ -468,26 +509,25 @@ def run_reference(args, rank, world):
     if rank != 0:
         return None
     cores = os.cpu_count() or 1
-    frac = 1.0 / 16
+    frac = 1.0 / 256 if args.workload == "city" else 1.0 / 16
+    step = args.step_level or 2
     tris, rows = cpu_sample(args, frac)
     for _ in range(max(args.warmup, 0)):
-        cpu_build(oracle_py, tris, args.levels, chunked=True, threads=cores)
+        cpu_build(oracle_py, tris, args.levels, chunked=True, threads=cores, step_level=step)
     times = []
     vox = 0
     for _ in range(args.steps):
-        vox, dt = cpu_build(oracle_py, tris, args.levels, chunked=True, threads=cores)
+        vox, dt = cpu_build(oracle_py, tris, args.levels, chunked=True, threads=cores, step_level=step)
         times.append(dt)
     dt = sum(times) / len(times)
     v = vox / dt / 1e6
     sample = ("first %d of %d terrain rows (%d triangles, %d voxels) at depth %d: chunked OpenMP buildDAG "
-              "(step level 2) + toSDAG + mergeAcrossAllLevels, restated CPU port" %
-              (rows, args.grid - 1, tris.shape[0], vox, args.levels))
+              "(step level %d) + toSDAG + mergeAcrossAllLevels, restated CPU port" %
+              (rows, args.grid - 1, tris.shape[0], vox, args.levels, step))
     return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64-exact SAT (certified fp32 filter) + u32 keys", "data": "synthetic", "impl": "reference",
-            "config": {"workload": "terrain %dx%d fBm (8 octaves) + skirts, depth %d (%d^3): voxelize -> SVDAG -> "
-                                   "SSVDAG + CSVDAG" % (args.grid, args.grid, args.levels, 2 ** args.levels),
-                       "sample": sample},
+            "config": {"workload": workload_name(args), "sample": sample},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

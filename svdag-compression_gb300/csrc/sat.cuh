@@ -408,6 +408,7 @@ struct Pair32 {
   bool fast;         // fp32 path usable (finite, moderate magnitudes)
   uint32_t slab;     // 2 bits per (axis q, side s) at bit 2*(2q+s)
   uint32_t tang;     // bit 2q+s: grid-plane tangency on axis q, side s (see pair_slabs)
+  uint32_t flat;     // bit q: the three vertices share coordinate q exactly (see pair_slabs)
   float vmax[6];     // max_i |fl32(t_iq - chi)| per (axis, side)
   float n[3], sn[3]; // plane normal e0 x e1 in fp32 and |m1| + |m2| per component
   float nh;          // fl32(|n|_1 h)
@@ -475,6 +476,7 @@ SAT_HD void pair_basic(const float t[9], const float* tp, const double* c, const
   P.k = k;
   P.slab = 0;
   P.tang = 0;
+  P.flat = 0;
 }
 
 // Slab classification of the pair (see Slab).
@@ -534,6 +536,18 @@ SAT_HD void pair_slabs(Pair32& P) {
   // component non-zero with box corner offsets {0, +-2h} on q, giving
   // dmin <= 0 <= dmax.
   uint32_t tang = 0;
+  // Axis-aligned triangle.  When the three vertices share coordinate q, the
+  // reference's fp64 offsets v_iq are one value v_q, so both edges have
+  // e_q = 0 exactly and the normal's other two components are exact zeros;
+  // its dot products reduce to dmin = fl(n_q * vmin_q), dmax = fl(n_q * vmax_q)
+  // with vmin_q, vmax_q = fl(-+h - v_q) picked by sign(n_q).  Rounding keeps
+  // signs, so the plane test rejects exactly when |v_q| > h (any sign of n_q;
+  // n_q = 0 never rejects) -- which the bounding-box test on q rejects too.
+  // The plane test therefore never decides the box and is skipped.
+  uint32_t flat = 0;
+  for (int q = 0; q < 3; ++q)
+    if (t[q] == t[3 + q] && t[q] == t[6 + q]) flat |= 1u << q;
+  P.flat = flat;
   if (clo == 0.f) {
     for (int q = 0; q < 3; ++q) {
       if (!(t[q] == t[3 + q] && t[q] == t[6 + q])) continue;
@@ -699,6 +713,7 @@ SAT_HD bool child_full(const Pair32& P, int ci, unsigned* fallbacks) {
     if (need64(3 + (__builtin_ctz_(m)))) return false;
 
   if (tx || ty || tz) return true;  // the plane test passes on a tangent grid plane
+  if (P.flat) return true;          // axis-aligned triangle: implied by the bounding-box test (pair_slabs)
 
   // plane test with the pair's normal n = e0 x e1 (pair constants n, sn, nh):
   //   dmin* = -(|n|_1 h + n.v0),  dmax* = |n|_1 h - n.v0

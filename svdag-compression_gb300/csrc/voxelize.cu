@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
       s_pl[6][tid] = PP.nh;
       s_tri[tid] = t;
       s_node[tid] = node;
-      s_slab[tid] = PP.slab | (PP.tang << 16) | (PP.fast ? 0x80000000u : 0u);  // classes, tangency, fp32 path
+      // slab classes, tangency, axis-aligned triangle, fp32 path
+      s_slab[tid] = PP.slab | (PP.tang << 16) | (PP.flat << 24) | (PP.fast ? 0x80000000u : 0u);
     }
     s_hits[tid] = hits;
     __syncthreads();
@@ -152,6 +153,7 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
       PP.fast = (word >> 31) != 0u;
       PP.slab = word & 0xFFFFu;
       PP.tang = (word >> 16) & 0x3Fu;
+      PP.flat = (word >> 24) & 0x7u;
       PP.tp = tris + 9ull * s_tri[slot];
       PP.c = ctr + 3ull * node;
       PP.k = k;

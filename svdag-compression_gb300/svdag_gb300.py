@@ -159,6 +159,36 @@ def boxes(lo, hi):
     return out
 
 
+def city(grid=4096, n_boxes=200000, levels=15, seed=15, octaves=8, height=0.3):
+    """A procedural city on an fBm terrain: the terrain (grid x grid, skirts)
+    followed by `n_boxes` seeded boxes with footprints of 8-256 voxels and
+    log-normal heights (median 64 voxels) at a resolution of 2^levels,
+    standing on the terrain (base 2 voxels below the lowest of the four
+    terrain vertices around the box centre)."""
+    t = terrain(grid, octaves, height, seed)
+    n = grid
+    cells = t[: 2 * (n - 1) ** 2].reshape(n - 1, n - 1, 2, 9)
+    hgt = np.empty((n, n), np.float32)  # [j, i] -> y at grid vertex (i, j)
+    hgt[:-1, :-1] = cells[:, :, 0, 1]   # a = (i, j)
+    hgt[:-1, -1] = cells[:, -1, 0, 4]   # b = (i+1, j)
+    hgt[-1, :-1] = cells[-1, :, 1, 7]   # d = (i, j+1)
+    hgt[-1, -1] = cells[-1, -1, 0, 7]   # c = (i+1, j+1)
+    rng = np.random.default_rng(seed)
+    vox = 1.0 / (1 << levels)
+    fx = rng.uniform(8, 256, n_boxes) * vox
+    fz = rng.uniform(8, 256, n_boxes) * vox
+    hy = rng.lognormal(np.log(64.0), 0.5, n_boxes) * vox
+    cx = rng.uniform(fx / 2, 1 - fx / 2)
+    cz = rng.uniform(fz / 2, 1 - fz / 2)
+    gi = np.minimum((cx * (n - 1)).astype(np.int64), n - 2)
+    gj = np.minimum((cz * (n - 1)).astype(np.int64), n - 2)
+    base = np.minimum(np.minimum(hgt[gj, gi], hgt[gj, gi + 1]), np.minimum(hgt[gj + 1, gi], hgt[gj + 1, gi + 1]))
+    base = np.maximum(base - 2 * vox, 0.0)
+    lo = np.stack([cx - fx / 2, base, cz - fz / 2], axis=1)
+    hi = np.stack([cx + fx / 2, np.minimum(base + hy, 1.0), cz + fz / 2], axis=1)
+    return np.concatenate([t, boxes(lo, hi)])
+
+
 def write_obj(path, tris, pin_unit_cube=True):
     h = load_host()
     tris = np.ascontiguousarray(tris, np.float32)

@@ -91,6 +91,13 @@ int main(int argc, char** argv) {
         for (int q = 0; q < 3; ++q) t[6 + q] = float(0.5 * (double(t[q]) + double(t[3 + q])));  // collinear
       }
     }
+    if (mode == 7 && it % 4 == 3) {
+      // axis-aligned triangle at an arbitrary (off-grid) coordinate, or on a
+      // child face, as box faces are
+      const int q = int(U(rng) * 3);
+      const float c = (it % 16 == 3) ? float(pc[q] + (U(rng) < 0.5 ? -k : k)) : t[q];
+      for (int v = 0; v < 3; ++v) t[3 * v + q] = c;
+    }
     if (mode == 4 && it % 32 == 4) {
       // triangle in an axis-aligned plane through the child grid
       const int q = int(U(rng) * 3);
