@@ -136,6 +136,66 @@ int svdag_level_device_ptrs(const svdag_ctx* ctx, uint32_t level, const uint32_t
 int svdag_profile_enable(svdag_ctx* ctx, int enable);
 int svdag_profile_report(svdag_ctx* ctx, char* buf, uint64_t capacity);
 
+/* ---- Voxel-brick chunks (no counterpart in the reference, which voxelizes
+ * triangles only; a voxel grid enters it as node pools through
+ * GeomOctree(const NodeData&, ...), src/symvox/geom_octree.cpp:49-60).
+ *
+ * A chunk of depth d (2..11) is a dense grid of 2^d voxels per side, given
+ * as 8^(d-1) bricks (one byte = 2^3 voxels, bit 4x+2y+z) in Morton order
+ * (x the most significant bit of each coordinate triple), in device memory
+ * aligned to 8 bytes.  Its node pools: the non-empty bricks in Morton order
+ * on level d-1, on each level above the non-empty cells of 8 consecutive
+ * entries of the level below (child k = entry 8j+k), the root always present.
+ *
+ * Seeded synthetic chunk: 3D value noise (lattice period 16 voxels) below a
+ * threshold chosen so that about `fill` of the voxels are set; writes the
+ * threshold used when `threshold` is not NULL. */
+int svdag_synth_noise_bricks(void* stream, uint32_t depth, uint64_t seed, double fill, uint8_t* device_bricks,
+                             float* threshold);
+/* The plain per-chunk form: the chunk's node pools into `ctx` (DAG state, as
+ * the NodeData constructor leaves them); svdag_reduce_dag / reduce_sdag /
+ * cross_level_merge then run on them. */
+int svdag_import_bricks(svdag_ctx* ctx, uint32_t depth, const uint8_t* device_bricks);
+
+/* The batched form: many chunks (of any depths) reduced together, height by
+ * height (every chunk's leaves first), one launch per step for all chunks;
+ * then toSDAG and the cross-level merge of each chunk on several streams.
+ * Each chunk's results equal the plain form's (toDAG / toSDAG /
+ * mergeAcrossAllLevels of its node pools).  Chunks are borrowed: their bricks
+ * must stay valid until the build returns.  Result views are owned by the
+ * batch and valid until the next build, clear or destroy: read them with
+ * svdag_level_count / svdag_download_level / svdag_get_stats, or
+ * svdag_clone them to work on; do not destroy them or run phases on them. */
+typedef struct svdag_batch svdag_batch;
+enum { SVDAG_BATCH_SDAG = 1, SVDAG_BATCH_CSVDAG = 2 };
+enum { SVDAG_BATCH_RESULT_DAG = 0, SVDAG_BATCH_RESULT_SDAG = 1, SVDAG_BATCH_RESULT_CSVDAG = 2 };
+typedef struct svdag_batch_tuning {
+  double table_factor; /* hash slots per cell of a height (rounded up to a power of two), 1.25..16 */
+  uint32_t threads;    /* block size of the per-height kernels, 64..1024, multiple of 32 */
+  uint32_t streams;    /* chunks reduced concurrently in the SSVDAG / CSVDAG stage, 1..64 */
+} svdag_batch_tuning;
+typedef struct svdag_batch_stats {
+  double dag_ms;       /* wall time of the batched toDAG stage of the last build */
+  double reduce_ms;    /* wall time of the SSVDAG / CSVDAG stage */
+  uint64_t gpu_launches;
+} svdag_batch_stats;
+int svdag_batch_create(svdag_batch** out, int device, void* stream);
+int svdag_batch_destroy(svdag_batch* batch);
+const char* svdag_batch_last_error(const svdag_batch* batch);
+int svdag_batch_clear(svdag_batch* batch);
+int svdag_batch_add_chunk(svdag_batch* batch, uint32_t depth, const uint8_t* device_bricks);
+int svdag_batch_chunk_count(const svdag_batch* batch, uint32_t* n);
+/* flags: SVDAG_BATCH_SDAG and / or SVDAG_BATCH_CSVDAG (the DAG is always built) */
+int svdag_batch_build(svdag_batch* batch, uint32_t flags);
+int svdag_batch_result(svdag_batch* batch, uint32_t chunk, uint32_t kind, svdag_ctx** view);
+int svdag_batch_set_tuning(svdag_batch* batch, const svdag_batch_tuning* tuning);
+int svdag_batch_get_tuning(const svdag_batch* batch, svdag_batch_tuning* tuning);
+/* Times full builds of the current chunks under candidate settings
+ * (coordinate search, at most max_trials builds), keeps the fastest setting
+ * and leaves its results in place. */
+int svdag_batch_autotune(svdag_batch* batch, uint32_t flags, uint32_t max_trials);
+int svdag_batch_get_stats(const svdag_batch* batch, svdag_batch_stats* out);
+
 /* toDAG without allocating (no counterpart in the reference, whose toDAG,
  * src/symvox/geom_octree.cpp:462-548, works in host containers).
  *

@@ -35,6 +35,7 @@ _SIGS = {
     "ora_clone": (_VP, [_VP]),
     "ora_build_svo": (_I, [_VP, _VP, _U64, _VP, _U32]),
     "ora_build_dag_chunked": (_I, [_VP, _VP, _U64, _VP, _U32, _U32, _I]),
+    "ora_build_from_bricks": (_I, [_VP, _U32, _VP]),
     "ora_to_dag": (_I, [_VP]),
     "ora_to_sdag": (_I, [_VP]),
     "ora_init_child_levels": (_I, [_VP]),
@@ -88,6 +89,12 @@ class OracleOctree:
         bb = np.array(bbox, np.float64)
         assert self.L.ora_build_dag_chunked(self.h, tris.ctypes.data, tris.shape[0], bb.ctypes.data, levels,
                                             step_level, threads) == 0
+
+    def buildFromBricks(self, depth, bricks):
+        """Node pools of a voxel-brick grid (Morton order), DAG state."""
+        bricks = np.ascontiguousarray(bricks, np.uint8)
+        assert bricks.size == 8 ** (depth - 1)
+        assert self.L.ora_build_from_bricks(self.h, depth, bricks.ctypes.data) == 0
 
     def toDAG(self):
         assert self.L.ora_to_dag(self.h) == 0

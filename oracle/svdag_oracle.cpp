@@ -611,6 +611,57 @@ int ora_build_dag_chunked(ora_octree* o, const float* tris, uint64_t n_tris, con
   return 0;
 }
 
+// Voxel-brick ingest.  The reference has no voxel-grid input; a grid enters
+// it as node data through GeomOctree(const NodeData&, bbox, rootSide, levels,
+// stats) (src/symvox/geom_octree.cpp:49-60), which stores the pools and sets
+// the DAG state.  The pools restated here: bricks[8^(depth-1)] are 2^3 voxel
+// masks (bit 4x+2y+z) in Morton order (x the most significant bit of each
+// coordinate triple); level depth-1 holds the non-empty bricks in that order,
+// and each level above the non-empty cells of 8 consecutive entries of the
+// level below (child k = entry 8j+k), in Morton order; the root always exists.
+int ora_build_from_bricks(ora_octree* o, uint32_t depth, const uint8_t* bricks) {
+  if (!o || depth < 1 || depth > 11 || !bricks) return -1;
+  o->levels = depth;
+  o->d.assign(depth, std::vector<Node>());
+  uint64_t cells = 1ull << (3 * (depth - 1));
+  std::vector<uint32_t> idx(cells, kNull), up;
+  o->n_voxels = 0;
+  for (uint64_t i = 0; i < cells; ++i) {
+    if (!bricks[i]) continue;
+    Node n;
+    n.mask = bricks[i];
+    idx[i] = uint32_t(o->d[depth - 1].size());
+    o->d[depth - 1].push_back(n);
+    o->n_voxels += popc8(n.mask);
+  }
+  for (int l = int(depth) - 2; l >= 0; --l) {
+    cells >>= 3;
+    up.assign(cells, kNull);
+    for (uint64_t j = 0; j < cells; ++j) {
+      Node n;
+      for (int k = 0; k < 8; ++k) {
+        const uint32_t c = idx[8 * j + k];
+        if (c == kNull) continue;
+        n.mask |= uint8_t(1u << k);
+        n.ch[k] = c;
+      }
+      if (!n.mask && l > 0) continue;
+      up[j] = uint32_t(o->d[l].size());
+      o->d[l].push_back(n);
+    }
+    idx.swap(up);
+  }
+  if (depth == 1 && o->d[0].empty()) o->d[0].push_back(Node());
+  o->n_nodes = 0;
+  for (const auto& L : o->d) o->n_nodes += L.size();
+  o->state = 2;
+  o->st = ora_stats{};
+  o->st.levels = depth;
+  o->st.n_total_voxels = o->n_voxels;
+  o->st.n_nodes_dag = o->n_nodes;
+  return 0;
+}
+
 int ora_to_dag(ora_octree* o) { return o ? to_dag(o) : -1; }
 int ora_to_sdag(ora_octree* o) { return o ? to_sdag(o) : -1; }
 int ora_init_child_levels(ora_octree* o) {

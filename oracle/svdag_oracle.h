@@ -37,6 +37,9 @@ int ora_build_svo(ora_octree* o, const float* tris, uint64_t n_tris, const doubl
 /* GeomOctree::buildDAG (geom_octree.cpp:289-435), OpenMP over chunks; n_threads<=0 = all. */
 int ora_build_dag_chunked(ora_octree* o, const float* tris, uint64_t n_tris, const double bbox[6],
                           uint32_t levels, uint32_t step_level, int n_threads);
+/* voxel bricks (8^(depth-1) masks, Morton order) -> node pools in the DAG
+ * state, the GeomOctree(NodeData, ...) route (geom_octree.cpp:49-60) */
+int ora_build_from_bricks(ora_octree* o, uint32_t depth, const uint8_t* bricks);
 int ora_to_dag(ora_octree* o);                 /* geom_octree.cpp:462-548 */
 int ora_to_sdag(ora_octree* o);                /* geom_octree.cpp:551-697 (greedy, symmetry on) */
 int ora_init_child_levels(ora_octree* o);      /* geom_octree_extension.cpp:21-30 */

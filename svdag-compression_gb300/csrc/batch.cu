@@ -1,0 +1,929 @@
+// Voxel-brick chunks: the plain per-chunk ingest and the batched build.
+//
+// A chunk of depth d is a dense grid of 2^d voxels per side given as
+// 8^(d-1) leaf bricks (2^3 voxels, bit 4x+2y+z) in Morton order (x the most
+// significant bit of each coordinate triple).  The reference has no voxel
+// input; a grid enters it as node pools through the NodeData constructor
+// (src/symvox/geom_octree.cpp:49-60): level d-1 = the non-empty bricks in
+// Morton order, each level above = the non-empty cells of 8 consecutive
+// entries of the level below, the root always present.  toDAG, toSDAG and the
+// cross-level merge then run on those pools as on any other.
+//
+// Plain form (svdag_import_bricks): those SVO pools are materialised in a
+// context, which the ordinary per-chunk pipeline reduces.
+//
+// Batched form (svdag_batch_*): many chunks at once, height by height (height
+// h = level d-1-h, so every chunk's leaves are height 0).  The SVO is never
+// materialised: toDAG's first-occurrence order over a level is the Morton
+// order of its non-empty cells, so each cell's DAG id is found directly from
+// its key (mask, DAG ids of its 8 children) in one hash table shared by all
+// chunks, with the chunk id in the key; equal keys converge on the smallest
+// global cell index, i.e. the first occurrence within their chunk.  One
+// launch per step covers every chunk of a height.  The DAGs then go through
+// toSDAG and the cross-level merge per chunk, on several streams at once.
+#include <algorithm>
+#include <chrono>
+#include <mutex>
+#include <new>
+#include <thread>
+
+#include "ctx.cuh"
+#include "dedup.cuh"
+
+namespace svdag {
+namespace {
+
+// ---------------------------------------------------------------------------
+// Seeded 3D value noise (lattice period 16 voxels, trilinear), used to make
+// synthetic occupancy grids.
+__host__ __device__ __forceinline__ uint32_t hash3(uint32_t x, uint32_t y, uint32_t z, uint32_t s) {
+  uint32_t h = x * 0x8DA6B343u ^ y * 0xD8163841u ^ z * 0xCB1AB31Fu ^ s * 0x165667B1u;
+  h ^= h >> 15;
+  h *= 0x2C1B3C6Du;
+  h ^= h >> 12;
+  h *= 0x297A2D39u;
+  h ^= h >> 15;
+  return h;
+}
+__host__ __device__ __forceinline__ float lattice(uint32_t x, uint32_t y, uint32_t z, uint32_t s) {
+  return float(hash3(x, y, z, s) >> 8) * (1.0f / 16777216.0f);
+}
+__host__ __device__ __forceinline__ float value_noise3(uint32_t x, uint32_t y, uint32_t z, uint32_t s) {
+  const uint32_t X = x >> 4, Y = y >> 4, Z = z >> 4;
+  const float fx = float(x & 15u) * (1.0f / 16.0f), fy = float(y & 15u) * (1.0f / 16.0f),
+              fz = float(z & 15u) * (1.0f / 16.0f);
+  float c[2][2];
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) {
+      const float a = lattice(X + i, Y + j, Z, s), b = lattice(X + i, Y + j, Z + 1, s);
+      c[i][j] = a + (b - a) * fz;
+    }
+  const float c0 = c[0][0] + (c[0][1] - c[0][0]) * fy, c1 = c[1][0] + (c[1][1] - c[1][0]) * fy;
+  return c0 + (c1 - c0) * fx;
+}
+
+// Morton brick index -> brick coordinates (x most significant per triple).
+__host__ __device__ __forceinline__ void morton_decode(uint64_t m, uint32_t& x, uint32_t& y, uint32_t& z) {
+  x = y = z = 0;
+  for (int i = 0; i < 21; ++i) {
+    z |= uint32_t((m >> (3 * i)) & 1u) << i;
+    y |= uint32_t((m >> (3 * i + 1)) & 1u) << i;
+    x |= uint32_t((m >> (3 * i + 2)) & 1u) << i;
+  }
+}
+
+__global__ void k_noise_samples(uint32_t side, uint32_t seed, uint32_t n, float* out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t h = hash3(i, 0x51ED27u, 0x2F0Bu, seed ^ 0xA5A5A5A5u);
+    const uint32_t g = hash3(h, i, 7u, seed);
+    const uint32_t k = hash3(g, h, 11u, seed);
+    out[i] = value_noise3(h % side, g % side, k % side, seed);
+  }
+}
+
+__global__ void k_noise_bricks(uint64_t n_bricks, uint32_t seed, float thr, uint8_t* __restrict__ out) {
+  for (uint64_t b = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; b < n_bricks; b += uint64_t(gridDim.x) * blockDim.x) {
+    uint32_t bx, by, bz;
+    morton_decode(b, bx, by, bz);
+    uint32_t m = 0;
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      const uint32_t x = 2 * bx + ((v >> 2) & 1), y = 2 * by + ((v >> 1) & 1), z = 2 * bz + (v & 1);
+      m |= uint32_t(value_noise3(x, y, z, seed) < thr) << v;
+    }
+    out[b] = uint8_t(m);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Plain form: SVO pools of one chunk.
+
+// Cells of one level: occupancy from the level below (bricks or child ids).
+struct BrickNonEmpty {
+  const uint8_t* b;
+  __device__ __forceinline__ uint32_t operator()(uint64_t i) const { return b[i] ? 1u : 0u; }
+};
+struct CellNonEmpty {
+  const uint32_t* below;  // node index per cell of the level below (kNone = empty)
+  bool root;
+  __device__ __forceinline__ uint32_t operator()(uint64_t j) const {
+    if (root) return 1u;
+    const uint4 a = reinterpret_cast<const uint4*>(below + 8 * j)[0], b = reinterpret_cast<const uint4*>(below + 8 * j)[1];
+    return (a.x & a.y & a.z & a.w & b.x & b.y & b.z & b.w) == kNone ? 0u : 1u;
+  }
+};
+struct IndexOut {
+  uint32_t* idx;
+  const uint8_t* b;
+  const uint32_t* below;
+  bool root;
+  __device__ __forceinline__ void operator()(uint64_t j, uint32_t pos) const {
+    bool ne;
+    if (b) {
+      ne = b[j] != 0;
+    } else if (root) {
+      ne = true;
+    } else {
+      const uint4 a = reinterpret_cast<const uint4*>(below + 8 * j)[0], c = reinterpret_cast<const uint4*>(below + 8 * j)[1];
+      ne = (a.x & a.y & a.z & a.w & c.x & c.y & c.z & c.w) != kNone;
+    }
+    idx[j] = ne ? pos : kNone;
+  }
+};
+
+__global__ void k_leaf_nodes(const uint8_t* __restrict__ b, uint64_t n, const uint32_t* __restrict__ idx,
+                             uint32_t* __restrict__ hdr, unsigned long long* vox) {
+  uint64_t s = 0;
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t m = b[i];
+    if (m) {
+      hdr[idx[i]] = m;
+      s += __popc(m);
+    }
+  }
+  for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, o);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(vox, (unsigned long long)s);
+}
+
+__global__ void k_inner_nodes(const uint32_t* __restrict__ below, uint64_t n, const uint32_t* __restrict__ idx,
+                              uint32_t* __restrict__ hdr, uint32_t* __restrict__ ch) {
+  for (uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; j < n; j += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t id = idx[j];
+    if (id == kNone) continue;
+    uint32_t c[8], m = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const uint32_t v = below[8 * j + k];
+      c[k] = (v == kNone) ? kNull : v;
+      m |= uint32_t(v != kNone) << k;
+    }
+    hdr[id] = m;
+    store_children(ch, id, c);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Batched form.
+
+struct ChunkSet {
+  const uint64_t* base;   // [n+1] global cell offset of each chunk at this height
+  uint32_t n;
+};
+__device__ __forceinline__ uint32_t chunk_of(const ChunkSet& S, uint64_t g) {
+  uint32_t lo = 0, hi = S.n;  // base[lo] <= g < base[hi]
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (S.base[mid] <= g) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+struct HeightView {
+  ChunkSet cells;                // cells of this height
+  const uint32_t* part;          // [n] chunk id of each participating entry
+  const uint8_t* const* bricks;  // [n] (height 1) bricks of each entry
+  const uint32_t* leaf_rank;     // [chunks*256] (height 1) leaf DAG id per mask
+  const uint64_t* below_base;    // [n] (height >= 2) global offset of each entry's cells one height down
+  const uint32_t* below_ids;     // (height >= 2) DAG id per cell one height down (kNone = empty)
+  const uint8_t* is_top;         // [n] 1 when this height is the entry's root level
+  uint32_t h;
+};
+
+// Key of cell g: chunk, mask and the DAG ids of its 8 children.
+__device__ __forceinline__ uint32_t cell_key(const HeightView& V, uint64_t g, uint32_t& e, uint32_t ids[8]) {
+  e = chunk_of(V.cells, g);
+  const uint64_t j = g - V.cells.base[e];
+  uint32_t m = 0;
+  if (V.h == 1) {
+    const uint64_t w = reinterpret_cast<const uint64_t*>(V.bricks[e])[j];
+    const uint32_t* rk = V.leaf_rank + 256u * V.part[e];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const uint32_t b = uint32_t(w >> (8 * k)) & 0xFFu;
+      ids[k] = b ? rk[b] : kNull;
+      m |= uint32_t(b != 0) << k;
+    }
+  } else {
+    const uint4* p = reinterpret_cast<const uint4*>(V.below_ids + V.below_base[e] + 8 * j);
+    const uint4 a = p[0], c = p[1];
+    const uint32_t v[8] = {a.x, a.y, a.z, a.w, c.x, c.y, c.z, c.w};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      ids[k] = (v[k] == kNone) ? kNull : v[k];
+      m |= uint32_t(v[k] != kNone) << k;
+    }
+  }
+  return m;
+}
+
+__device__ __forceinline__ uint64_t key_hash(uint32_t chunk, uint32_t m, const uint32_t ids[8]) {
+  uint64_t h = mix_word(0x243F6A8885A308D3ull, chunk);
+  h = mix_word(h, m);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) h = mix_word(h, ids[k]);
+  return finish_hash(h);
+}
+
+constexpr int kGBits = 40;  // cell index bits in a slot (the rest: hash tag)
+constexpr uint64_t kGMask = (1ull << kGBits) - 1;
+
+__global__ void k_batch_insert(HeightView V, uint64_t total, unsigned long long* __restrict__ slots, uint64_t mask,
+                               int* err) {
+  for (uint64_t g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; g < total; g += uint64_t(gridDim.x) * blockDim.x) {
+    uint32_t e, ids[8];
+    const uint32_t m = cell_key(V, g, e, ids);
+    if (!m && !V.is_top[e]) continue;
+    const uint32_t chunk = V.part[e];
+    const uint64_t hk = key_hash(chunk, m, ids);
+    const uint64_t tag = hk >> kGBits;
+    const unsigned long long mine = (tag << kGBits) | g;
+    uint64_t pos = hk & mask;
+    bool done = false;
+    for (uint64_t probe = 0; probe <= mask && !done; ++probe) {
+      unsigned long long cur = __ldcg(&slots[pos]);
+      if (cur == kEmpty64) {
+        const unsigned long long prev = atomicCAS(&slots[pos], kEmpty64, mine);
+        if (prev == kEmpty64) { done = true; break; }
+        cur = prev;
+      }
+      if ((cur >> kGBits) == tag) {
+        const uint64_t g2 = cur & kGMask;
+        uint32_t e2, ids2[8];
+        const uint32_t m2 = cell_key(V, g2, e2, ids2);
+        bool eq = (V.part[e2] == chunk) && (m2 == m);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) eq &= (ids2[k] == ids[k]);
+        if (eq) {
+          if (g < g2) atomicMin(&slots[pos], mine);
+          done = true;
+          break;
+        }
+      }
+      pos = (pos + 1) & mask;
+    }
+    if (!done) atomicExch(err, 1);
+  }
+}
+
+// The representative (smallest index with the same key) of every non-empty
+// cell, found by a lookup of its own key.
+__global__ void k_batch_rep(HeightView V, uint64_t total, const unsigned long long* __restrict__ slots, uint64_t mask,
+                            uint64_t* __restrict__ rep) {
+  for (uint64_t g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; g < total; g += uint64_t(gridDim.x) * blockDim.x) {
+    uint32_t e, ids[8];
+    const uint32_t m = cell_key(V, g, e, ids);
+    if (!m && !V.is_top[e]) { rep[g] = ~0ull; continue; }
+    const uint32_t chunk = V.part[e];
+    const uint64_t hk = key_hash(chunk, m, ids);
+    const uint64_t tag = hk >> kGBits;
+    uint64_t pos = hk & mask;
+    uint64_t r = ~0ull;
+    for (uint64_t probe = 0; probe <= mask; ++probe) {
+      const unsigned long long cur = slots[pos];
+      if (cur == kEmpty64) break;
+      if ((cur >> kGBits) == tag) {
+        const uint64_t g2 = cur & kGMask;
+        uint32_t e2, ids2[8];
+        const uint32_t m2 = cell_key(V, g2, e2, ids2);
+        bool eq = (V.part[e2] == chunk) && (m2 == m);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) eq &= (ids2[k] == ids[k]);
+        if (eq) { r = g2; break; }
+      }
+      pos = (pos + 1) & mask;
+    }
+    rep[g] = r;
+  }
+}
+
+struct RepIn {
+  const uint64_t* rep;
+  __device__ __forceinline__ uint64_t operator()(uint64_t g) const { return rep[g] == g ? 1u : 0u; }
+};
+struct U64Out {
+  uint64_t* a;
+  __device__ __forceinline__ void operator()(uint64_t i, uint64_t v) const { a[i] = v; }
+};
+
+// DAG id (within the chunk) of every cell, and the DAG nodes of this height.
+__global__ void k_batch_emit(HeightView V, uint64_t total, const uint64_t* __restrict__ rep,
+                             const uint64_t* __restrict__ newid, const uint64_t* __restrict__ rep_base,
+                             uint32_t* __restrict__ ids_out, uint32_t* __restrict__ hdr, uint32_t* __restrict__ ch) {
+  for (uint64_t g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; g < total; g += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t r = rep[g];
+    if (r == ~0ull) { ids_out[g] = kNone; continue; }
+    const uint32_t e = chunk_of(V.cells, g);
+    ids_out[g] = uint32_t(newid[r] - rep_base[e]);
+    if (r == g) {
+      uint32_t e2, ids[8];
+      const uint32_t m = cell_key(V, g, e2, ids);
+      const uint64_t id = newid[g];
+      hdr[id] = m;
+      store_children(ch, id, ids);
+    }
+  }
+}
+
+// Leaf height: first occurrence of every mask per chunk, ranks, voxel counts.
+__global__ void k_batch_leaf_first(const uint8_t* const* __restrict__ bricks, const uint64_t* __restrict__ n_bricks,
+                                   uint32_t* __restrict__ first, unsigned long long* __restrict__ vox) {
+  const uint32_t c = blockIdx.y;
+  const uint8_t* b = bricks[c];
+  const uint64_t n = n_bricks[c];
+  __shared__ uint32_t sf[256];
+  for (int m = threadIdx.x; m < 256; m += blockDim.x) sf[m] = kNone;
+  __syncthreads();
+  unsigned long long s = 0;
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t m = b[i];
+    if (m) {
+      s += __popc(m);
+      if (sf[m] > uint32_t(i)) atomicMin(&sf[m], uint32_t(i));
+    }
+  }
+  __syncthreads();
+  for (int m = threadIdx.x; m < 256; m += blockDim.x)
+    if (sf[m] != kNone) atomicMin(&first[256u * c + m], sf[m]);
+  for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, o);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(&vox[c], s);
+}
+
+__global__ void k_batch_leaf_rank(const uint32_t* __restrict__ first, uint32_t* __restrict__ rank,
+                                  uint32_t* __restrict__ leaf_hdr, uint32_t* __restrict__ leaf_count) {
+  const uint32_t c = blockIdx.x;
+  __shared__ uint32_t sf[256];
+  const int m = threadIdx.x;
+  sf[m] = first[256u * c + m];
+  __syncthreads();
+  if (sf[m] != kNone) {
+    uint32_t r = 0;
+    for (int k = 0; k < 256; ++k) r += (sf[k] < sf[m]) ? 1u : 0u;
+    rank[256u * c + m] = r;
+    leaf_hdr[256u * c + r] = uint32_t(m);
+  } else {
+    rank[256u * c + m] = kNone;
+  }
+  if (m == 0) {
+    uint32_t n = 0;
+    for (int k = 0; k < 256; ++k) n += (sf[k] != kNone) ? 1u : 0u;
+    leaf_count[c] = n;
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+float synth_noise_bricks(cudaStream_t st, uint32_t depth, uint64_t seed, double fill, uint8_t* out) {
+  if (depth < 2 || depth > 11) throw Error(SVDAG_ERR_INVALID_ARG, "noise bricks: depth must be in [2, 11]");
+  if (!(fill > 0.0 && fill < 1.0)) throw Error(SVDAG_ERR_INVALID_ARG, "noise bricks: fill must be in (0, 1)");
+  const uint32_t s32 = uint32_t(seed ^ (seed >> 32));
+  const uint32_t ns = 1u << 16;
+  DBuf<float> smp(ns, st);
+  k_noise_samples<<<64, 256, 0, st>>>(1u << depth, s32, ns, smp.get());
+  SVDAG_CUDA(cudaPeekAtLastError());
+  std::vector<float> h(ns);
+  SVDAG_CUDA(cudaMemcpyAsync(h.data(), smp.get(), 4ull * ns, cudaMemcpyDeviceToHost, st));
+  SVDAG_CUDA(cudaStreamSynchronize(st));
+  const size_t k = std::min<size_t>(ns - 1, size_t(fill * ns));
+  std::nth_element(h.begin(), h.begin() + k, h.end());
+  const float thr = h[k];
+  const uint64_t nb = 1ull << (3 * (depth - 1));
+  k_noise_bricks<<<unsigned(std::min<uint64_t>((nb + 255) / 256, 152ull * 16)), 256, 0, st>>>(nb, s32, thr, out);
+  SVDAG_CUDA(cudaPeekAtLastError());
+  return thr;
+}
+
+void phase_import_bricks(Ctx& c, uint32_t depth, const uint8_t* bricks) {
+  if (depth < 2 || depth > 11) throw Error(SVDAG_ERR_INVALID_ARG, "import_bricks: depth must be in [2, 11]");
+  if (!bricks || (reinterpret_cast<uintptr_t>(bricks) & 7u))
+    throw Error(SVDAG_ERR_INVALID_ARG, "import_bricks: bricks must be a device pointer aligned to 8 bytes");
+  const Exec& ex = c.ex;
+  const cudaStream_t st = c.stream;
+  c.levels = depth;
+  c.lev.clear();
+  c.lev.resize(depth);
+  c.child_levels_init = false;
+  DBuf<uint32_t> idx, up, d_n(1, st);
+  DBuf<unsigned long long> d_vox(1, st);
+  SVDAG_CUDA(cudaMemsetAsync(d_vox.get(), 0, 8, st));
+  // leaves
+  uint64_t cells = 1ull << (3 * (depth - 1));
+  idx.alloc(cells, st);
+  device_exclusive_scan<uint32_t>(ex, BrickNonEmpty{bricks}, cells, IndexOut{idx.get(), bricks, nullptr, false},
+                                  d_n.get());
+  uint64_t n = read_scalar(ex, d_n.get());
+  {
+    Level& L = c.lev[depth - 1];
+    L.n = n;
+    L.hdr.alloc(n ? n : 1, st);
+    SVDAG_LAUNCH(ex, k_leaf_nodes, grid_for(ex, cells, 256), 256, 0, bricks, cells, idx.get(), L.hdr.get(), d_vox.get());
+  }
+  for (int l = int(depth) - 2; l >= 0; --l) {
+    cells >>= 3;
+    up.alloc(cells, st);
+    device_exclusive_scan<uint32_t>(ex, CellNonEmpty{idx.get(), l == 0}, cells,
+                                    IndexOut{up.get(), nullptr, idx.get(), l == 0}, d_n.get());
+    n = read_scalar(ex, d_n.get());
+    Level& L = c.lev[l];
+    L.n = n;
+    L.hdr.alloc(n ? n : 1, st);
+    L.ch.alloc(8 * (n ? n : 1), st);
+    SVDAG_LAUNCH(ex, k_inner_nodes, grid_for(ex, cells, 256), 256, 0, idx.get(), cells, up.get(), L.hdr.get(),
+                 L.ch.get());
+    std::swap(idx, up);
+  }
+  uint64_t nodes = 0;
+  for (uint32_t l = 0; l < depth; ++l) nodes += c.lev[l].n;
+  c.st = svdag_stats{};
+  c.st.levels = depth;
+  c.st.n_total_voxels = read_scalar(ex, d_vox.get());
+  c.st.n_nodes = nodes;
+  c.st.n_nodes_dag = nodes;
+  c.state = SVDAG_S_DAG;  // the NodeData constructor's state
+}
+
+// ---------------------------------------------------------------------------
+void batch_build_dags(Batch& B) {
+  const Exec& ex = B.ex;
+  const cudaStream_t st = B.stream;
+  const uint32_t N = uint32_t(B.chunks.size());
+  B.results.clear();
+  B.results.resize(N);
+  if (!N) return;
+  uint32_t maxd = 0;
+  for (auto& ch : B.chunks) maxd = std::max(maxd, ch.depth);
+
+  // --- leaf height: per-chunk first occurrence of every mask
+  std::vector<const uint8_t*> hb(N);
+  std::vector<uint64_t> hn(N);
+  for (uint32_t c = 0; c < N; ++c) { hb[c] = B.chunks[c].bricks; hn[c] = 1ull << (3 * (B.chunks[c].depth - 1)); }
+  DBuf<const uint8_t*> d_bricks(N, st);
+  DBuf<uint64_t> d_nb(N, st);
+  DBuf<uint32_t> first(256ull * N, st), rank(256ull * N, st), leaf_hdr(256ull * N, st), leaf_cnt(N, st);
+  DBuf<unsigned long long> vox(N, st);
+  DBuf<int> d_err(1, st);
+  SVDAG_CUDA(cudaMemcpyAsync(d_bricks.get(), hb.data(), sizeof(void*) * N, cudaMemcpyHostToDevice, st));
+  SVDAG_CUDA(cudaMemcpyAsync(d_nb.get(), hn.data(), 8ull * N, cudaMemcpyHostToDevice, st));
+  SVDAG_CUDA(cudaMemsetAsync(first.get(), 0xFF, 4 * 256ull * N, st));
+  SVDAG_CUDA(cudaMemsetAsync(vox.get(), 0, 8ull * N, st));
+  SVDAG_CUDA(cudaMemsetAsync(d_err.get(), 0, 4, st));
+  {
+    uint64_t mx = 0;
+    for (auto v : hn) mx = std::max(mx, v);
+    const unsigned gx = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((mx + 255) / 256, 2048)));
+    SVDAG_LAUNCH(ex, k_batch_leaf_first, dim3(gx, N), 256, 0, d_bricks.get(), d_nb.get(), first.get(), vox.get());
+  }
+  SVDAG_LAUNCH(ex, k_batch_leaf_rank, N, 256, 0, first.get(), rank.get(), leaf_hdr.get(), leaf_cnt.get());
+  std::vector<uint32_t> h_leaf_cnt(N);
+  std::vector<unsigned long long> h_vox(N);
+  SVDAG_CUDA(cudaMemcpyAsync(h_leaf_cnt.data(), leaf_cnt.get(), 4ull * N, cudaMemcpyDeviceToHost, st));
+  SVDAG_CUDA(cudaMemcpyAsync(h_vox.data(), vox.get(), 8ull * N, cudaMemcpyDeviceToHost, st));
+  SVDAG_CUDA(cudaStreamSynchronize(st));
+  for (uint32_t c = 0; c < N; ++c) {
+    BatchResult& R = B.results[c];
+    const uint32_t d = B.chunks[c].depth;
+    R.dag.reset(new svdag_ctx());
+    Ctx& X = R.dag->c;
+    X.device = B.device;
+    X.stream = st;
+    X.ex = B.ex;
+    X.levels = d;
+    X.lev.resize(d);
+    X.state = SVDAG_S_DAG;
+    X.st = svdag_stats{};
+    X.st.levels = d;
+    X.st.n_total_voxels = h_vox[c];
+    Level& L = X.lev[d - 1];
+    L.n = h_leaf_cnt[c];
+    L.hdr.alloc(L.n ? L.n : 1, st);
+    if (L.n)
+      SVDAG_CUDA(cudaMemcpyAsync(L.hdr.get(), leaf_hdr.get() + 256ull * c, 4ull * L.n, cudaMemcpyDeviceToDevice, st));
+  }
+
+  // --- heights 1 .. maxd-1
+  DBuf<uint32_t> below_ids;  // DAG ids of the cells one height down
+  std::vector<uint64_t> below_base_h;
+  std::vector<uint32_t> below_part;
+  for (uint32_t h = 1; h < maxd; ++h) {
+    std::vector<uint32_t> part;
+    std::vector<uint64_t> base{0};
+    std::vector<uint8_t> top;
+    std::vector<const uint8_t*> pb;
+    std::vector<uint64_t> bb;  // below base per entry
+    // entries deepest first, so every entry's cell range starts on a multiple
+    // of 8 except the single root cells at the end (16-byte child-id loads)
+    std::vector<uint32_t> order(N);
+    for (uint32_t c = 0; c < N; ++c) order[c] = c;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t a, uint32_t b) { return B.chunks[a].depth > B.chunks[b].depth; });
+    for (uint32_t c : order) {
+      const uint32_t d = B.chunks[c].depth;
+      if (d <= h) continue;
+      const uint32_t l = d - 1 - h;
+      part.push_back(c);
+      base.push_back(base.back() + (1ull << (3 * l)));
+      top.push_back(l == 0 ? 1 : 0);
+      pb.push_back(B.chunks[c].bricks);
+      if (h >= 2) {
+        const size_t k = size_t(std::find(below_part.begin(), below_part.end(), c) - below_part.begin());
+        bb.push_back(below_base_h[k]);
+      } else {
+        bb.push_back(0);
+      }
+    }
+    const uint32_t n = uint32_t(part.size());
+    const uint64_t total = base.back();
+    if (total > kGMask) throw Error(SVDAG_ERR_OVERFLOW, "batch: more than 2^40 cells on one height");
+    DBuf<uint64_t> d_base(n + 1, st), d_bb(n, st);
+    DBuf<uint32_t> d_part(n, st);
+    DBuf<uint8_t> d_top(n, st);
+    DBuf<const uint8_t*> d_pb(n, st);
+    SVDAG_CUDA(cudaMemcpyAsync(d_base.get(), base.data(), 8ull * (n + 1), cudaMemcpyHostToDevice, st));
+    SVDAG_CUDA(cudaMemcpyAsync(d_bb.get(), bb.data(), 8ull * n, cudaMemcpyHostToDevice, st));
+    SVDAG_CUDA(cudaMemcpyAsync(d_part.get(), part.data(), 4ull * n, cudaMemcpyHostToDevice, st));
+    SVDAG_CUDA(cudaMemcpyAsync(d_top.get(), top.data(), n, cudaMemcpyHostToDevice, st));
+    SVDAG_CUDA(cudaMemcpyAsync(d_pb.get(), pb.data(), sizeof(void*) * n, cudaMemcpyHostToDevice, st));
+    HeightView V;
+    V.cells = ChunkSet{d_base.get(), n};
+    V.part = d_part.get();
+    V.bricks = d_pb.get();
+    V.leaf_rank = rank.get();
+    V.below_base = d_bb.get();
+    V.below_ids = below_ids.get();
+    V.is_top = d_top.get();
+    V.h = h;
+
+    // hash table sized from the cell count (load <= 1 / B.tuning.table_factor)
+    const uint64_t size = next_pow2(uint64_t(double(std::max<uint64_t>(total, 16)) * B.tuning.table_factor));
+    DBuf<unsigned long long> slots(size, st);
+    SVDAG_CUDA(cudaMemsetAsync(slots.get(), 0xFF, 8 * size, st));
+    const unsigned tb = B.tuning.threads;
+    SVDAG_LAUNCH(ex, k_batch_insert, grid_for(ex, total, tb, 8), tb, 0, V, total, slots.get(), size - 1, d_err.get());
+    DBuf<uint64_t> rep(total, st), newid(total, st);
+    SVDAG_LAUNCH(ex, k_batch_rep, grid_for(ex, total, tb, 8), tb, 0, V, total, slots.get(), size - 1, rep.get());
+    slots.release();
+    DBuf<uint64_t> d_total(1, st);
+    device_exclusive_scan<uint64_t>(ex, RepIn{rep.get()}, total, U64Out{newid.get()}, d_total.get());
+    // DAG nodes of each entry: newid range [newid at its first cell, next entry's)
+    std::vector<uint64_t> rep_base(n + 1);
+    {
+      DBuf<uint64_t> d_rb(n, st);
+      std::vector<uint64_t> h_nid(n);
+      for (uint32_t e = 0; e < n; ++e)
+        SVDAG_CUDA(cudaMemcpyAsync(&h_nid[e], newid.get() + base[e], 8, cudaMemcpyDeviceToHost, st));
+      SVDAG_CUDA(cudaMemcpyAsync(&rep_base[n], d_total.get(), 8, cudaMemcpyDeviceToHost, st));
+      SVDAG_CUDA(cudaStreamSynchronize(st));
+      for (uint32_t e = 0; e < n; ++e) rep_base[e] = h_nid[e];
+    }
+    DBuf<uint64_t> d_rep_base(n, st);
+    SVDAG_CUDA(cudaMemcpyAsync(d_rep_base.get(), rep_base.data(), 8ull * n, cudaMemcpyHostToDevice, st));
+    const uint64_t nodes = rep_base[n];
+    DBuf<uint32_t> hdr(nodes ? nodes : 1, st), ch(8 * (nodes ? nodes : 1), st), ids(total, st);
+    SVDAG_LAUNCH(ex, k_batch_emit, grid_for(ex, total, tb, 8), tb, 0, V, total, rep.get(), newid.get(),
+                 d_rep_base.get(), ids.get(), hdr.get(), ch.get());
+    // hand each entry its level
+    for (uint32_t e = 0; e < n; ++e) {
+      const uint32_t c = part[e];
+      Ctx& X = B.results[c].dag->c;
+      Level& L = X.lev[B.chunks[c].depth - 1 - h];
+      L.n = rep_base[e + 1] - rep_base[e];
+      L.hdr.alloc(L.n ? L.n : 1, st);
+      L.ch.alloc(8 * (L.n ? L.n : 1), st);
+      if (L.n) {
+        SVDAG_CUDA(cudaMemcpyAsync(L.hdr.get(), hdr.get() + rep_base[e], 4 * L.n, cudaMemcpyDeviceToDevice, st));
+        SVDAG_CUDA(cudaMemcpyAsync(L.ch.get(), ch.get() + 8 * rep_base[e], 32 * L.n, cudaMemcpyDeviceToDevice, st));
+      }
+    }
+    below_ids = std::move(ids);
+    below_base_h.assign(base.begin(), base.end() - 1);
+    below_part = part;
+  }
+  check_err(ex, d_err.get(), "batch toDAG");
+  for (uint32_t c = 0; c < N; ++c) {
+    Ctx& X = B.results[c].dag->c;
+    uint64_t nodes = 0;
+    for (auto& L : X.lev) nodes += L.n;
+    X.st.n_nodes = nodes;
+    X.st.n_nodes_dag = nodes;
+  }
+}
+
+// SSVDAG and CSVDAG of every chunk's DAG, on B.tuning.streams streams.
+void batch_reduce(Batch& B, bool sdag, bool csv) {
+  const uint32_t N = uint32_t(B.results.size());
+  if (!N || (!sdag && !csv)) return;
+  SVDAG_CUDA(cudaStreamSynchronize(B.stream));
+  const int W = std::max(1, std::min<int>(B.tuning.streams, int(N)));
+  // worker streams live as long as the batch: the results' buffers are
+  // stream-ordered allocations on them
+  while (int(B.streams.size()) < W) {
+    cudaStream_t s;
+    SVDAG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    B.streams.push_back(s);
+  }
+  const std::vector<cudaStream_t>& streams = B.streams;
+  std::mutex mu;
+  uint32_t next = 0;
+  std::string err;
+  int err_code = SVDAG_OK;
+  auto work = [&](int w) {
+    try {
+      SVDAG_CUDA(cudaSetDevice(B.device));
+      for (;;) {
+        uint32_t c;
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          if (next >= N || err_code != SVDAG_OK) return;
+          c = next++;
+        }
+        BatchResult& R = B.results[c];
+        auto clone_of = [&](const svdag_ctx* src) {
+          std::unique_ptr<svdag_ctx> o(new svdag_ctx());
+          Ctx& X = o->c;
+          const Ctx& S = src->c;
+          X.device = S.device;
+          X.stream = streams[w];
+          X.ex = B.ex;
+          X.ex.stream = streams[w];
+          X.ex.launches = &B.worker_launches[w];
+          X.ex.prof = nullptr;
+          X.levels = S.levels;
+          X.state = S.state;
+          X.st = S.st;
+          X.lev.resize(S.lev.size());
+          for (size_t l = 0; l < S.lev.size(); ++l) {
+            const Level& a = S.lev[l];
+            Level& b = X.lev[l];
+            b.n = a.n;
+            b.hdr.alloc(a.n ? a.n : 1, streams[w]);
+            if (a.n) SVDAG_CUDA(cudaMemcpyAsync(b.hdr.get(), a.hdr.get(), 4 * a.n, cudaMemcpyDeviceToDevice, streams[w]));
+            if (a.ch.get()) {
+              b.ch.alloc(8 * (a.n ? a.n : 1), streams[w]);
+              if (a.n)
+                SVDAG_CUDA(cudaMemcpyAsync(b.ch.get(), a.ch.get(), 32 * a.n, cudaMemcpyDeviceToDevice, streams[w]));
+            }
+          }
+          return o;
+        };
+        if (sdag) {
+          R.sdag = clone_of(R.dag.get());
+          phase_reduce_sdag(R.sdag->c);
+        }
+        if (csv && R.dag->c.levels >= 2) {
+          R.csv = clone_of(R.dag.get());
+          R.csv->c.child_levels_init = true;  // initChildLevels before the merge, as svbuilder does
+          phase_cross_level_merge(R.csv->c);
+        }
+        SVDAG_CUDA(cudaStreamSynchronize(streams[w]));
+      }
+    } catch (const Error& e) {
+      std::lock_guard<std::mutex> lk(mu);
+      if (err_code == SVDAG_OK) { err_code = e.code; err = e.what(); }
+    }
+  };
+  B.worker_launches.assign(W, 0);
+  std::vector<std::thread> th;
+  for (int w = 1; w < W; ++w) th.emplace_back(work, w);
+  work(0);
+  for (auto& t : th) t.join();
+  for (auto v : B.worker_launches) B.launches += v;
+  if (err_code != SVDAG_OK) throw Error(err_code, err);
+}
+
+}  // namespace svdag
+
+// ---------------------------------------------------------------------------
+// C ABI (include/svdag_gpu.h)
+namespace {
+
+using svdag::Batch;
+using svdag::Error;
+
+template <class F>
+int batch_guarded(svdag_batch* h, F&& f) {
+  if (!h) return SVDAG_ERR_INVALID_ARG;
+  try {
+    SVDAG_CUDA(cudaSetDevice(h->b.device));
+    f(h->b);
+    h->b.last_error.clear();
+    return SVDAG_OK;
+  } catch (const Error& e) {
+    h->b.last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    h->b.last_error = "host allocation failed";
+    return SVDAG_ERR_OOM;
+  } catch (const std::exception& e) {
+    h->b.last_error = e.what();
+    return SVDAG_ERR_CUDA;
+  }
+}
+
+double wall_ms(const std::chrono::steady_clock::time_point& t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void run_batch(Batch& B, uint32_t flags) {
+  const auto t0 = std::chrono::steady_clock::now();
+  svdag::batch_build_dags(B);
+  SVDAG_CUDA(cudaStreamSynchronize(B.stream));
+  B.dag_ms = wall_ms(t0);
+  const auto t1 = std::chrono::steady_clock::now();
+  svdag::batch_reduce(B, (flags & SVDAG_BATCH_SDAG) != 0, (flags & SVDAG_BATCH_CSVDAG) != 0);
+  B.reduce_ms = wall_ms(t1);
+}
+
+}  // namespace
+
+extern "C" {
+
+int svdag_synth_noise_bricks(void* stream, uint32_t depth, uint64_t seed, double fill, uint8_t* device_bricks,
+                             float* threshold) {
+  if (!device_bricks) return SVDAG_ERR_INVALID_ARG;
+  try {
+    const float t = svdag::synth_noise_bricks(static_cast<cudaStream_t>(stream), depth, seed, fill, device_bricks);
+    if (threshold) *threshold = t;
+    return SVDAG_OK;
+  } catch (const Error& e) {
+    return e.code;
+  } catch (const std::exception&) {
+    return SVDAG_ERR_CUDA;
+  }
+}
+
+int svdag_import_bricks(svdag_ctx* h, uint32_t depth, const uint8_t* device_bricks) {
+  if (!h) return SVDAG_ERR_INVALID_ARG;
+  svdag::Ctx& c = h->c;
+  try {
+    SVDAG_CUDA(cudaSetDevice(c.device));
+    SVDAG_CUDA(cudaEventRecord(c.ev0, c.stream));
+    svdag::phase_import_bricks(c, depth, device_bricks);
+    SVDAG_CUDA(cudaEventRecord(c.ev1, c.stream));
+    SVDAG_CUDA(cudaEventSynchronize(c.ev1));
+    float ms = 0.f;
+    SVDAG_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+    c.st.svo_ms = double(ms);
+    c.last_error.clear();
+    return SVDAG_OK;
+  } catch (const Error& e) {
+    c.last_error = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    c.last_error = e.what();
+    return SVDAG_ERR_CUDA;
+  }
+}
+
+int svdag_batch_create(svdag_batch** out, int device, void* stream) {
+  if (!out) return SVDAG_ERR_INVALID_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return SVDAG_ERR_NO_DEVICE;
+  if (device < 0 || device >= n) return SVDAG_ERR_INVALID_ARG;
+  svdag_batch* h = new (std::nothrow) svdag_batch();
+  if (!h) return SVDAG_ERR_OOM;
+  Batch& B = h->b;
+  B.device = device;
+  if (cudaSetDevice(device) != cudaSuccess) { delete h; return SVDAG_ERR_CUDA; }
+  if (stream) {
+    B.stream = static_cast<cudaStream_t>(stream);
+  } else {
+    if (cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking) != cudaSuccess) { delete h; return SVDAG_ERR_CUDA; }
+    B.own_stream = true;
+  }
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  B.ex.stream = B.stream;
+  B.ex.sm_count = sms;
+  B.ex.launches = &B.launches;
+  *out = h;
+  return SVDAG_OK;
+}
+
+int svdag_batch_destroy(svdag_batch* h) {
+  if (!h) return SVDAG_ERR_INVALID_ARG;
+  Batch& B = h->b;
+  cudaSetDevice(B.device);
+  cudaDeviceSynchronize();
+  B.results.clear();
+  for (auto s : B.streams) cudaStreamDestroy(s);
+  if (B.own_stream) cudaStreamDestroy(B.stream);
+  delete h;
+  return SVDAG_OK;
+}
+
+const char* svdag_batch_last_error(const svdag_batch* h) { return h ? h->b.last_error.c_str() : "null batch"; }
+
+int svdag_batch_clear(svdag_batch* h) {
+  return batch_guarded(h, [&](Batch& B) {
+    SVDAG_CUDA(cudaStreamSynchronize(B.stream));
+    B.results.clear();
+    B.chunks.clear();
+  });
+}
+
+int svdag_batch_add_chunk(svdag_batch* h, uint32_t depth, const uint8_t* device_bricks) {
+  return batch_guarded(h, [&](Batch& B) {
+    if (depth < 2 || depth > 11) throw Error(SVDAG_ERR_INVALID_ARG, "batch: chunk depth must be in [2, 11]");
+    if (!device_bricks || (reinterpret_cast<uintptr_t>(device_bricks) & 7u))
+      throw Error(SVDAG_ERR_INVALID_ARG, "batch: bricks must be a device pointer aligned to 8 bytes");
+    B.chunks.push_back(svdag::BatchChunk{depth, device_bricks});
+  });
+}
+
+int svdag_batch_chunk_count(const svdag_batch* h, uint32_t* n) {
+  if (!h || !n) return SVDAG_ERR_INVALID_ARG;
+  *n = uint32_t(h->b.chunks.size());
+  return SVDAG_OK;
+}
+
+int svdag_batch_build(svdag_batch* h, uint32_t flags) {
+  return batch_guarded(h, [&](Batch& B) { run_batch(B, flags); });
+}
+
+int svdag_batch_result(svdag_batch* h, uint32_t chunk, uint32_t kind, svdag_ctx** view) {
+  return batch_guarded(h, [&](Batch& B) {
+    if (!view) throw Error(SVDAG_ERR_INVALID_ARG, "batch_result: null view");
+    if (chunk >= B.results.size()) throw Error(SVDAG_ERR_INVALID_ARG, "batch_result: no such chunk (build first)");
+    svdag::BatchResult& R = B.results[chunk];
+    svdag_ctx* v = kind == SVDAG_BATCH_RESULT_DAG ? R.dag.get()
+                   : kind == SVDAG_BATCH_RESULT_SDAG ? R.sdag.get()
+                   : kind == SVDAG_BATCH_RESULT_CSVDAG ? R.csv.get() : nullptr;
+    if (!v) throw Error(SVDAG_ERR_INVALID_STATE, "batch_result: this result was not built");
+    *view = v;
+  });
+}
+
+int svdag_batch_set_tuning(svdag_batch* h, const svdag_batch_tuning* t) {
+  return batch_guarded(h, [&](Batch& B) {
+    if (!t || !(t->table_factor >= 1.25 && t->table_factor <= 16.0) || t->threads < 64 || t->threads > 1024 ||
+        (t->threads & 31u) || t->streams < 1 || t->streams > 64)
+      throw Error(SVDAG_ERR_INVALID_ARG, "batch tuning out of range");
+    B.tuning.table_factor = t->table_factor;
+    B.tuning.threads = t->threads;
+    B.tuning.streams = int(t->streams);
+  });
+}
+
+int svdag_batch_get_tuning(const svdag_batch* h, svdag_batch_tuning* t) {
+  if (!h || !t) return SVDAG_ERR_INVALID_ARG;
+  t->table_factor = h->b.tuning.table_factor;
+  t->threads = h->b.tuning.threads;
+  t->streams = uint32_t(h->b.tuning.streams);
+  return SVDAG_OK;
+}
+
+// Coordinate search over the three settings on the current chunks (each trial
+// is a full build); keeps the fastest and leaves its results in place.
+int svdag_batch_autotune(svdag_batch* h, uint32_t flags, uint32_t max_trials) {
+  return batch_guarded(h, [&](Batch& B) {
+    auto trial = [&]() {
+      const auto t0 = std::chrono::steady_clock::now();
+      run_batch(B, flags);
+      return wall_ms(t0);
+    };
+    uint32_t trials = 0;
+    double best = trial();
+    ++trials;
+    const double tf[] = {1.5, 2.0, 3.0, 4.0};
+    const unsigned th[] = {128, 256, 512};
+    const int sm[] = {1, 2, 4, 8, 16};
+    for (int pass = 0; pass < 2 && trials < max_trials; ++pass) {
+      for (double v : tf) {
+        if (trials >= max_trials || v == B.tuning.table_factor) continue;
+        const double old = B.tuning.table_factor;
+        B.tuning.table_factor = v;
+        const double t = trial();
+        ++trials;
+        if (t < best) best = t; else B.tuning.table_factor = old;
+      }
+      for (unsigned v : th) {
+        if (trials >= max_trials || v == B.tuning.threads) continue;
+        const unsigned old = B.tuning.threads;
+        B.tuning.threads = v;
+        const double t = trial();
+        ++trials;
+        if (t < best) best = t; else B.tuning.threads = old;
+      }
+      for (int v : sm) {
+        if (trials >= max_trials || v == B.tuning.streams) continue;
+        const int old = B.tuning.streams;
+        B.tuning.streams = v;
+        const double t = trial();
+        ++trials;
+        if (t < best) best = t; else B.tuning.streams = old;
+      }
+    }
+    run_batch(B, flags);  // results of the chosen setting
+  });
+}
+
+int svdag_batch_get_stats(const svdag_batch* h, svdag_batch_stats* out) {
+  if (!h || !out) return SVDAG_ERR_INVALID_ARG;
+  out->dag_ms = h->b.dag_ms;
+  out->reduce_ms = h->b.reduce_ms;
+  out->gpu_launches = h->b.launches;
+  return SVDAG_OK;
+}
+
+}  // extern "C"

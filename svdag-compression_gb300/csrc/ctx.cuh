@@ -2,6 +2,7 @@
 // C ABI (api.cu) dispatches to.
 #pragma once
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -63,8 +64,49 @@ void phase_cross_level_merge(Ctx& c);
 // toDAG with every temporary in caller-provided device scratch (no allocation).
 void phase_reduce_dag_scratch(Ctx& c, uint8_t* scratch, uint64_t capacity);
 
+// Voxel-brick chunks (batch.cu).
+float synth_noise_bricks(cudaStream_t st, uint32_t depth, uint64_t seed, double fill, uint8_t* out);
+void phase_import_bricks(Ctx& c, uint32_t depth, const uint8_t* bricks);
+
 }  // namespace svdag
 
 struct svdag_ctx {
   svdag::Ctx c;
+};
+
+namespace svdag {
+
+struct BatchChunk {
+  uint32_t depth;
+  const uint8_t* bricks;  // device, borrowed
+};
+struct BatchResult {
+  std::unique_ptr<svdag_ctx> dag, sdag, csv;
+};
+struct BatchTuning {
+  double table_factor = 2.0;  // hash slots per cell of a height (power of two above)
+  unsigned threads = 256;     // block size of the per-height kernels
+  int streams = 4;            // concurrent per-chunk reductions
+};
+struct Batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  Exec ex;
+  uint64_t launches = 0;
+  std::vector<BatchChunk> chunks;
+  std::vector<BatchResult> results;
+  BatchTuning tuning;
+  std::vector<uint64_t> worker_launches;
+  std::vector<cudaStream_t> streams;
+  std::string last_error;
+  double dag_ms = 0, reduce_ms = 0;
+};
+void batch_build_dags(Batch& B);
+void batch_reduce(Batch& B, bool sdag, bool csv);
+
+}  // namespace svdag
+
+struct svdag_batch {
+  svdag::Batch b;
 };

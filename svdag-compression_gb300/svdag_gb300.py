@@ -77,7 +77,29 @@ GPU_SYMBOLS = {
     "svdag_profile_enable": (_I, [_VP, _I]),
     "svdag_profile_report": (_I, [_VP, ctypes.c_char_p, _U64]),
     "svdag_reduce_dag_noalloc": (_I, [_VP]),
+    "svdag_synth_noise_bricks": (_I, [_VP, _U32, _U64, ctypes.c_double, _VP, ctypes.POINTER(ctypes.c_float)]),
+    "svdag_import_bricks": (_I, [_VP, _U32, _VP]),
+    "svdag_batch_create": (_I, [ctypes.POINTER(_VP), _I, _VP]),
+    "svdag_batch_destroy": (_I, [_VP]),
+    "svdag_batch_last_error": (ctypes.c_char_p, [_VP]),
+    "svdag_batch_clear": (_I, [_VP]),
+    "svdag_batch_add_chunk": (_I, [_VP, _U32, _VP]),
+    "svdag_batch_chunk_count": (_I, [_VP, ctypes.POINTER(_U32)]),
+    "svdag_batch_build": (_I, [_VP, _U32]),
+    "svdag_batch_result": (_I, [_VP, _U32, _U32, ctypes.POINTER(_VP)]),
+    "svdag_batch_set_tuning": (_I, [_VP, _VP]),
+    "svdag_batch_get_tuning": (_I, [_VP, _VP]),
+    "svdag_batch_autotune": (_I, [_VP, _U32, _U32]),
+    "svdag_batch_get_stats": (_I, [_VP, _VP]),
 }
+
+
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("table_factor", ctypes.c_double), ("threads", ctypes.c_uint32), ("streams", ctypes.c_uint32)]
+
+
+class _BatchStats(ctypes.Structure):
+    _fields_ = [("dag_ms", ctypes.c_double), ("reduce_ms", ctypes.c_double), ("gpu_launches", ctypes.c_uint64)]
 
 HOST_SYMBOLS = {
     "svdag_synth_icosphere_count": (_U64, [_U32]),
@@ -216,8 +238,9 @@ def write_encoded(path, fmt, pool, n_nodes, state, bbox=UNIT_BOX, root_side=1.0)
 class Octree:
     """GPU octree with the GeomOctree build surface."""
 
-    def __init__(self, device=0, stream=None, _handle=None):
+    def __init__(self, device=0, stream=None, _handle=None, _owner=None):
         self._lib = load_gpu()
+        self._owner = _owner  # a Batch whose result view this is (not destroyed here)
         if _handle is not None:
             self._h = _handle
         else:
@@ -234,7 +257,8 @@ class Octree:
 
     def close(self):
         if getattr(self, "_h", None):
-            self._lib.svdag_destroy(self._h)
+            if getattr(self, "_owner", None) is None:
+                self._lib.svdag_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -268,6 +292,11 @@ class Octree:
         """GeomOctree::buildDAG: chunked build, DAG state, reference node order."""
         bb = (ctypes.c_double * 6)(*bbox)
         self._check(self._lib.svdag_build_dag(self._h, levels, step_level, bb))
+
+    def import_bricks(self, depth, bricks):
+        """Node pools of a voxel-brick chunk (a torch uint8 CUDA tensor of
+        8^(depth-1) Morton-ordered bricks), DAG state."""
+        self._check(self._lib.svdag_import_bricks(self._h, depth, ctypes.c_void_p(bricks.data_ptr())))
 
     def toDAG(self):
         self._check(self._lib.svdag_reduce_dag(self._h))
@@ -354,3 +383,86 @@ class Octree:
 
     def handle(self):
         return self._h.value
+
+
+# --------------------------------------------------------------------------
+# voxel-brick chunks
+
+def noise_bricks(depth, seed, fill, device=0):
+    """Seeded synthetic chunk: a torch uint8 CUDA tensor of 8^(depth-1)
+    Morton-ordered bricks with about `fill` of the voxels set."""
+    import torch
+
+    t = torch.empty(8 ** (depth - 1), dtype=torch.uint8, device="cuda:%d" % device)
+    lib = load_gpu()
+    thr = ctypes.c_float()
+    st = torch.cuda.current_stream(device).cuda_stream
+    r = lib.svdag_synth_noise_bricks(ctypes.c_void_p(st), depth, seed, fill, ctypes.c_void_p(t.data_ptr()),
+                                     ctypes.byref(thr))
+    if r != 0:
+        raise SvdagError(r, "noise bricks failed")
+    torch.cuda.synchronize(device)
+    return t
+
+
+class Batch:
+    """Batched build of voxel-brick chunks (svdag_batch_*)."""
+
+    RESULT = {"dag": 0, "sdag": 1, "csvdag": 2}
+
+    def __init__(self, device=0, stream=None):
+        self._lib = load_gpu()
+        h = ctypes.c_void_p()
+        r = self._lib.svdag_batch_create(ctypes.byref(h), device, stream)
+        if r != 0:
+            raise SvdagError(r, "batch create failed")
+        self._h = h
+        self._keep = []
+
+    def _check(self, status):
+        if status != 0:
+            raise SvdagError(status, self._lib.svdag_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.svdag_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_chunk(self, depth, bricks):
+        self._check(self._lib.svdag_batch_add_chunk(self._h, depth, ctypes.c_void_p(bricks.data_ptr())))
+        self._keep.append(bricks)
+
+    def clear(self):
+        self._check(self._lib.svdag_batch_clear(self._h))
+        self._keep = []
+
+    def build(self, sdag=True, csvdag=True):
+        self._check(self._lib.svdag_batch_build(self._h, (1 if sdag else 0) | (2 if csvdag else 0)))
+
+    def result(self, chunk, kind="dag"):
+        v = ctypes.c_void_p()
+        self._check(self._lib.svdag_batch_result(self._h, chunk, self.RESULT[kind], ctypes.byref(v)))
+        return Octree(_handle=v, _owner=self)
+
+    def tuning(self):
+        t = BatchTuning()
+        self._check(self._lib.svdag_batch_get_tuning(self._h, ctypes.byref(t)))
+        return {"table_factor": t.table_factor, "threads": t.threads, "streams": t.streams}
+
+    def set_tuning(self, table_factor=2.0, threads=256, streams=4):
+        t = BatchTuning(table_factor, threads, streams)
+        self._check(self._lib.svdag_batch_set_tuning(self._h, ctypes.byref(t)))
+
+    def autotune(self, sdag=True, csvdag=True, max_trials=12):
+        self._check(self._lib.svdag_batch_autotune(self._h, (1 if sdag else 0) | (2 if csvdag else 0), max_trials))
+
+    def stats(self):
+        s = _BatchStats()
+        self._check(self._lib.svdag_batch_get_stats(self._h, ctypes.byref(s)))
+        return {"dag_ms": s.dag_ms, "reduce_ms": s.reduce_ms, "gpu_launches": s.gpu_launches}
