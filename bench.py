@@ -40,9 +40,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["terrain", "city"], default="terrain",
+    ap.add_argument("--workload", choices=["terrain", "city", "batch"], default="terrain",
                     help="terrain: 2048^2 fBm terrain at depth 12 (the headline); city: 4096^2 terrain + 200,000 "
-                         "boxes at depth 15, chunked build with step level 1")
+                         "boxes at depth 15, chunked build with step level 1; batch: 256 voxel-brick chunks of "
+                         "depths 7-11 (value noise, 5-40%% fill), batched SSVDAG + CSVDAG")
+    ap.add_argument("--chunks", type=int, default=256)
+    ap.add_argument("--max-depth", type=int, default=11)
     ap.add_argument("--grid", type=int, default=None)
     ap.add_argument("--levels", type=int, default=None)
     ap.add_argument("--step-level", type=int, default=None, help="buildDAG step level (0 = buildSVO + toDAG)")
@@ -532,9 +535,95 @@ def run_reference(args, rank, world):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_batch(args, rank, local, world):
+    """Voxel-brick chunks: the batched build (svdag_batch_*) timed over K
+    steps, the plain per-chunk form timed once over the same chunks."""
+    import numpy as np
+    import torch
+
+    import svdag_gb300 as sv
+
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(args.seed)
+    depths = rng.integers(7, args.max_depth + 1, size=args.chunks)
+    fills = rng.uniform(0.05, 0.40, size=args.chunks)
+    bricks = [sv.noise_bricks(int(d), int(args.seed) * 100003 + i, float(f), local)
+              for i, (d, f) in enumerate(zip(depths, fills))]
+    in_bytes = sum(b.numel() for b in bricks)
+    B = sv.Batch(device=local)
+    # settings: autotuned on a sample of the chunks (every 8th), untimed
+    T = sv.Batch(device=local)
+    for i in range(0, args.chunks, 8):
+        T.add_chunk(int(depths[i]), bricks[i])
+    T.autotune(max_trials=10)
+    tune = T.tuning()
+    T.close()
+    B.set_tuning(**tune)
+    for d, b in zip(depths, bricks):
+        B.add_chunk(int(d), b)
+    for _ in range(max(args.warmup, 0)):
+        B.build()
+    voxels = sum(B.result(i, "dag").stats()["n_total_voxels"] for i in range(args.chunks))
+    launches0 = B.stats()["gpu_launches"]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    clocks.mark()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    stage = {"dag_ms": 0.0, "reduce_ms": 0.0}
+    for _ in range(args.steps):
+        B.build()
+        st = B.stats()
+        stage["dag_ms"] += st["dag_ms"]
+        stage["reduce_ms"] += st["reduce_ms"]
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    clk = clocks.stop()
+    launches = (B.stats()["gpu_launches"] - launches0) // max(args.steps, 1)
+    nodes = [sum(B.result(i, k).stats()["n_nodes"] for i in range(args.chunks)) for k in ("dag", "sdag", "csvdag")]
+    B.close()
+    # plain per-chunk form over the same chunks, once
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for d, b in zip(depths, bricks):
+        o = sv.Octree(device=local)
+        o.import_bricks(int(d), b)
+        o.toDAG()
+        s_ = o.clone()
+        s_.toSDAG()
+        c_ = o.clone()
+        c_.initChildLevels()
+        c_.mergeAcrossAllLevels()
+        for x in (o, s_, c_):
+            x.close()
+    torch.cuda.synchronize()
+    plain_ms = (time.perf_counter() - t0) * 1e3
+    return {
+        "metric": METRIC, "value": voxels / (ms / 1e3) / 1e6, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8 bricks + u32 keys", "data": "synthetic",
+        "config": {"workload": "batch: %d voxel-brick chunks, depths uniform %d-%d, 3D value noise (period 16 "
+                               "voxels) at fills uniform 5-40%%, batched toDAG + per-chunk SSVDAG + CSVDAG"
+                               % (args.chunks, 7, args.max_depth),
+                   "chunks": args.chunks, "voxels": int(voxels), "input_bytes": int(in_bytes),
+                   "nodes_dag": int(nodes[0]), "nodes_sdag": int(nodes[1]), "nodes_csvdag": int(nodes[2]),
+                   "chunks_per_s": args.chunks / (ms / 1e3), "plain_chunks_per_s": args.chunks / (plain_ms / 1e3),
+                   "speedup_vs_plain": plain_ms / ms, "stage_ms_per_step": {k: v / args.steps for k, v in stage.items()},
+                   "tuning": tune, "l2": "inputs larger than L2 (%d MB of bricks)" % (in_bytes // 10**6),
+                   "parallelism": "single GPU"},
+        "clocks": clk, "gpu_launches": int(launches), "e2e": None,
+    }
+
+
 def main():
     args = parse()
     rank, local, world = rank_info()
+    if args.workload == "batch" and args.impl != "reference":
+        res = run_batch(args, rank, local, world)
+        if rank == 0:
+            print(json.dumps(res))
+        return
     if args.impl == "reference":
         res = run_reference(args, rank, world)
         if res is not None:

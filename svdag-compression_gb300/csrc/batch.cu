@@ -443,20 +443,23 @@ void phase_import_bricks(Ctx& c, uint32_t depth, const uint8_t* bricks) {
 }
 
 // ---------------------------------------------------------------------------
-void batch_build_dags(Batch& B) {
+namespace {
+
+// One wave of chunks (sel = their indices in B.chunks), all heights.
+void build_wave(Batch& B, const std::vector<uint32_t>& sel) {
   const Exec& ex = B.ex;
   const cudaStream_t st = B.stream;
-  const uint32_t N = uint32_t(B.chunks.size());
-  B.results.clear();
-  B.results.resize(N);
+  const uint32_t N = uint32_t(sel.size());
   if (!N) return;
+  auto CH = [&](uint32_t c) -> const BatchChunk& { return B.chunks[sel[c]]; };
+  auto RES = [&](uint32_t c) -> BatchResult& { return B.results[sel[c]]; };
   uint32_t maxd = 0;
-  for (auto& ch : B.chunks) maxd = std::max(maxd, ch.depth);
+  for (uint32_t c = 0; c < N; ++c) maxd = std::max(maxd, CH(c).depth);
 
   // --- leaf height: per-chunk first occurrence of every mask
   std::vector<const uint8_t*> hb(N);
   std::vector<uint64_t> hn(N);
-  for (uint32_t c = 0; c < N; ++c) { hb[c] = B.chunks[c].bricks; hn[c] = 1ull << (3 * (B.chunks[c].depth - 1)); }
+  for (uint32_t c = 0; c < N; ++c) { hb[c] = CH(c).bricks; hn[c] = 1ull << (3 * (CH(c).depth - 1)); }
   DBuf<const uint8_t*> d_bricks(N, st);
   DBuf<uint64_t> d_nb(N, st);
   DBuf<uint32_t> first(256ull * N, st), rank(256ull * N, st), leaf_hdr(256ull * N, st), leaf_cnt(N, st);
@@ -480,8 +483,8 @@ void batch_build_dags(Batch& B) {
   SVDAG_CUDA(cudaMemcpyAsync(h_vox.data(), vox.get(), 8ull * N, cudaMemcpyDeviceToHost, st));
   SVDAG_CUDA(cudaStreamSynchronize(st));
   for (uint32_t c = 0; c < N; ++c) {
-    BatchResult& R = B.results[c];
-    const uint32_t d = B.chunks[c].depth;
+    BatchResult& R = RES(c);
+    const uint32_t d = CH(c).depth;
     R.dag.reset(new svdag_ctx());
     Ctx& X = R.dag->c;
     X.device = B.device;
@@ -515,15 +518,15 @@ void batch_build_dags(Batch& B) {
     std::vector<uint32_t> order(N);
     for (uint32_t c = 0; c < N; ++c) order[c] = c;
     std::stable_sort(order.begin(), order.end(),
-                     [&](uint32_t a, uint32_t b) { return B.chunks[a].depth > B.chunks[b].depth; });
+                     [&](uint32_t a, uint32_t b) { return CH(a).depth > CH(b).depth; });
     for (uint32_t c : order) {
-      const uint32_t d = B.chunks[c].depth;
+      const uint32_t d = CH(c).depth;
       if (d <= h) continue;
       const uint32_t l = d - 1 - h;
       part.push_back(c);
       base.push_back(base.back() + (1ull << (3 * l)));
       top.push_back(l == 0 ? 1 : 0);
-      pb.push_back(B.chunks[c].bricks);
+      pb.push_back(CH(c).bricks);
       if (h >= 2) {
         const size_t k = size_t(std::find(below_part.begin(), below_part.end(), c) - below_part.begin());
         bb.push_back(below_base_h[k]);
@@ -584,8 +587,8 @@ void batch_build_dags(Batch& B) {
     // hand each entry its level
     for (uint32_t e = 0; e < n; ++e) {
       const uint32_t c = part[e];
-      Ctx& X = B.results[c].dag->c;
-      Level& L = X.lev[B.chunks[c].depth - 1 - h];
+      Ctx& X = RES(c).dag->c;
+      Level& L = X.lev[CH(c).depth - 1 - h];
       L.n = rep_base[e + 1] - rep_base[e];
       L.hdr.alloc(L.n ? L.n : 1, st);
       L.ch.alloc(8 * (L.n ? L.n : 1), st);
@@ -600,12 +603,35 @@ void batch_build_dags(Batch& B) {
   }
   check_err(ex, d_err.get(), "batch toDAG");
   for (uint32_t c = 0; c < N; ++c) {
-    Ctx& X = B.results[c].dag->c;
+    Ctx& X = RES(c).dag->c;
     uint64_t nodes = 0;
     for (auto& L : X.lev) nodes += L.n;
     X.st.n_nodes = nodes;
     X.st.n_nodes_dag = nodes;
   }
+}
+
+}  // namespace
+
+// All chunks, in waves of at most 2^30 cells one height above the leaves
+// (bounds the per-height tables and index arrays to a few tens of GB).
+void batch_build_dags(Batch& B) {
+  const uint32_t N = uint32_t(B.chunks.size());
+  B.results.clear();
+  B.results.resize(N);
+  std::vector<uint32_t> sel;
+  uint64_t cells = 0;
+  for (uint32_t c = 0; c < N; ++c) {
+    const uint64_t k = 1ull << (3 * (B.chunks[c].depth - 2));
+    if (!sel.empty() && cells + k > (1ull << 30)) {
+      build_wave(B, sel);
+      sel.clear();
+      cells = 0;
+    }
+    sel.push_back(c);
+    cells += k;
+  }
+  build_wave(B, sel);
 }
 
 // SSVDAG and CSVDAG of every chunk's DAG, on B.tuning.streams streams.
