@@ -196,6 +196,54 @@ int svdag_batch_get_tuning(const svdag_batch* batch, svdag_batch_tuning* tuning)
 int svdag_batch_autotune(svdag_batch* batch, uint32_t flags, uint32_t max_trials);
 int svdag_batch_get_stats(const svdag_batch* batch, svdag_batch_stats* out);
 
+/* ---- Lossy LSVDAG (project-defined; the reference's toLossyDag,
+ * src/symvox/geom_octree_extension.cpp:797-1179, clusters with the external
+ * MCL binary, which is not available, and its candidate order depends on
+ * OpenMP scheduling).  On a DAG: candidates are the referenced nodes of
+ * levels L-1-levels_above_max .. L-1-levels_above_min (top-down) outside
+ * subtrees already kept as merge targets; a merge i -> j is allowed when the
+ * exact voxel Hamming distance of the two subtrees is at most
+ * floor(max_error * 8^(L-level)), the voxels of the subtree's cube; each candidate joins the
+ * lowest-index leader among its allowed partners below it, else leads;
+ * unreachable nodes are then dropped and toDAG merges new duplicates.  The
+ * proposer picks which pairs get the exact check: all pairs whose voxel
+ * counts permit the bound (SVDAG_LOSSY_EXACT), the top_k partners by the
+ * distance of embeddings from an MLP trained on the GPU on train_pairs exact
+ * distances of the scene (SVDAG_LOSSY_LEARNED), or the same network left
+ * untrained (SVDAG_LOSSY_UNTRAINED, for comparison).  Every accepted merge
+ * is checked exactly, whatever the proposer. */
+enum { SVDAG_LOSSY_EXACT = 0, SVDAG_LOSSY_LEARNED = 1, SVDAG_LOSSY_UNTRAINED = 2 };
+typedef struct svdag_lossy_params {
+  uint32_t levels_above_min; /* 3 */
+  uint32_t levels_above_max; /* 5 */
+  double max_error;          /* 0.01 */
+  uint32_t proposer;
+  uint32_t top_k;            /* learned: proposals per candidate (0 = 16) */
+  uint64_t train_pairs;      /* learned: training pairs (0 = 2,000,000) */
+  uint32_t train_epochs;     /* learned: passes over them (0 = 2) */
+  uint64_t seed;
+} svdag_lossy_params;
+typedef struct svdag_lossy_stats {
+  uint64_t nodes_before, nodes_after, candidates, pairs_evaluated, edges, merged;
+  double ms, propose_ms, train_ms;
+  float final_loss;
+} svdag_lossy_stats;
+int svdag_lossy_dag(svdag_ctx* ctx, const svdag_lossy_params* params, svdag_lossy_stats* out);
+
+/* The proposer's network on host buffers (512 -> 256 -> 256 -> 64, ReLU;
+ * parameters W1[512x256], b1, W2[256x256], b2, W3[256x64], b3 row-major,
+ * concatenated).  loss_grad: siamese loss mean(|f(a) - f(b)|^2 - t)^2 over n
+ * pairs and the gradient of every parameter. */
+typedef struct svdag_mlp svdag_mlp;
+int svdag_mlp_create(svdag_mlp** out, int device, uint64_t seed);
+int svdag_mlp_destroy(svdag_mlp* mlp);
+uint64_t svdag_mlp_param_count(void);
+int svdag_mlp_get_params(svdag_mlp* mlp, float* host_params);
+int svdag_mlp_set_params(svdag_mlp* mlp, const float* host_params);
+int svdag_mlp_loss_grad(svdag_mlp* mlp, const float* x_a, const float* x_b, const float* t, uint32_t n, float* loss,
+                        float* grads);
+int svdag_mlp_embed(svdag_mlp* mlp, const float* x, uint32_t n, float* out);
+
 /* toDAG without allocating (no counterpart in the reference, whose toDAG,
  * src/symvox/geom_octree.cpp:462-548, works in host containers).
  *

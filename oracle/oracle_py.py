@@ -36,6 +36,7 @@ _SIGS = {
     "ora_build_svo": (_I, [_VP, _VP, _U64, _VP, _U32]),
     "ora_build_dag_chunked": (_I, [_VP, _VP, _U64, _VP, _U32, _U32, _I]),
     "ora_build_from_bricks": (_I, [_VP, _U32, _VP]),
+    "ora_lossy_exact": (_I, [_VP, _U32, _U32, ctypes.c_double, ctypes.POINTER(_U64)]),
     "ora_to_dag": (_I, [_VP]),
     "ora_to_sdag": (_I, [_VP]),
     "ora_init_child_levels": (_I, [_VP]),
@@ -95,6 +96,12 @@ class OracleOctree:
         bricks = np.ascontiguousarray(bricks, np.uint8)
         assert bricks.size == 8 ** (depth - 1)
         assert self.L.ora_build_from_bricks(self.h, depth, bricks.ctypes.data) == 0
+
+    def lossyExact(self, min_above=3, max_above=5, max_error=0.01):
+        """Lossy LSVDAG, exact-proposer form; returns the number of merged nodes."""
+        m = ctypes.c_uint64()
+        assert self.L.ora_lossy_exact(self.h, min_above, max_above, max_error, ctypes.byref(m)) == 0
+        return m.value
 
     def toDAG(self):
         assert self.L.ora_to_dag(self.h) == 0

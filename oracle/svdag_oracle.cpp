@@ -662,6 +662,132 @@ int ora_build_from_bricks(ora_octree* o, uint32_t depth, const uint8_t* bricks) 
   return 0;
 }
 
+// Lossy LSVDAG, the exact-proposer form of the GPU path (its definition is
+// project-defined: the reference's toLossyDag, geom_octree_extension.cpp:
+// 797-1179, needs the external MCL binary).  Levels L-1-max_above ..
+// L-1-min_above top-down; candidates = reachable, not frozen; leaf bytes of
+// each candidate's subtree in Morton order; an edge (a < b) when the XOR
+// popcount is <= floor(max_err * 8^(L-lev)); leader rule in candidate
+// order; parents redirected to leaders; leaders' subtrees frozen; finally
+// unreachable nodes dropped and toDAG.
+namespace {
+void subtree_bytes(const ora_octree* o, uint32_t lev, uint32_t node, uint32_t k, uint64_t base, uint8_t* out) {
+  if (k == 0) {
+    out[base] = o->d[lev][node].mask;
+    return;
+  }
+  const Node& n = o->d[lev][node];
+  for (int d = 0; d < 8; ++d)
+    if (n.has_child(d)) subtree_bytes(o, lev + 1, n.ch[d], k - 1, (base << 3) | uint64_t(d), out);
+}
+std::vector<std::vector<char>> reachable(const ora_octree* o) {
+  std::vector<std::vector<char>> r(o->levels);
+  for (uint32_t l = 0; l < o->levels; ++l) r[l].assign(o->d[l].size(), 0);
+  if (!o->d[0].empty()) r[0][0] = 1;
+  for (uint32_t l = 0; l + 1 < o->levels; ++l)
+    for (size_t i = 0; i < o->d[l].size(); ++i)
+      if (r[l][i])
+        for (int c = 0; c < 8; ++c)
+          if (o->d[l][i].has_child(c)) r[l + 1][o->d[l][i].ch[c]] = 1;
+  return r;
+}
+}  // namespace
+
+int ora_lossy_exact(ora_octree* o, uint32_t min_above, uint32_t max_above, double max_err, uint64_t* merged) {
+  if (!o || o->state != 2 || min_above > max_above) return -1;
+  const uint32_t L = o->levels;
+  std::vector<std::vector<char>> frozen(L);
+  for (uint32_t l = 0; l < L; ++l) frozen[l].assign(o->d[l].size(), 0);
+  uint64_t nmerged = 0;
+  for (uint32_t a = max_above + 1; a-- > min_above;) {
+    if (a + 1 >= L) continue;
+    const uint32_t lev = L - 1 - a;
+    auto reach = reachable(o);
+    std::vector<uint32_t> cand;
+    for (uint32_t i = 0; i < o->d[lev].size(); ++i)
+      if (reach[lev][i] && !frozen[lev][i]) cand.push_back(i);
+    const uint32_t n = uint32_t(cand.size());
+    if (n < 2) continue;
+    const uint32_t k = L - 1 - lev;
+    const uint64_t per = 1ull << (3 * k);
+    std::vector<uint8_t> bytes(per * n, 0);
+    std::vector<uint32_t> pop(n, 0);
+    for (uint32_t c = 0; c < n; ++c) {
+      const Node& nd = o->d[lev][cand[c]];
+      uint8_t* out = bytes.data() + per * c;
+      for (int d = 0; d < 8; ++d)
+        if (nd.has_child(d)) subtree_bytes(o, lev + 1, nd.ch[d], k - 1, uint64_t(d), out);
+      for (uint64_t s = 0; s < per; ++s) pop[c] += popc8(out[s]);
+    }
+    const uint32_t lim = uint32_t(max_err * double(1ull << (3 * (L - lev))));
+    std::vector<std::vector<uint32_t>> below(n);
+    for (uint32_t b = 0; b < n; ++b)
+      for (uint32_t a2 = 0; a2 < b; ++a2) {
+        const uint32_t gap = pop[a2] > pop[b] ? pop[a2] - pop[b] : pop[b] - pop[a2];
+        if (gap > lim) continue;
+        uint32_t dist = 0;
+        const uint8_t* x = bytes.data() + per * a2;
+        const uint8_t* y = bytes.data() + per * b;
+        for (uint64_t s = 0; s < per && dist <= lim; ++s) dist += popc8(uint8_t(x[s] ^ y[s]));
+        if (dist <= lim) below[b].push_back(a2);
+      }
+    const uint32_t kLeadO = 0xFFFFFFFEu;
+    std::vector<uint32_t> state(n, 0xFFFFFFFFu);
+    for (uint32_t i = 0; i < n; ++i) {
+      uint32_t r = kLeadO;
+      for (uint32_t j : below[i])
+        if (state[j] == kLeadO) { r = j; break; }
+      state[i] = r;
+    }
+    std::vector<uint32_t> node_to(o->d[lev].size(), 0xFFFFFFFFu);
+    std::vector<char> lead(o->d[lev].size(), 0);
+    for (uint32_t i = 0; i < n; ++i) {
+      if (state[i] == kLeadO) lead[cand[i]] = 1;
+      else { node_to[cand[i]] = cand[state[i]]; ++nmerged; }
+    }
+    for (auto& p : o->d[lev - 1])
+      for (int c = 0; c < 8; ++c)
+        if (p.has_child(c) && node_to[p.ch[c]] != 0xFFFFFFFFu) p.ch[c] = node_to[p.ch[c]];
+    for (size_t i = 0; i < o->d[lev].size(); ++i)
+      if (lead[i])
+        for (int c = 0; c < 8; ++c)
+          if (o->d[lev][i].has_child(c)) frozen[lev + 1][o->d[lev][i].ch[c]] = 1;
+    for (uint32_t l = lev + 1; l + 1 < L; ++l)
+      for (size_t i = 0; i < o->d[l].size(); ++i)
+        if (frozen[l][i])
+          for (int c = 0; c < 8; ++c)
+            if (o->d[l][i].has_child(c)) frozen[l + 1][o->d[l][i].ch[c]] = 1;
+  }
+  // drop unreachable nodes, renumber
+  auto reach = reachable(o);
+  std::vector<std::vector<uint32_t>> nid(L);
+  for (uint32_t l = 0; l < L; ++l) {
+    nid[l].assign(o->d[l].size(), 0xFFFFFFFFu);
+    uint32_t c = 0;
+    for (size_t i = 0; i < o->d[l].size(); ++i)
+      if (reach[l][i]) nid[l][i] = c++;
+  }
+  for (uint32_t l = 0; l < L; ++l) {
+    std::vector<Node> keep;
+    for (size_t i = 0; i < o->d[l].size(); ++i) {
+      if (!reach[l][i]) continue;
+      Node nd = o->d[l][i];
+      for (int c = 0; c < 8; ++c) {
+        if (l + 1 < L && nd.has_child(c)) nd.ch[c] = nid[l + 1][nd.ch[c]];
+        else nd.ch[c] = kNull;
+        nd.clev[c] = 0xFFFFFFFFu;
+      }
+      nd.inv = 0;
+      keep.push_back(nd);
+    }
+    o->d[l].swap(keep);
+  }
+  o->state = 2;
+  to_dag(o);
+  if (merged) *merged = nmerged;
+  return 0;
+}
+
 int ora_to_dag(ora_octree* o) { return o ? to_dag(o) : -1; }
 int ora_to_sdag(ora_octree* o) { return o ? to_sdag(o) : -1; }
 int ora_init_child_levels(ora_octree* o) {

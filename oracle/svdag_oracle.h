@@ -40,6 +40,8 @@ int ora_build_dag_chunked(ora_octree* o, const float* tris, uint64_t n_tris, con
 /* voxel bricks (8^(depth-1) masks, Morton order) -> node pools in the DAG
  * state, the GeomOctree(NodeData, ...) route (geom_octree.cpp:49-60) */
 int ora_build_from_bricks(ora_octree* o, uint32_t depth, const uint8_t* bricks);
+/* lossy LSVDAG, exact-proposer form (project-defined; see the .cpp) */
+int ora_lossy_exact(ora_octree* o, uint32_t min_above, uint32_t max_above, double max_err, uint64_t* merged);
 int ora_to_dag(ora_octree* o);                 /* geom_octree.cpp:462-548 */
 int ora_to_sdag(ora_octree* o);                /* geom_octree.cpp:551-697 (greedy, symmetry on) */
 int ora_init_child_levels(ora_octree* o);      /* geom_octree_extension.cpp:21-30 */

@@ -91,7 +91,28 @@ GPU_SYMBOLS = {
     "svdag_batch_get_tuning": (_I, [_VP, _VP]),
     "svdag_batch_autotune": (_I, [_VP, _U32, _U32]),
     "svdag_batch_get_stats": (_I, [_VP, _VP]),
+    "svdag_lossy_dag": (_I, [_VP, _VP, _VP]),
+    "svdag_mlp_create": (_I, [ctypes.POINTER(_VP), _I, _U64]),
+    "svdag_mlp_destroy": (_I, [_VP]),
+    "svdag_mlp_param_count": (_U64, []),
+    "svdag_mlp_get_params": (_I, [_VP, _VP]),
+    "svdag_mlp_set_params": (_I, [_VP, _VP]),
+    "svdag_mlp_loss_grad": (_I, [_VP, _VP, _VP, _VP, _U32, _VP, _VP]),
+    "svdag_mlp_embed": (_I, [_VP, _VP, _U32, _VP]),
 }
+
+
+class LossyParams(ctypes.Structure):
+    _fields_ = [("levels_above_min", ctypes.c_uint32), ("levels_above_max", ctypes.c_uint32),
+                ("max_error", ctypes.c_double), ("proposer", ctypes.c_uint32), ("top_k", ctypes.c_uint32),
+                ("train_pairs", ctypes.c_uint64), ("train_epochs", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
+
+
+class _LossyStats(ctypes.Structure):
+    _fields_ = [("nodes_before", ctypes.c_uint64), ("nodes_after", ctypes.c_uint64), ("candidates", ctypes.c_uint64),
+                ("pairs_evaluated", ctypes.c_uint64), ("edges", ctypes.c_uint64), ("merged", ctypes.c_uint64),
+                ("ms", ctypes.c_double), ("propose_ms", ctypes.c_double), ("train_ms", ctypes.c_double),
+                ("final_loss", ctypes.c_float)]
 
 
 class BatchTuning(ctypes.Structure):
@@ -301,6 +322,16 @@ class Octree:
     def toDAG(self):
         self._check(self._lib.svdag_reduce_dag(self._h))
 
+    LOSSY = {"exact": 0, "learned": 1, "untrained": 2}
+
+    def lossy(self, proposer="exact", min_above=3, max_above=5, max_error=0.01, top_k=16, train_pairs=0,
+              epochs=0, seed=1):
+        """Lossy LSVDAG on a DAG (svdag_lossy_dag); returns its statistics."""
+        p = LossyParams(min_above, max_above, max_error, self.LOSSY[proposer], top_k, train_pairs, epochs, seed)
+        s = _LossyStats()
+        self._check(self._lib.svdag_lossy_dag(self._h, ctypes.byref(p), ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in _LossyStats._fields_}
+
     def toDAG_noalloc(self):
         """toDAG with the library's static device scratch (no allocation);
         raises SvdagError (SVDAG_ERR_OVERFLOW) when a level does not fit."""
@@ -466,3 +497,56 @@ class Batch:
         s = _BatchStats()
         self._check(self._lib.svdag_batch_get_stats(self._h, ctypes.byref(s)))
         return {"dag_ms": s.dag_ms, "reduce_ms": s.reduce_ms, "gpu_launches": s.gpu_launches}
+
+
+class Mlp:
+    """The lossy proposer's network on host buffers (svdag_mlp_*)."""
+
+    def __init__(self, seed=1, device=0):
+        self._lib = load_gpu()
+        h = ctypes.c_void_p()
+        r = self._lib.svdag_mlp_create(ctypes.byref(h), device, seed)
+        if r != 0:
+            raise SvdagError(r, "mlp create failed")
+        self._h = h
+        self.n_params = int(self._lib.svdag_mlp_param_count())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.svdag_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        out = np.empty(self.n_params, np.float32)
+        assert self._lib.svdag_mlp_get_params(self._h, out.ctypes.data) == 0
+        return out
+
+    def set_params(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        assert self._lib.svdag_mlp_set_params(self._h, w.ctypes.data) == 0
+
+    def loss_grad(self, xa, xb, t):
+        xa = np.ascontiguousarray(xa, np.float32)
+        xb = np.ascontiguousarray(xb, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        loss = ctypes.c_float()
+        g = np.empty(self.n_params, np.float32)
+        r = self._lib.svdag_mlp_loss_grad(self._h, xa.ctypes.data, xb.ctypes.data, t.ctypes.data, t.shape[0],
+                                          ctypes.byref(loss), g.ctypes.data)
+        if r != 0:
+            raise SvdagError(r, "mlp loss_grad failed")
+        return loss.value, g
+
+    def embed(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        out = np.empty((x.shape[0], 64), np.float32)
+        r = self._lib.svdag_mlp_embed(self._h, x.ctypes.data, x.shape[0], out.ctypes.data)
+        if r != 0:
+            raise SvdagError(r, "mlp embed failed")
+        return out
