@@ -40,10 +40,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["terrain", "city", "batch"], default="terrain",
+    ap.add_argument("--workload", choices=["terrain", "city", "batch", "lossy"], default="terrain",
                     help="terrain: 2048^2 fBm terrain at depth 12 (the headline); city: 4096^2 terrain + 200,000 "
                          "boxes at depth 15, chunked build with step level 1; batch: 256 voxel-brick chunks of "
-                         "depths 7-11 (value noise, 5-40%% fill), batched SSVDAG + CSVDAG")
+                         "depths 7-11 (value noise, 5-40%% fill), batched SSVDAG + CSVDAG; lossy: 2048^2 terrain + "
+                         "5,000 boxes at depth 11, lossy LSVDAG with exact and learned pair proposals")
+    ap.add_argument("--top-k", type=int, default=16)
+    ap.add_argument("--train-pairs", type=int, default=2000000)
+    ap.add_argument("--epochs", type=int, default=2)
     ap.add_argument("--chunks", type=int, default=256)
     ap.add_argument("--max-depth", type=int, default=11)
     ap.add_argument("--grid", type=int, default=None)
@@ -59,7 +63,7 @@ def parse():
     if a.grid is None:
         a.grid = 4096 if city else 2048
     if a.levels is None:
-        a.levels = 15 if city else 12
+        a.levels = 15 if city else (11 if a.workload == "lossy" else 12)
     if a.step_level is None:
         a.step_level = 1 if city else 0
     if a.seed is None:
@@ -616,11 +620,72 @@ def run_batch(args, rank, local, world):
     }
 
 
+def run_lossy(args, rank, local, world):
+    """Lossy LSVDAG on the DAG of the 2048^2 terrain + 5,000 boxes at depth
+    11: the exact proposer and the learned one (training included), each
+    timed over K runs on fresh copies of the DAG."""
+    import numpy as np
+    import torch
+
+    import svdag_gb300 as sv
+
+    torch.cuda.set_device(local)
+    L = args.levels
+    rng = np.random.default_rng(args.seed)
+    res_ = 1 << L
+    lo = rng.integers(0, res_ - 64, size=(5000, 3))
+    side = rng.integers(1, 65, size=(5000, 3))
+    hi = np.minimum(lo + side, res_)
+    tris = np.concatenate([sv.terrain(args.grid, 8, 0.3, args.seed), sv.boxes((lo + 0.25) / res_, (hi - 0.25) / res_)])
+    base = sv.Octree(device=local)
+    base.upload_triangles(tris)
+    base.buildSVO(L)
+    base.toDAG()
+    runs = {}
+    for kind in ("exact", "learned"):
+        for _ in range(max(args.warmup, 0) if kind == "exact" else 0):
+            base.clone().lossy(kind, 3, 5, 0.01)
+        times, st = [], None
+        for _ in range(args.steps):
+            o = base.clone()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            l0 = o.stats()["gpu_launches"]
+            st = o.lossy(kind, 3, 5, 0.01, top_k=args.top_k, train_pairs=args.train_pairs, epochs=args.epochs,
+                         seed=args.seed)
+            torch.cuda.synchronize()
+            times.append((time.perf_counter() - t0) * 1e3)
+            st["gpu_launches"] = o.stats()["gpu_launches"] - l0
+            o.close()
+        st["wall_ms"] = sum(times) / len(times)
+        st["merges_per_s"] = st["merged"] / (st["wall_ms"] / 1e3)
+        st["merges_per_s_without_training"] = st["merged"] / max(1e-9, (st["wall_ms"] - st["train_ms"]) / 1e3)
+        st["nodes_saved"] = st["nodes_before"] - st["nodes_after"]
+        runs[kind] = st
+    ex, le = runs["exact"], runs["learned"]
+    voxels = base.stats()["n_total_voxels"]
+    return {
+        "metric": METRIC, "value": le["merged"] / (le["wall_ms"] / 1e3), "unit": "lossy merges/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": le["wall_ms"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8 voxels + fp32 MLP",
+        "data": "synthetic",
+        "config": {"workload": "lossy: %dx%d terrain + 5000 boxes (sides 1-64 voxels), depth %d, candidates 3-5 "
+                               "levels above the leaves, merges within 1%% of the subtree cube's voxels" % (
+                                   args.grid, args.grid, L),
+                   "voxels": int(voxels), "exact": ex, "learned": le,
+                   "savings_vs_exact": le["nodes_saved"] / max(1, ex["nodes_saved"]),
+                   "throughput_vs_exact": (le["merged"] / le["wall_ms"]) / max(1e-9, ex["merged"] / ex["wall_ms"]),
+                   "top_k": args.top_k, "train_pairs": args.train_pairs, "epochs": args.epochs,
+                   "parallelism": "single GPU"},
+        "gpu_launches": int(le["gpu_launches"]), "e2e": None,
+    }
+
+
 def main():
     args = parse()
     rank, local, world = rank_info()
-    if args.workload == "batch" and args.impl != "reference":
-        res = run_batch(args, rank, local, world)
+    if args.workload in ("batch", "lossy") and args.impl != "reference":
+        res = (run_batch if args.workload == "batch" else run_lossy)(args, rank, local, world)
         if rank == 0:
             print(json.dumps(res))
         return

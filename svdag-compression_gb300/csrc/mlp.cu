@@ -13,10 +13,11 @@
 // each proposal with the exact distance, so the network only decides which
 // pairs get checked, never which merges are accepted.
 //
-// Kernels: a tiled fp32 GEMM (64x64 block tile, 4x4 per thread, optional
-// transposes, fused bias + ReLU), the siamese loss and its gradient, bias
-// gradients, Adam, and a banded top-k selection.  GEMMs here are small
-// (512x256 at most per layer); they run on the FP32 pipes.
+// Kernels: a tiled fp32 GEMM (128x128 block tile, 8x8 per thread, optional
+// transposes, fused bias + ReLU, split-K for the weight gradients), the
+// siamese loss and its gradient, bias gradients, Adam, and a banded top-k
+// selection.  The layers are small (512x256 at most); they run on the FP32
+// pipes.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -29,68 +30,94 @@ namespace svdag {
 namespace {
 
 constexpr int kIn = 512, kH = 256, kOut = 64;
-constexpr int kTile = 64, kTK = 16;
+constexpr int kBM = 128, kBN = 128, kBK = 8;
 
 // C[M x N] = op(A)[M x K] * op(B)[K x N] (+ bias[N]) (ReLU); row-major.
-// TA: A is stored K x M; TB: B is stored N x K.  accumulate: C += result.
+// TA: A is stored K x M; TB: B is stored N x K.  128x128 block tile, 8x8
+// outputs per thread (rows ty*4+{0..3} and 64+ty*4+{0..3}, columns likewise),
+// operands staged k-major in shared memory and read as float4.  With
+// gridDim.z > 1 the K range is split and partial sums are added into C
+// (zeroed by the caller; no bias or ReLU then).
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(256) k_gemm(const float* __restrict__ A, const float* __restrict__ B,
-                                              float* __restrict__ C, int M, int N, int K,
+                                              float* __restrict__ C, int M, int N, int K, int k_per,
                                               const float* __restrict__ bias, int relu, int accumulate) {
-  __shared__ float sA[kTK][kTile + 1];
-  __shared__ float sB[kTK][kTile + 1];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int row0 = blockIdx.y * kTile, col0 = blockIdx.x * kTile;
-  float acc[4][4] = {};
-  for (int k0 = 0; k0 < K; k0 += kTK) {
-    for (int t = threadIdx.x; t < kTK * kTile; t += 256) {
-      const int kk = t / kTile, mm = t % kTile;
-      const int r = row0 + mm, k = k0 + kk;
+  __shared__ __align__(16) float sA[kBK][kBM];
+  __shared__ __align__(16) float sB[kBK][kBN];
+  const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
+  const int row0 = blockIdx.y * kBM, col0 = blockIdx.x * kBN;
+  const int kb = blockIdx.z * k_per, ke = min(K, kb + k_per);
+  float acc[8][8] = {};
+  for (int k0 = kb; k0 < ke; k0 += kBK) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int idx = t * 4 + e;  // 0..1023 over the 128 x 8 tile
+      int r, k;
+      if (TA) { k = idx / kBM; r = idx % kBM; } else { r = idx / kBK; k = idx % kBK; }
+      const int gr = row0 + r, gk = k0 + k;
       float a = 0.f;
-      if (r < M && k < K) a = TA ? A[size_t(k) * M + r] : A[size_t(r) * K + k];
-      sA[kk][mm] = a;
-      const int cidx = col0 + mm;
+      if (gr < M && gk < ke) a = TA ? A[size_t(gk) * M + gr] : A[size_t(gr) * K + gk];
+      sA[k][r] = a;
+      int c, kk;
+      if (TB) { c = idx / kBK; kk = idx % kBK; } else { kk = idx / kBN; c = idx % kBN; }
+      const int gc = col0 + c, gk2 = k0 + kk;
       float b = 0.f;
-      if (cidx < N && k < K) b = TB ? B[size_t(cidx) * K + k] : B[size_t(k) * N + cidx];
-      sB[kk][mm] = b;
+      if (gc < N && gk2 < ke) b = TB ? B[size_t(gc) * K + gk2] : B[size_t(gk2) * N + gc];
+      sB[kk][c] = b;
     }
     __syncthreads();
 #pragma unroll
-    for (int kk = 0; kk < kTK; ++kk) {
-      float a[4], b[4];
+    for (int k = 0; k < kBK; ++k) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&sA[k][ty * 4]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&sA[k][64 + ty * 4]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&sB[k][tx * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&sB[k][64 + tx * 4]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = sA[kk][ty * 4 + i];
+      for (int i = 0; i < 8; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = sB[kk][tx * 4 + j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
     }
     __syncthreads();
   }
+  const bool split = gridDim.z > 1;
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int r = row0 + ty * 4 + i;
+  for (int i = 0; i < 8; ++i) {
+    const int r = row0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + i - 4);
     if (r >= M) continue;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int cidx = col0 + tx * 4 + j;
+    for (int j = 0; j < 8; ++j) {
+      const int cidx = col0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + j - 4);
       if (cidx >= N) continue;
+      float* o = C + size_t(r) * N + cidx;
+      if (split) {
+        atomicAdd(o, acc[i][j]);
+        continue;
+      }
       float v = acc[i][j];
       if (bias) v += bias[cidx];
       if (relu) v = fmaxf(v, 0.f);
-      float* o = C + size_t(r) * N + cidx;
       *o = accumulate ? *o + v : v;
     }
   }
 }
 
+// Splits K when the output has too few tiles to fill the GPU (the weight
+// gradients: 512x256 outputs over K = 2 x batch rows).
 template <bool TA, bool TB>
 void gemm(const Exec& ex, const float* A, const float* B, float* C, int M, int N, int K, const float* bias = nullptr,
           bool relu = false, bool acc = false) {
-  dim3 grid((N + kTile - 1) / kTile, (M + kTile - 1) / kTile);
-  SVDAG_LAUNCH(ex, (k_gemm<TA, TB>), grid, 256, 0, A, B, C, M, N, K, bias, relu ? 1 : 0, acc ? 1 : 0);
+  const int tiles = ((N + kBN - 1) / kBN) * ((M + kBM - 1) / kBM);
+  int splits = 1;
+  if (!bias && !relu && !acc && tiles < 2 * ex.sm_count) {
+    splits = std::max(1, std::min(2 * ex.sm_count / tiles, K / 256));
+  }
+  const int k_per = ((K + splits - 1) / splits + kBK - 1) / kBK * kBK;
+  splits = (K + k_per - 1) / k_per;
+  if (splits > 1) SVDAG_CUDA(cudaMemsetAsync(C, 0, sizeof(float) * size_t(M) * N, ex.stream));
+  dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM, splits);
+  SVDAG_LAUNCH(ex, (k_gemm<TA, TB>), grid, 256, 0, A, B, C, M, N, K, k_per, bias, relu ? 1 : 0, acc ? 1 : 0);
 }
 
 // Siamese loss: rows [0, n) are side a, [n, 2n) side b of the embeddings.
@@ -119,13 +146,19 @@ __global__ void k_relu_back(float* __restrict__ dH, const float* __restrict__ H,
     if (H[i] <= 0.f) dH[i] = 0.f;
 }
 
-// db[j] = sum_i dY[i][j]
+// db[j] += sum over this block's rows of dY[i][j] (db zeroed by the caller)
+constexpr int kBiasRows = 128;
 __global__ void k_bias_grad(const float* __restrict__ dY, int M, int N, float* __restrict__ db) {
+  const int r0 = blockIdx.y * kBiasRows, r1 = min(M, r0 + kBiasRows);
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x) {
     float s = 0.f;
-    for (int i = 0; i < M; ++i) s += dY[size_t(i) * N + j];
-    db[j] = s;
+    for (int i = r0; i < r1; ++i) s += dY[size_t(i) * N + j];
+    atomicAdd(&db[j], s);
   }
+}
+void bias_grad(const Exec& ex, const float* dY, int M, int N, float* db) {
+  SVDAG_CUDA(cudaMemsetAsync(db, 0, sizeof(float) * N, ex.stream));
+  SVDAG_LAUNCH(ex, k_bias_grad, dim3((N + 255) / 256, (M + kBiasRows - 1) / kBiasRows), 256, 0, dY, M, N, db);
 }
 
 __global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
@@ -316,17 +349,17 @@ void mlp_loss_grad(const Exec& ex, Mlp& net, MlpWork& W, int n) {
   SVDAG_LAUNCH(ex, k_pair_loss, grid_for(ex, n, 8), 256, 0, W.E.get(), W.t.get(), n, W.dE.get(), W.loss.get());
   // layer 3
   gemm<true, false>(ex, W.H2.get(), W.dE.get(), net.gp[4], kH, kOut, rows);
-  SVDAG_LAUNCH(ex, k_bias_grad, 1, 256, 0, W.dE.get(), rows, kOut, net.gp[5]);
+  bias_grad(ex, W.dE.get(), rows, kOut, net.gp[5]);
   gemm<false, true>(ex, W.dE.get(), net.p[4], W.dH2.get(), rows, kH, kOut);
   SVDAG_LAUNCH(ex, k_relu_back, grid_for(ex, size_t(rows) * kH, 256), 256, 0, W.dH2.get(), W.H2.get(), size_t(rows) * kH);
   // layer 2
   gemm<true, false>(ex, W.H1.get(), W.dH2.get(), net.gp[2], kH, kH, rows);
-  SVDAG_LAUNCH(ex, k_bias_grad, 1, 256, 0, W.dH2.get(), rows, kH, net.gp[3]);
+  bias_grad(ex, W.dH2.get(), rows, kH, net.gp[3]);
   gemm<false, true>(ex, W.dH2.get(), net.p[2], W.dH1.get(), rows, kH, kH);
   SVDAG_LAUNCH(ex, k_relu_back, grid_for(ex, size_t(rows) * kH, 256), 256, 0, W.dH1.get(), W.H1.get(), size_t(rows) * kH);
   // layer 1
   gemm<true, false>(ex, W.X.get(), W.dH1.get(), net.gp[0], kIn, kH, rows);
-  SVDAG_LAUNCH(ex, k_bias_grad, 1, 256, 0, W.dH1.get(), rows, kH, net.gp[1]);
+  bias_grad(ex, W.dH1.get(), rows, kH, net.gp[1]);
 }
 
 void mlp_adam(const Exec& ex, Mlp& net, float lr) {
