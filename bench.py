@@ -168,9 +168,10 @@ def peaks():
 R = 36
 
 # DRAM bytes (read + write) per launch measured by ncu on the full default
-# workload (one timed step's launches, averaged); see the k_expand profile
-# summary under profiles/.
-KERNEL_DRAM_BYTES_PER_LAUNCH = {}
+# workload (the 12 k_expand launches of one timed step, averaged; per-launch
+# figures in profiles/k_expand_terrain2048_L12_dram.txt).  Valid for the
+# default terrain workload only.
+KERNEL_DRAM_BYTES_PER_LAUNCH = {"k_expand": 564155413}
 
 
 def model_bytes(info, T):
@@ -321,14 +322,17 @@ def run_ours(args, rank, local, world):
         achieved = (ab / launches_per_step) / (per_launch_ms / 1e3) / 1e9 if ab else None
         roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": (achieved / hbm_peak) if achieved else None,
-                "traffic": KERNEL_DRAM_BYTES_PER_LAUNCH.get(name), "peak_source": peak_src,
+                "traffic": (KERNEL_DRAM_BYTES_PER_LAUNCH.get(name)
+                            if args.workload == "terrain" and args.grid == 2048 and args.levels == 12 else None),
+                "peak_source": peak_src,
                 "avg_launch_ms": per_launch_ms, "share": ms / sum(v[1] for v in prof.values())}
         if name == "k_expand":
             pairs = info["frontier"][0]
             roof["algorithmic_bytes"] = "B_vox = 36 T + 36 sum_l N_l per build, spread over its %d launches" % args.levels
-            roof["note"] = ("k_expand is instruction-issue bound (SAT box tests), not HBM bound: ncu on its two "
-                            "largest launches of terrain 1024 depth 11 shows issue slots 51-54% busy, ALU pipe "
-                            "46-50%, FMA pipe 14-16%, DRAM 3-4% of peak")
+            roof["note"] = ("k_expand is instruction-issue / latency bound (SAT box tests), not HBM bound: ncu on "
+                            "its two largest launches of terrain 1024 depth 11 shows issue slots 38-51% busy at 16 "
+                            "warps/SM, ALU pipe 35-48%, FMA 9-13%, FP64 <1%, DRAM 3% of peak "
+                            "(profiles/k_expand_terrain1024_L11.txt)")
             roof["sat"] = {"frontier_pairs_per_s": pairs / (ms / args.steps / 1e3),
                            "child_box_tests_per_s": 8 * pairs / (ms / args.steps / 1e3)}
     # reduction phases (toDAG, toSDAG, cross-level merge): algorithmic bytes
