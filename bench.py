@@ -45,7 +45,7 @@ def parse():
                          "boxes at depth 15, chunked build with step level 1; batch: 256 voxel-brick chunks of "
                          "depths 7-11 (value noise, 5-40%% fill), batched SSVDAG + CSVDAG; lossy: 2048^2 terrain + "
                          "5,000 boxes at depth 11, lossy LSVDAG with exact and learned pair proposals")
-    ap.add_argument("--top-k", type=int, default=16)
+    ap.add_argument("--top-k", type=int, default=256)
     ap.add_argument("--train-pairs", type=int, default=2000000)
     ap.add_argument("--epochs", type=int, default=2)
     ap.add_argument("--chunks", type=int, default=256)

@@ -401,11 +401,16 @@ void phase_reduce_sdag(Ctx& c) {
       SVDAG_LAUNCH(ex, k_sdag_candidates, grid_for(ex, n, 256), 256, 0, T, L.hdr.get(), ch, n, slot_of.get(),
                    child_inv, inv.get(), cand.get());
       fill<uint32_t>(ex, state.get(), n, kUndecided);
+      // rounds in groups of 4 between host reads (a round with nothing left
+      // is a no-op), at most 64 before the serial finish
       int rounds = 0;
       for (;;) {
-        SVDAG_CUDA(cudaMemsetAsync(d_left.get(), 0, 8, st));
-        SVDAG_LAUNCH(ex, k_sdag_round, grid_for(ex, n, 256), 256, 0, cand.get(), n, state.get(), var.get(), d_left.get());
-        ++rounds;
+        for (int r = 0; r < 4; ++r) {
+          SVDAG_CUDA(cudaMemsetAsync(d_left.get(), 0, 8, st));
+          SVDAG_LAUNCH(ex, k_sdag_round, grid_for(ex, n, 256), 256, 0, cand.get(), n, state.get(), var.get(),
+                       d_left.get());
+        }
+        rounds += 4;
         if (read_scalar(ex, d_left.get()) == 0) break;
         if (rounds >= 64) {
           SVDAG_LAUNCH(ex, k_sdag_serial, 1, 32, 0, cand.get(), n, state.get(), var.get());
