@@ -127,6 +127,15 @@ int svdag_level_device_ptrs(const svdag_ctx* ctx, uint32_t level, const uint32_t
                             const uint32_t** children, const uint8_t** child_levels,
                             const uint8_t** invariant);
 
+/* EncodedSVDAG::encode (src/symvox/encoded_svdag.cpp:105-199; DAG or CSVDAG
+ * after initChildLevels) and EncodedUSSVDAG::encode (encoded_ussvdag.cpp:
+ * 86-170; SDAG) on the GPU: the u32 stream that follows the file header.
+ * host_words may be NULL to query the size.  The file is: bbox min, max
+ * (6 floats), rootSide (float), levels (u32), nNodes (u32), the word count
+ * twice (the reference's "first leaf pointer" field holds it), the words. */
+enum { SVDAG_FORMAT_SVDAG = 0, SVDAG_FORMAT_USSVDAG = 1 };
+int svdag_encode(svdag_ctx* ctx, uint32_t format, uint32_t* host_words, uint64_t capacity, uint64_t* n_words);
+
 /* Per-kernel device timing (no counterpart in the reference, whose Stats
  * hold phase times only, src/symvox/geom_octree.hpp:54).  While enabled,
  * every kernel launch of the context is bracketed by CUDA events on its

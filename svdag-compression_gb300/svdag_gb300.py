@@ -92,6 +92,7 @@ GPU_SYMBOLS = {
     "svdag_batch_autotune": (_I, [_VP, _U32, _U32]),
     "svdag_batch_get_stats": (_I, [_VP, _VP]),
     "svdag_lossy_dag": (_I, [_VP, _VP, _VP]),
+    "svdag_encode": (_I, [_VP, _U32, _VP, _U64, ctypes.POINTER(_U64)]),
     "svdag_mlp_create": (_I, [ctypes.POINTER(_VP), _I, _U64]),
     "svdag_mlp_destroy": (_I, [_VP]),
     "svdag_mlp_param_count": (_U64, []),
@@ -321,6 +322,26 @@ class Octree:
 
     def toDAG(self):
         self._check(self._lib.svdag_reduce_dag(self._h))
+
+    def encode(self, fmt="svdag"):
+        """The EncodedSVDAG ("svdag") or EncodedUSSVDAG ("ussvdag") word
+        stream, encoded on the GPU (svdag_encode)."""
+        f = {"svdag": 0, "ussvdag": 1}[fmt]
+        n = ctypes.c_uint64()
+        self._check(self._lib.svdag_encode(self._h, f, None, 0, ctypes.byref(n)))
+        out = np.empty(n.value, np.uint32)
+        self._check(self._lib.svdag_encode(self._h, f, out.ctypes.data, n.value, ctypes.byref(n)))
+        return out
+
+    def save_encoded(self, path, fmt="svdag", bbox=UNIT_BOX, root_side=1.0):
+        """Writes the file the reference's saver writes for this stream."""
+        words = self.encode(fmt)
+        head = np.array(bbox, np.float32).tobytes() + np.array([root_side], np.float32).tobytes()
+        head += np.array([self.getLevels(), self.stats()["n_nodes"] & 0xFFFFFFFF, words.size, words.size],
+                         np.uint32).tobytes()
+        with open(path, "wb") as f:
+            f.write(head)
+            f.write(words.tobytes())
 
     LOSSY = {"exact": 0, "learned": 1, "untrained": 2}
 

@@ -38,3 +38,28 @@ def test_svbuilder_files_match_reference(name, tmp_path):
     got["csv.svdag"] = sha(base + "-multi.svdag")
     assert got == g["files"]
     assert ("Voxels:" in r.stdout) and os.path.exists(str(tmp_path / "stats.txt"))
+
+
+@pytest.mark.parametrize("name", ["ico3_L6", "ico5_L9", "terrain65_L8", "boxes_L8", "terrain129_L9_step1"])
+def test_gpu_encoder_matches_reference_files(name, tmp_path):
+    """svdag_encode (the SVDAG / CSVDAG / USSVDAG streams built on the GPU)
+    gives the reference's files byte for byte."""
+    g = G[name]
+    o = sv.Octree()
+    o.upload_triangles(SCENES[name]())
+    if g["step_levels"]:
+        o.buildDAG(g["levels"], g["step_levels"])
+    else:
+        o.buildSVO(g["levels"])
+        o.toDAG()
+    o.initChildLevels()
+    p = str(tmp_path / "a")
+    o.save_encoded(p + ".svdag", "svdag")
+    s = o.clone()
+    s.toSDAG()
+    s.save_encoded(p + ".ussvdag", "ussvdag")
+    c = o.clone()
+    c.mergeAcrossAllLevels()
+    c.save_encoded(p + ".csv.svdag", "svdag")
+    got = {ext: sha(p + "." + ext) for ext in ("svdag", "ussvdag", "csv.svdag")}
+    assert got == {ext: g["files"][ext] for ext in got}
