@@ -80,6 +80,39 @@ bool EncodedSVDAG::encode(const NodeData& d, const float bb[6], float rs, uint64
   return true;
 }
 
+namespace {
+// The device-built stream of `o` in format f into `data`; false when the
+// octree's state does not fit the format.
+bool gpu_stream(const GeomOctree& o, uint32_t f, std::vector<uint32_t>& data) {
+  uint64_t n = 0;
+  if (svdag_encode(o.handle(), f, nullptr, 0, &n) != SVDAG_OK) return false;
+  data.resize(n);
+  return svdag_encode(o.handle(), f, data.data(), n, &n) == SVDAG_OK;
+}
+}  // namespace
+
+bool EncodedSVDAG::encode(const GeomOctree& o) {
+  if (o.getState() != S_DAG) return false;
+  if (!gpu_stream(o, SVDAG_FORMAT_SVDAG, data)) return false;
+  std::memcpy(bbox, o.getSceneBBox(), sizeof(bbox));
+  rootSide = o.getRootSide();
+  levels = o.getLevels();
+  nNodes = o.getNNodes();
+  firstLeafPtr = uint32_t(data.size());  // the reference writes the word count here
+  return true;
+}
+
+bool EncodedUSSVDAG::encode(const GeomOctree& o) {
+  if (o.getState() != S_SDAG) return false;
+  if (!gpu_stream(o, SVDAG_FORMAT_USSVDAG, data)) return false;
+  std::memcpy(bbox, o.getSceneBBox(), sizeof(bbox));
+  rootSide = o.getRootSide();
+  levels = o.getLevels();
+  nNodes = o.getNNodes();
+  firstLeafPtr = uint32_t(data.size());
+  return true;
+}
+
 bool EncodedSVDAG::save(const std::string& path) const {
   std::ofstream f(path, std::ios::binary);
   if (!f) return false;

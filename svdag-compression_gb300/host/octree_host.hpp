@@ -108,6 +108,8 @@ struct EncodedSVDAG {
   uint32_t firstLeafPtr = 0;
   std::vector<uint32_t> data;
   bool encode(const NodeData& d, const float bbox[6], float rootSide, uint64_t nNodes, State st);
+  // the same stream built on the GPU from the octree's device pools (svdag_encode)
+  bool encode(const GeomOctree& o);
   bool save(const std::string& path) const;
   size_t getDataSize() const { return data.size() * 4; }
   // EncodedSVDAG::load / decode (encoded_svdag.cpp:44-74, 217-281): the
@@ -127,6 +129,8 @@ struct EncodedUSSVDAG {
   uint32_t firstLeafPtr = 0;
   std::vector<uint32_t> data;
   bool encode(const NodeData& d, const float bbox[6], float rootSide, uint64_t nNodes, State st);
+  // the same stream built on the GPU (svdag_encode)
+  bool encode(const GeomOctree& o);
   bool save(const std::string& path) const;
   size_t getDataSize() const { return data.size() * 4; }
 };

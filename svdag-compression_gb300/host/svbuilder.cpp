@@ -133,14 +133,16 @@ int main(int argc, char** argv) {
   octree.initChildLevels();
   const std::string basePath = dir_of(input) + "/" + base_of(input) + "_" + std::to_string(nLevels);
 
+  // the SVDAG / USSVDAG pointer streams are built on the GPU; the SSVDAG
+  // (reference-count order, libstdc++ sort) is encoded on the host
   EncodedSVDAG svdag2;
-  svdag2.encode(octree.getNodeData(), octree.getSceneBBox(), octree.getRootSide(), octree.getNNodes(), octree.getState());
+  svdag2.encode(octree);
   svdag2.save(basePath + ".svdag");
 
   if (multiLevel) octree.mergeAcrossAllLevels();
 
   EncodedSVDAG svdag;
-  svdag.encode(octree.getNodeData(), octree.getSceneBBox(), octree.getRootSide(), octree.getNNodes(), octree.getState());
+  svdag.encode(octree);
   EncodedSSVDAG esvdag;
   if (!multiLevel)
     esvdag.encode(octree.getNodeData(), octree.getSceneBBox(), octree.getRootSide(), octree.getNNodes(),
@@ -149,8 +151,7 @@ int main(int argc, char** argv) {
   EncodedUSSVDAG ussvdag;
   EncodedSSVDAG ssvdag;
   if (!multiLevel) {
-    ussvdag.encode(octree.getNodeData(), octree.getSceneBBox(), octree.getRootSide(), octree.getNNodes(),
-                   octree.getState());
+    ussvdag.encode(octree);
     ssvdag.encode(octree.getNodeData(), octree.getSceneBBox(), octree.getRootSide(), octree.getNNodes(),
                   octree.getState());
   }
