@@ -136,6 +136,15 @@ int svdag_level_device_ptrs(const svdag_ctx* ctx, uint32_t level, const uint32_t
 enum { SVDAG_FORMAT_SVDAG = 0, SVDAG_FORMAT_USSVDAG = 1 };
 int svdag_encode(svdag_ctx* ctx, uint32_t format, uint32_t* host_words, uint64_t capacity, uint64_t* n_words);
 
+/* EncodedSSVDAG::traverse (src/symvox/encoded_ssvdag.cpp:527-574) on the
+ * GPU, one point query per thread: the depth each point reaches in an encoded
+ * SSVDAG (the arrays of a .ssvdag file), `levels` when its voxel is set, -1
+ * outside the box.  Host buffers; points as x, y, z floats. */
+int svdag_ssvdag_traverse(const uint16_t* inner, uint64_t n_inner, const uint8_t* leaves, uint64_t n_leaves,
+                          const uint32_t* level_offsets, uint32_t n_level_offsets, uint32_t levels,
+                          const float bbox[6], float root_side, const float* points, uint64_t n_points,
+                          int32_t* depth);
+
 /* Per-kernel device timing (no counterpart in the reference, whose Stats
  * hold phase times only, src/symvox/geom_octree.hpp:54).  While enabled,
  * every kernel launch of the context is bracketed by CUDA events on its

@@ -37,6 +37,7 @@ _SIGS = {
     "ora_build_dag_chunked": (_I, [_VP, _VP, _U64, _VP, _U32, _U32, _I]),
     "ora_build_from_bricks": (_I, [_VP, _U32, _VP]),
     "ora_lossy_exact": (_I, [_VP, _U32, _U32, ctypes.c_double, ctypes.POINTER(_U64)]),
+    "ora_ssvdag_traverse": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, _VP, _U64, _VP]),
     "ora_to_dag": (_I, [_VP]),
     "ora_to_sdag": (_I, [_VP]),
     "ora_init_child_levels": (_I, [_VP]),
@@ -164,3 +165,33 @@ def pool_digest(pool):
         h.update(np.uint64(len(lev)).tobytes())
         h.update(np.ascontiguousarray(lev).tobytes())
     return h.hexdigest()
+
+
+def read_ssvdag(path):
+    """Fields of a .ssvdag file (EncodedSSVDAG::save layout)."""
+    raw = open(path, "rb").read()
+    o = 0
+    bbox = np.frombuffer(raw, np.float32, 6, o); o += 24
+    root_side = float(np.frombuffer(raw, np.float32, 1, o)[0]); o += 4
+    levels, n_nodes = np.frombuffer(raw, np.uint32, 2, o); o += 8
+    n = int(np.frombuffer(raw, np.uint32, 1, o)[0]); o += 4
+    inner = np.frombuffer(raw, np.uint16, n, o).copy(); o += 2 * n
+    n = int(np.frombuffer(raw, np.uint32, 1, o)[0]); o += 4
+    leaves = np.frombuffer(raw, np.uint8, n, o).copy(); o += n
+    n = int(np.frombuffer(raw, np.uint32, 1, o)[0]); o += 4
+    offs = np.frombuffer(raw, np.uint32, n, o).copy()
+    return {"bbox": bbox.copy(), "root_side": root_side, "levels": int(levels), "n_nodes": int(n_nodes),
+            "inner": inner, "leaves": leaves, "level_offsets": offs}
+
+
+def ssvdag_traverse(f, pts):
+    """EncodedSSVDAG::traverse restated: depth reached per query point
+    (-1 outside the box, -2 where a pointer leads outside the arrays)."""
+    pts = np.ascontiguousarray(pts, np.float32)
+    out = np.empty(pts.shape[0], np.int32)
+    inner, leaves, offs = f["inner"], f["leaves"], f["level_offsets"]
+    rc = load().ora_ssvdag_traverse(inner.ctypes.data, inner.size, leaves.ctypes.data, leaves.size, offs.ctypes.data,
+                                    offs.size, f["levels"], f["bbox"].ctypes.data, f["root_side"], pts.ctypes.data,
+                                    pts.shape[0], out.ctypes.data)
+    assert rc in (0, -2), rc
+    return out

@@ -788,6 +788,96 @@ int ora_lossy_exact(ora_octree* o, uint32_t min_above, uint32_t max_above, doubl
   return 0;
 }
 
+// EncodedSSVDAG::traverse (src/symvox/encoded_ssvdag.cpp:527-574) with
+// getChild / getChildMask (:587-625) and getHalfSide (encoded_octree.hpp:68):
+// the depth a point query reaches in an encoded SSVDAG (levels = voxel set).
+// The leaf bricks are read in the encoder's default voxel-matrix order
+// (:32, 317-345, xyz_to_byte_voxel :119-135), not as traverse() reads them
+// (one byte per 2^3 sub-brick, the layout of the non-default mode).
+// A pointer that leads outside the arrays ends that query with depth -2 and
+// makes the call return -2.
+int ora_ssvdag_traverse(const uint16_t* inner, uint64_t n_inner, const uint8_t* leaves, uint64_t n_leaves,
+                        const uint32_t* level_off, uint32_t n_level_off, uint32_t levels, const float bbox[6],
+                        float root_side, const float* pts, uint64_t n, int32_t* out) {
+  if (levels < 3) return -1;
+  int status = 0;
+  auto code = [&](const uint16_t* nd, int c) { return (nd[0] >> (2 * c)) & 3u; };
+  for (uint64_t q = 0; q < n; ++q) {
+    float p[3] = {pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]};
+    bool inside = true;
+    for (int k = 0; k < 3; ++k) inside = inside && !(p[k] < bbox[k] || p[k] > bbox[3 + k]);
+    if (!inside) { out[q] = -1; continue; }
+    uint64_t idx = 0;
+    uint32_t lev = 0;
+    float c[3];
+    for (int k = 0; k < 3; ++k) c[k] = (bbox[k] + bbox[3 + k]) * 0.5f;
+    bool mx = false, my = false, mz = false;
+    bool broken = false;
+    while (lev < levels) {
+      if (idx >= n_inner) { broken = true; break; }
+      const uint16_t* nd = inner + idx;
+      if (mx) p[0] = 2.f * c[0] - p[0];
+      if (my) p[1] = 2.f * c[1] - p[1];
+      if (mz) p[2] = 2.f * c[2] - p[2];
+      int sel = 4 * int(p[0] > c[0]) + 2 * int(p[1] > c[1]) + int(p[2] > c[2]);
+      if (code(nd, sel) == 0) break;
+      ++lev;
+      float hs = root_side / float(1u << (lev + 1));
+      for (int k = 0; k < 3; ++k) c[k] += (p[k] > c[k]) ? hs : -1.f * hs;
+      uint64_t off = 1;
+      for (int i = 7; i > sel; --i) off += code(nd, i) == 0 ? 0 : (code(nd, i) == 1 ? 1 : 2);
+      const uint32_t cc = code(nd, sel);
+      if (idx + off + (cc >= 2 ? 2 : 1) > n_inner) { broken = true; break; }
+      uint32_t ch;
+      if (cc == 1) {
+        ch = nd[off];
+        mx = (ch >> 13) & 1u; my = (ch >> 14) & 1u; mz = (ch >> 15) & 1u;
+        ch &= ~(7u << 13);
+      } else {
+        // the high half is written first (encoded_ssvdag.cpp:395-403)
+        ch = (uint32_t(nd[off]) << 16) | uint32_t(nd[off + 1]);
+        mx = (ch >> 29) & 1u; my = (ch >> 30) & 1u; mz = (ch >> 31) & 1u;
+        ch &= ~(7u << 29);
+        ch |= (cc & 1u) << 29;
+      }
+      if (lev < levels - 2) {
+        if (lev >= n_level_off) { broken = true; break; }
+        idx = uint64_t(level_off[lev]) + ch;
+      } else if (lev == levels - 2) {
+        const uint64_t leaf = uint64_t(ch) * 8;
+        if (leaf + 8 > n_leaves) { broken = true; break; }
+        if (mx) p[0] = 2.f * c[0] - p[0];
+        if (my) p[1] = 2.f * c[1] - p[1];
+        if (mz) p[2] = 2.f * c[2] - p[2];
+        sel = 4 * int(p[0] > c[0]) + 2 * int(p[1] > c[1]) + int(p[2] > c[2]);
+        // the 2^3 sub-brick `sel` is empty when its 8 voxel bits are
+        uint32_t any = 0;
+        for (int v = 0; v < 8; ++v) {
+          const int b = (2 * (sel & 1) + (v & 1)) + 4 * (2 * ((sel >> 1) & 1) + ((v >> 1) & 1)) +
+                        16 * (2 * ((sel >> 2) & 1) + ((v >> 2) & 1));
+          any |= (leaves[leaf + b / 8] >> (b % 8)) & 1u;
+        }
+        if (!any) break;
+        ++lev;
+        hs = root_side / float(1u << (lev + 1));
+        for (int k = 0; k < 3; ++k) c[k] += (p[k] > c[k]) ? hs : -1.f * hs;
+        const int vox = 4 * int(p[0] > c[0]) + 2 * int(p[1] > c[1]) + int(p[2] > c[2]);
+        // the brick's bits in the encoder's default voxel-matrix order
+        // (encoded_ssvdag.cpp:32, 317-345, xyz_to_byte_voxel :119-135):
+        // local (x, y, z) in [0, 4)^3 at bit z + 4y + 16x
+        const int bi = 2 * ((sel >> 2) & 1) + ((vox >> 2) & 1), bj = 2 * ((sel >> 1) & 1) + ((vox >> 1) & 1),
+                  bk = 2 * (sel & 1) + (vox & 1);
+        const int bit = bk + 4 * bj + 16 * bi;
+        if ((leaves[leaf + bit / 8] >> (bit % 8)) & 1u) ++lev;
+        break;
+      }
+    }
+    if (broken) status = -2;
+    out[q] = broken ? -2 : int32_t(lev);
+  }
+  return status;
+}
+
 int ora_to_dag(ora_octree* o) { return o ? to_dag(o) : -1; }
 int ora_to_sdag(ora_octree* o) { return o ? to_sdag(o) : -1; }
 int ora_init_child_levels(ora_octree* o) {

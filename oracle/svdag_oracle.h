@@ -42,6 +42,10 @@ int ora_build_dag_chunked(ora_octree* o, const float* tris, uint64_t n_tris, con
 int ora_build_from_bricks(ora_octree* o, uint32_t depth, const uint8_t* bricks);
 /* lossy LSVDAG, exact-proposer form (project-defined; see the .cpp) */
 int ora_lossy_exact(ora_octree* o, uint32_t min_above, uint32_t max_above, double max_err, uint64_t* merged);
+/* EncodedSSVDAG::traverse (encoded_ssvdag.cpp:527-574): depth reached per point */
+int ora_ssvdag_traverse(const uint16_t* inner, uint64_t n_inner, const uint8_t* leaves, uint64_t n_leaves,
+                        const uint32_t* level_off, uint32_t n_level_off, uint32_t levels, const float bbox[6],
+                        float root_side, const float* pts, uint64_t n, int32_t* out);
 int ora_to_dag(ora_octree* o);                 /* geom_octree.cpp:462-548 */
 int ora_to_sdag(ora_octree* o);                /* geom_octree.cpp:551-697 (greedy, symmetry on) */
 int ora_init_child_levels(ora_octree* o);      /* geom_octree_extension.cpp:21-30 */

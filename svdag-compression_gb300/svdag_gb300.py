@@ -93,6 +93,7 @@ GPU_SYMBOLS = {
     "svdag_batch_get_stats": (_I, [_VP, _VP]),
     "svdag_lossy_dag": (_I, [_VP, _VP, _VP]),
     "svdag_encode": (_I, [_VP, _U32, _VP, _U64, ctypes.POINTER(_U64)]),
+    "svdag_ssvdag_traverse": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, _VP, _U64, _VP]),
     "svdag_mlp_create": (_I, [ctypes.POINTER(_VP), _I, _U64]),
     "svdag_mlp_destroy": (_I, [_VP]),
     "svdag_mlp_param_count": (_U64, []),
@@ -571,3 +572,18 @@ class Mlp:
         if r != 0:
             raise SvdagError(r, "mlp embed failed")
         return out
+
+
+def ssvdag_traverse(f, pts):
+    """GPU point queries of an encoded SSVDAG (fields as read from a .ssvdag
+    file: inner, leaves, level_offsets, levels, bbox, root_side)."""
+    lib = load_gpu()
+    pts = np.ascontiguousarray(pts, np.float32)
+    out = np.empty(pts.shape[0], np.int32)
+    bb = np.ascontiguousarray(f["bbox"], np.float32)
+    r = lib.svdag_ssvdag_traverse(f["inner"].ctypes.data, f["inner"].size, f["leaves"].ctypes.data, f["leaves"].size,
+                                  f["level_offsets"].ctypes.data, f["level_offsets"].size, f["levels"], bb.ctypes.data,
+                                  f["root_side"], pts.ctypes.data, pts.shape[0], out.ctypes.data)
+    if r != 0:
+        raise SvdagError(r, "ssvdag traverse failed")
+    return out
