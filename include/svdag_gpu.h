@@ -139,11 +139,56 @@ int svdag_encode(svdag_ctx* ctx, uint32_t format, uint32_t* host_words, uint64_t
 /* EncodedSSVDAG::traverse (src/symvox/encoded_ssvdag.cpp:527-574) on the
  * GPU, one point query per thread: the depth each point reaches in an encoded
  * SSVDAG (the arrays of a .ssvdag file), `levels` when its voxel is set, -1
- * outside the box.  Host buffers; points as x, y, z floats. */
+ * outside the box, -2 where a pointer leads outside the arrays (the call
+ * then returns SVDAG_ERR_INVALID_ARG).  Host buffers; points as x, y, z
+ * floats. */
 int svdag_ssvdag_traverse(const uint16_t* inner, uint64_t n_inner, const uint8_t* leaves, uint64_t n_leaves,
                           const uint32_t* level_offsets, uint32_t n_level_offsets, uint32_t levels,
                           const float bbox[6], float root_side, const float* points, uint64_t n_points,
                           int32_t* depth);
+
+/* Ray casting of an encoded SSVDAG: the viewer's DDA traversal
+ * (shaders/octree_dda.frag.glsl:539-581, trace_ray, SSVDAG variant, as
+ * OctreeDDARenderer feeds it, src/svviewer/octree_dda_renderer.cpp:199-223,
+ * 391-422) into a headless buffer, one ray per pixel, pixel (x, y) at index
+ * y * width + x with y = 0 the bottom row (gl_FragCoord).
+ * svdag_ssvdag_upload copies the arrays of a .ssvdag file to the current
+ * device (n_leaves a multiple of 8). */
+typedef struct svdag_ssvdag svdag_ssvdag;
+int svdag_ssvdag_upload(const uint16_t* inner, uint64_t n_inner, const uint8_t* leaves, uint64_t n_leaves,
+                        const uint32_t* level_offsets, uint32_t n_level_offsets, uint32_t levels,
+                        const float bbox[6], float root_side, svdag_ssvdag** out);
+int svdag_ssvdag_free(svdag_ssvdag* s);
+
+typedef struct svdag_camera {
+  float view_inv[16];       /* inverse view matrix, column-major (glUniformMatrix4fv, no transpose) */
+  float proj_inv[16];       /* inverse projection matrix, column-major */
+  uint32_t width, height;   /* screenRes */
+  uint32_t max_iters;       /* maxIters (the viewer's default: 300) */
+  uint32_t draw_level;      /* drawLevel (the viewer's default: the level count) */
+  float projection_factor;  /* projectionFactor (OctreeDDARenderer::getProjectionFactor) */
+  float t_min, t_max;       /* the ray's t range in world units (the viewer: 0, 1e30) */
+} svdag_camera;
+
+/* One pixel: trace_ray's result -- t = hit distance in world units, or -1
+ * (inside the box, no hit), -2 (past t_max), -3 (max_iters reached), -4
+ * (outside the box), -5 (a pointer outside the arrays); level = the shader
+ * level of the hit; iterations; node = node index of the hit (-1 none) --
+ * plus the hit cell's grid coordinates at that level and the entry face
+ * normal -stepDir as three signed bytes (x in the low byte). */
+typedef struct svdag_ray_hit {
+  float t;
+  int32_t level, iterations, node;
+  int32_t voxel[3];
+  uint32_t normal;
+} svdag_ray_hit;
+
+/* hits: width * height records, in device memory when device_buffer != 0
+ * (then on `stream`, or the handle's own stream when NULL), else host
+ * memory.  Returns when the buffer is written; SVDAG_ERR_INVALID_ARG when a
+ * ray met a pointer outside the arrays (its record has t = -5). */
+int svdag_ssvdag_raycast(svdag_ssvdag* s, const svdag_camera* cam, void* stream, svdag_ray_hit* hits,
+                         int device_buffer);
 
 /* Per-kernel device timing (no counterpart in the reference, whose Stats
  * hold phase times only, src/symvox/geom_octree.hpp:54).  While enabled,

@@ -38,6 +38,8 @@ _SIGS = {
     "ora_build_from_bricks": (_I, [_VP, _U32, _VP]),
     "ora_lossy_exact": (_I, [_VP, _U32, _U32, ctypes.c_double, ctypes.POINTER(_U64)]),
     "ora_ssvdag_traverse": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, _VP, _U64, _VP]),
+    "ora_ssvdag_raycast": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, _VP, _VP, _U32, _U32,
+                                _U32, _U32, ctypes.c_float, ctypes.c_float, ctypes.c_float, _VP]),
     "ora_to_dag": (_I, [_VP]),
     "ora_to_sdag": (_I, [_VP]),
     "ora_init_child_levels": (_I, [_VP]),
@@ -195,3 +197,26 @@ def ssvdag_traverse(f, pts):
                                     pts.shape[0], out.ctypes.data)
     assert rc in (0, -2), rc
     return out
+
+# one ray-cast pixel (the 32-byte hit record)
+HIT = np.dtype([("t", "<f4"), ("level", "<i4"), ("iterations", "<i4"), ("node", "<i4"), ("voxel", "<i4", (3,)),
+                ("normal", "<u4")])
+
+
+def ssvdag_raycast(f, cam):
+    """The viewer's SSVDAG ray traversal restated on the CPU: one hit record
+    per pixel (row y = 0 at the bottom).  `cam` holds view_inv, proj_inv
+    (column-major 16 floats), width, height, max_iters, draw_level,
+    projection_factor, t_min, t_max.  Returns (hits, status): status -2 when
+    a ray met a pointer outside the arrays."""
+    inner, leaves, offs = f["inner"], f["leaves"], f["level_offsets"]
+    bb = np.ascontiguousarray(f["bbox"], np.float32)
+    vi = np.ascontiguousarray(cam["view_inv"], np.float32).ravel()
+    pi = np.ascontiguousarray(cam["proj_inv"], np.float32).ravel()
+    out = np.zeros(cam["width"] * cam["height"], HIT)
+    rc = load().ora_ssvdag_raycast(inner.ctypes.data, inner.size, leaves.ctypes.data, leaves.size, offs.ctypes.data,
+                                   offs.size, f["levels"], bb.ctypes.data, f["root_side"], vi.ctypes.data,
+                                   pi.ctypes.data, cam["width"], cam["height"], cam["max_iters"], cam["draw_level"],
+                                   cam["projection_factor"], cam["t_min"], cam["t_max"], out.ctypes.data)
+    assert rc in (0, -2), rc
+    return out, rc

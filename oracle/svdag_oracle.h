@@ -46,6 +46,13 @@ int ora_lossy_exact(ora_octree* o, uint32_t min_above, uint32_t max_above, doubl
 int ora_ssvdag_traverse(const uint16_t* inner, uint64_t n_inner, const uint8_t* leaves, uint64_t n_leaves,
                         const uint32_t* level_off, uint32_t n_level_off, uint32_t levels, const float bbox[6],
                         float root_side, const float* pts, uint64_t n, int32_t* out);
+/* the viewer's SSVDAG ray traversal (shaders/octree_dda.frag.glsl:539-581),
+ * one 32-byte hit record per pixel (ssvdag_raycast.cpp) */
+int ora_ssvdag_raycast(const uint16_t* inner, uint64_t n_inner, const uint8_t* leaves, uint64_t n_leaves,
+                       const uint32_t* level_off, uint32_t n_level_off, uint32_t levels, const float bbox[6],
+                       float root_side, const float view_inv[16], const float proj_inv[16], uint32_t width,
+                       uint32_t height, uint32_t max_iters, uint32_t draw_level, float projection_factor,
+                       float t_min, float t_max, void* hits);
 int ora_to_dag(ora_octree* o);                 /* geom_octree.cpp:462-548 */
 int ora_to_sdag(ora_octree* o);                /* geom_octree.cpp:551-697 (greedy, symmetry on) */
 int ora_init_child_levels(ora_octree* o);      /* geom_octree_extension.cpp:21-30 */

@@ -26,7 +26,7 @@ CXX = os.environ.get("CXX", "g++")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # extra nvcc flags (e.g. tuning macros), whitespace separated
 EXTRA_NVCC = os.environ.get("SVDAG_NVCC_FLAGS", "").split()
-CU_SOURCES = ["api.cu", "voxelize.cu", "reduce.cu", "csvdag.cu", "chunked.cu", "batch.cu", "lossy.cu", "mlp.cu", "encode.cu", "traverse.cu", "noalloc.cu"]
+CU_SOURCES = ["api.cu", "voxelize.cu", "reduce.cu", "csvdag.cu", "chunked.cu", "batch.cu", "lossy.cu", "mlp.cu", "encode.cu", "traverse.cu", "raycast.cu", "noalloc.cu"]
 HOST_SOURCES = ["synth.cpp", "encoders.cpp", "scene.cpp", "geom_octree.cpp"]
 
 
@@ -92,10 +92,10 @@ def build_cli(gpu_lib):
 def build_oracle():
     d = os.path.join(ORACLE, "build")
     os.makedirs(d, exist_ok=True)
-    src = os.path.join(ORACLE, "svdag_oracle.cpp")
+    srcs = [os.path.join(ORACLE, "svdag_oracle.cpp"), os.path.join(ORACLE, "ssvdag_raycast.cpp")]
     out = os.path.join(d, "liboracle.so")
-    if not _newer(out, [src, os.path.join(ORACLE, "svdag_oracle.h")]):
-        _run([CXX, "-O3", "-std=gnu++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", out])
+    if not _newer(out, srcs + [os.path.join(ORACLE, "svdag_oracle.h")]):
+        _run([CXX, "-O3", "-std=gnu++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"] + srcs + ["-o", out])
     return out
 
 

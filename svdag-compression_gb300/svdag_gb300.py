@@ -94,6 +94,9 @@ GPU_SYMBOLS = {
     "svdag_lossy_dag": (_I, [_VP, _VP, _VP]),
     "svdag_encode": (_I, [_VP, _U32, _VP, _U64, ctypes.POINTER(_U64)]),
     "svdag_ssvdag_traverse": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, _VP, _U64, _VP]),
+    "svdag_ssvdag_upload": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, ctypes.POINTER(_VP)]),
+    "svdag_ssvdag_free": (_I, [_VP]),
+    "svdag_ssvdag_raycast": (_I, [_VP, _VP, _VP, _VP, _I]),
     "svdag_mlp_create": (_I, [ctypes.POINTER(_VP), _I, _U64]),
     "svdag_mlp_destroy": (_I, [_VP]),
     "svdag_mlp_param_count": (_U64, []),
@@ -587,3 +590,122 @@ def ssvdag_traverse(f, pts):
     if r != 0:
         raise SvdagError(r, "ssvdag traverse failed")
     return out
+
+
+# --------------------------------------------------------------------------
+# ray casting of encoded SSVDAGs
+
+# one pixel's result (svdag_ray_hit)
+HIT = np.dtype([("t", "<f4"), ("level", "<i4"), ("iterations", "<i4"), ("node", "<i4"), ("voxel", "<i4", (3,)),
+                ("normal", "<u4")])
+
+
+class _Camera(ctypes.Structure):
+    _fields_ = [
+        ("view_inv", ctypes.c_float * 16),
+        ("proj_inv", ctypes.c_float * 16),
+        ("width", ctypes.c_uint32),
+        ("height", ctypes.c_uint32),
+        ("max_iters", ctypes.c_uint32),
+        ("draw_level", ctypes.c_uint32),
+        ("projection_factor", ctypes.c_float),
+        ("t_min", ctypes.c_float),
+        ("t_max", ctypes.c_float),
+    ]
+
+
+def camera(eye, target, width, height, levels, up=(0.0, 1.0, 0.0), fovy_deg=60.0, near=0.01, far=100.0,
+           pixel_tolerance=1.0, max_iters=300):
+    """A perspective camera as the viewer sets one up: gluLookAt /
+    gluPerspective matrices inverted (column-major floats), the viewer's
+    default 60-degree field of view, 300 iterations, full draw level, and
+    OctreeDDARenderer::getProjectionFactor for the pixel tolerance."""
+    eye, target, up = (np.asarray(v, np.float64) for v in (eye, target, up))
+    f = target - eye
+    f /= np.linalg.norm(f)
+    sd = np.cross(f, up)
+    sd /= np.linalg.norm(sd)
+    u = np.cross(sd, f)
+    view = np.eye(4)
+    view[0, :3], view[1, :3], view[2, :3] = sd, u, -f
+    view[:3, 3] = -view[:3, :3] @ eye
+    fovy = np.float32(fovy_deg * 3.14159265359 / 180.0)
+    g = 1.0 / np.tan(float(fovy) / 2)
+    proj = np.zeros((4, 4))
+    proj[0, 0] = g / (width / height)
+    proj[1, 1] = g
+    proj[2, 2] = (far + near) / (near - far)
+    proj[2, 3] = 2 * far * near / (near - far)
+    proj[3, 2] = -1.0
+    inv2tan = np.float32(1.0) / (np.float32(2.0) * np.float32(np.tan(np.float32(0.5) * fovy)))
+    tol = np.float32(pixel_tolerance) / np.float32(height)
+    return {"view_inv": np.linalg.inv(view).T.astype(np.float32).ravel(),
+            "proj_inv": np.linalg.inv(proj).T.astype(np.float32).ravel(),
+            "width": int(width), "height": int(height), "max_iters": int(max_iters), "draw_level": int(levels),
+            "projection_factor": float(inv2tan / tol), "t_min": 0.0, "t_max": 1e30}
+
+
+def _camera_struct(cam):
+    c = _Camera()
+    c.view_inv[:] = [float(x) for x in np.asarray(cam["view_inv"], np.float32).ravel()]
+    c.proj_inv[:] = [float(x) for x in np.asarray(cam["proj_inv"], np.float32).ravel()]
+    for k in ("width", "height", "max_iters", "draw_level", "projection_factor", "t_min", "t_max"):
+        setattr(c, k, cam[k])
+    return c
+
+
+class Ssvdag:
+    """An encoded SSVDAG (the arrays of a .ssvdag file, as read_ssvdag
+    returns them) resident on the current CUDA device."""
+
+    def __init__(self, f):
+        self._lib = load_gpu()
+        self.h = _VP()
+        bb = np.ascontiguousarray(f["bbox"], np.float32)
+        self.levels = int(f["levels"])
+        r = self._lib.svdag_ssvdag_upload(f["inner"].ctypes.data, f["inner"].size, f["leaves"].ctypes.data,
+                                          f["leaves"].size, f["level_offsets"].ctypes.data, f["level_offsets"].size,
+                                          f["levels"], bb.ctypes.data, f["root_side"], ctypes.byref(self.h))
+        if r != 0:
+            raise SvdagError(r, "ssvdag upload failed")
+
+    def close(self):
+        if self.h:
+            self._lib.svdag_ssvdag_free(self.h)
+            self.h = _VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def raycast(self, cam):
+        """One hit record per pixel (row y = 0 at the bottom), host array."""
+        out = np.zeros(cam["width"] * cam["height"], HIT)
+        c = _camera_struct(cam)
+        r = self._lib.svdag_ssvdag_raycast(self.h, ctypes.byref(c), None, out.ctypes.data, 0)
+        if r != 0:
+            raise SvdagError(r, "ssvdag raycast failed")
+        return out
+
+    def raycast_device(self, cam, hits_ptr, stream_ptr=None):
+        """Ray cast into a device buffer of width * height * 32 bytes."""
+        c = _camera_struct(cam)
+        r = self._lib.svdag_ssvdag_raycast(self.h, ctypes.byref(c), stream_ptr, hits_ptr, 1)
+        if r != 0:
+            raise SvdagError(r, "ssvdag raycast failed")
+
+
+def write_depth_pgm(path, hits, width, height):
+    """The hit distances as a 16-bit binary PGM (nearest white, misses
+    black), top row first -- the headless stand-in for the viewer's window."""
+    t = hits["t"].reshape(height, width)[::-1]
+    ok = t > 0
+    img = np.zeros((height, width), np.uint16)
+    if ok.any():
+        lo, hi = float(t[ok].min()), float(t[ok].max())
+        img[ok] = (65535 - (t[ok] - lo) / max(hi - lo, 1e-30) * 60000).astype(np.uint16)
+    with open(path, "wb") as fh:
+        fh.write(b"P5\n%d %d\n65535\n" % (width, height))
+        fh.write(img.astype(">u2").tobytes())
