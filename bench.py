@@ -40,11 +40,15 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["terrain", "city", "batch", "lossy"], default="terrain",
+    ap.add_argument("--workload", choices=["terrain", "city", "batch", "lossy", "raycast"], default="terrain",
                     help="terrain: 2048^2 fBm terrain at depth 12 (the headline); city: 4096^2 terrain + 200,000 "
                          "boxes at depth 15, chunked build with step level 1; batch: 256 voxel-brick chunks of "
                          "depths 7-11 (value noise, 5-40%% fill), batched SSVDAG + CSVDAG; lossy: 2048^2 terrain + "
-                         "5,000 boxes at depth 11, lossy LSVDAG with exact and learned pair proposals")
+                         "5,000 boxes at depth 11, lossy LSVDAG with exact and learned pair proposals; raycast: "
+                         "1920x1080 frames of the depth-12 terrain's encoded SSVDAG, the viewer's DDA traversal")
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--pixel-tolerance", type=float, default=1.0)
     ap.add_argument("--top-k", type=int, default=256)
     ap.add_argument("--train-pairs", type=int, default=2000000)
     ap.add_argument("--epochs", type=int, default=2)
@@ -685,9 +689,140 @@ def run_lossy(args, rank, local, world):
     }
 
 
+# the four views of the ray-casting workload (eye, target), unit-cube coordinates
+RAY_VIEWS = [((1.1, 0.55, 1.2), (0.5, 0.12, 0.5)), ((-0.5, 0.6, 0.3), (0.6, 0.1, 0.55)),
+             ((0.5, 1.6, 0.5001), (0.5, 0.0, 0.5)), ((0.2, 0.32, 0.25), (0.8, 0.12, 0.9))]
+
+
+def raycast_scene(args, sv, local, path):
+    """The depth-12 terrain built on the GPU to an SSVDAG, written as a
+    .ssvdag file (host encoder) and read back as arrays."""
+    o = sv.Octree(device=local)
+    o.upload_triangles(sv.terrain(args.grid, 8, 0.3, args.seed))
+    o.buildSVO(args.levels)
+    o.toDAG()
+    o.initChildLevels()
+    o.toSDAG()
+    sv.write_encoded(path, "ssvdag", o.pool(), o.stats()["n_nodes"], 3)
+    o.close()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+
+    return oracle_py.read_ssvdag(path)
+
+
+def run_raycast(args, rank, local, world):
+    """Ray casting of the terrain's encoded SSVDAG: K frames of each of four
+    views at 1920x1080 with the viewer's defaults (60-degree field of view,
+    300 iterations, pixel tolerance 1), hit records written to HBM."""
+    import numpy as np
+    import torch
+
+    import svdag_gb300 as sv
+
+    torch.cuda.set_device(local)
+    with tempfile.TemporaryDirectory() as td:
+        f = raycast_scene(args, sv, local, os.path.join(td, "t.ssvdag"))
+    L = args.levels
+    W, H = args.width, args.height
+    cams = [sv.camera(e, t, W, H, L, pixel_tolerance=args.pixel_tolerance) for e, t in RAY_VIEWS]
+    S = sv.Ssvdag(f)
+    npix = W * H
+    buf = torch.empty(npix * 32, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(max(args.warmup, 0)):
+        for c in cams:
+            S.raycast_device(c, buf.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    clocks.mark()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in cams]
+    per_view = [0.0] * len(cams)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for i, c in enumerate(cams):
+            ev[i][0].record(stream)
+            S.raycast_device(c, buf.data_ptr(), stream.cuda_stream)
+            ev[i][1].record(stream)
+            torch.cuda.synchronize()
+            per_view[i] += ev[i][0].elapsed_time(ev[i][1])
+    torch.cuda.synchronize()
+    wall_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    clk = clocks.stop()
+    kernel_ms = sum(per_view) / args.steps  # one step = one frame of each view
+    hits = [S.raycast(c) for c in cams]
+    stats = [{"hit_frac": float((h["t"] > 0).mean()), "mean_iterations": float(h["iterations"].mean()),
+              "device_ms": per_view[i] / args.steps} for i, h in enumerate(hits)]
+    # e2e: host hit buffers (device -> host copy of every frame's records)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        for c in cams:
+            S.raycast(c)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps // 2)
+    S.close()
+    rays = npix * len(cams)
+    iters = sum(float(h["iterations"].sum()) for h in hits)
+    # algorithmic bytes per frame: the 32-byte hit records written once; the
+    # node reads are cache-resident re-reads of a few MB of encoded nodes
+    alg = 32.0 * rays
+    peak, src = peaks()
+    res = {
+        "metric": METRIC, "value": rays / (kernel_ms / 1e3) / 1e6, "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 rays, u16/u8 nodes", "data": "synthetic",
+        "config": {"workload": "raycast: %dx%d frames of 4 views of the %dx%d terrain's SSVDAG at depth %d "
+                               "(.ssvdag: %d inner words, %d leaf bytes), viewer defaults: 60-degree fov, 300 "
+                               "iterations, pixel tolerance %g" % (W, H, args.grid, args.grid, L, f["inner"].size,
+                                                                   f["leaves"].size, args.pixel_tolerance),
+                   "views": stats, "dda_iterations_per_s": iters / (kernel_ms / 1e3),
+                   "l2": "encoded SSVDAG (%d MB) and hit buffer (%d MB) are L2-resident across frames" % (
+                       (2 * f["inner"].size + f["leaves"].size) // 10**6, npix * 32 // 10**6),
+                   "wall_ms_per_step": wall_ms, "parallelism": "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": alg / (kernel_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg / (kernel_ms / 1e3) / 1e9 / peak, "traffic": None,
+                     "note": "latency-bound pointer chase (one ray per thread, %.1f DDA iterations per ray); "
+                             "peak %s" % (iters / rays, src)},
+        "clocks": clk, "gpu_launches": len(cams),
+        "e2e": {"value": rays / (e2e_ms / 1e3) / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 32 * rays},
+    }
+    if not args.no_cpu_baseline:
+        res["cpu_baseline"] = raycast_cpu(args, f, cams)
+    return res
+
+
+def raycast_cpu(args, f, cams, frac=4):
+    """The oracle's restated traversal on all host cores, each view at 1/frac
+    of the resolution per axis with the full-size projection factor (a
+    subsample of the same rays' directions)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+
+    t = 0.0
+    rays = 0
+    for c in cams:
+        s = dict(c, width=c["width"] // frac, height=c["height"] // frac)
+        t0 = time.perf_counter()
+        oracle_py.ssvdag_raycast(f, s)
+        t += time.perf_counter() - t0
+        rays += s["width"] * s["height"]
+    return {"value": rays / t / 1e6, "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "the 4 views at %dx%d (1/%d of the rays per view), OpenMP over all cores" % (
+                cams[0]["width"] // frac, cams[0]["height"] // frac, frac * frac)}
+
+
 def main():
     args = parse()
     rank, local, world = rank_info()
+    if args.workload == "raycast" and args.impl != "reference":
+        res = run_raycast(args, rank, local, world)
+        if rank == 0:
+            print(json.dumps(res))
+        return
     if args.workload in ("batch", "lossy") and args.impl != "reference":
         res = (run_batch if args.workload == "batch" else run_lossy)(args, rank, local, world)
         if rank == 0:
