@@ -72,7 +72,7 @@ def build_host():
     hdrs = [os.path.join(PKG, "host", h) for h in os.listdir(os.path.join(PKG, "host")) if h.endswith((".h", ".hpp"))]
     out = os.path.join(LIB, "libsvdag_host.so")
     if not _newer(out, srcs + hdrs + [os.path.join(LIB, "libsvdag_gpu.so")]):
-        _run([CXX, "-O2", "-std=gnu++17", "-fPIC", "-shared", "-ffp-contract=off", "-I", INC,
+        _run([CXX, "-O2", "-std=gnu++17", "-fPIC", "-shared", "-pthread", "-ffp-contract=off", "-I", INC,
               "-I", os.path.join(PKG, "host")] + srcs + ["-L", LIB, "-lsvdag_gpu", "-Wl,-rpath,$ORIGIN", "-o", out])
     return out
 
@@ -84,7 +84,7 @@ def build_cli(gpu_lib):
     hdrs = [os.path.join(PKG, "host", h) for h in os.listdir(os.path.join(PKG, "host")) if h.endswith((".h", ".hpp"))]
     out = os.path.join(PKG, "bin", "svbuilder")
     if not _newer(out, srcs + hdrs + [gpu_lib]):
-        _run([CXX, "-O2", "-std=gnu++17", "-ffp-contract=off", "-I", INC, "-I", os.path.join(PKG, "host")] + srcs +
+        _run([CXX, "-O2", "-std=gnu++17", "-pthread", "-ffp-contract=off", "-I", INC, "-I", os.path.join(PKG, "host")] + srcs +
              ["-L", LIB, "-lsvdag_gpu", "-Wl,-rpath,$ORIGIN/../lib", "-o", out])
     return out
 

@@ -15,8 +15,13 @@ class Scene {
   // Scene::loadObj (scene.cpp:51-250): `v` lines (all of them grow the
   // bounding box, referenced or not), `f` lines as "%d//%d" tokens with
   // negative indices relative to the end; a binary cache "<file>.bincache"
-  // is read when present and written after an ASCII parse.
-  bool loadObj(const std::string& path, bool tryLoadBinCache = true, bool writeBinCache = true);
+  // is read when present and written after an ASCII parse.  The ASCII parse
+  // runs on `threads` host threads (0: all cores): the file is cut at line
+  // starts, each piece parsed on its own, and vertex numbering and negative
+  // indices resolved from the pieces' vertex counts, so the result is the
+  // same for every thread count.
+  bool loadObj(const std::string& path, bool tryLoadBinCache = true, bool writeBinCache = true,
+               unsigned threads = 0);
   // Triangle soup (Scene::buildTriVector, scene.cpp:394-416): 9 floats per
   // triangle, triangles with an out-of-range vertex index dropped.
   const std::vector<float>& triangles() const { return tris_; }
@@ -29,7 +34,7 @@ class Scene {
  private:
   bool loadBinCache(const std::string& path);
   bool saveBinCache(const std::string& path) const;
-  void buildTriVector();
+  void buildTriVector(unsigned threads);
   std::vector<float> verts_;                 // xyz per vertex
   std::vector<uint64_t> tri_idx_;            // 3 vertex indices per triangle
   std::vector<uint64_t> tri_nidx_;           // 3 normal indices per triangle (cache layout only)

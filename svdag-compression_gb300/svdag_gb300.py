@@ -135,6 +135,11 @@ HOST_SYMBOLS = {
     "svdag_synth_boxes": (_I, [_VP, _VP, _U64, _VP]),
     "svdag_write_obj": (_I, [ctypes.c_char_p, _VP, _U64, _I]),
     "svdag_write_encoded": (_I, [ctypes.c_char_p, _I, _U32, _VP, _VP, _VP, ctypes.c_float, _U64, _I]),
+    "svdag_scene_load_obj": (_I, [ctypes.c_char_p, _U32, _I, _I, ctypes.POINTER(_VP)]),
+    "svdag_scene_triangle_count": (_U64, [_VP]),
+    "svdag_scene_triangles": (_VP, [_VP]),
+    "svdag_scene_bbox": (_I, [_VP, _VP]),
+    "svdag_scene_free": (None, [_VP]),
 }
 
 FORMATS = {"svdag": 0, "ussvdag": 1, "ssvdag": 2}
@@ -709,3 +714,23 @@ def write_depth_pgm(path, hits, width, height):
     with open(path, "wb") as fh:
         fh.write(b"P5\n%d %d\n65535\n" % (width, height))
         fh.write(img.astype(">u2").tobytes())
+
+
+def load_obj(path, threads=0, use_bincache=False, write_bincache=False):
+    """Scene::loadObj on `threads` host threads (0: all cores): the triangle
+    soup (n, 9) float32 and the scene bounding box (6 floats)."""
+    lib = load_host()
+    h = _VP()
+    r = lib.svdag_scene_load_obj(os.fsencode(path), threads, int(use_bincache), int(write_bincache), ctypes.byref(h))
+    if r != 0:
+        raise SvdagError(r, "cannot load %s" % path)
+    try:
+        n = lib.svdag_scene_triangle_count(h)
+        tris = np.zeros((n, 9), np.float32)
+        if n:
+            ctypes.memmove(tris.ctypes.data, lib.svdag_scene_triangles(h), 36 * n)
+        bb = np.zeros(6, np.float32)
+        lib.svdag_scene_bbox(h, bb.ctypes.data)
+    finally:
+        lib.svdag_scene_free(h)
+    return tris, bb
