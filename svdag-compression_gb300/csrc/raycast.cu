@@ -40,7 +40,11 @@ struct SsvdagDev {
 
 namespace {
 
-constexpr int kMaxStack = 32;
+constexpr int kMaxStack = 30;  // one entry per inner level at most (levels <= 30)
+
+#ifndef SVDAG_RAY_MIN_BLOCKS
+#define SVDAG_RAY_MIN_BLOCKS 8
+#endif
 
 struct RayView {
   const uint16_t* inner;
@@ -180,10 +184,21 @@ struct Stack {
   uint32_t n;
 };
 
-__global__ void __launch_bounds__(128) k_raycast(RayView V, svdag_ray_hit* __restrict__ out, uint32_t* __restrict__ bad) {
-  const uint64_t npix = uint64_t(V.width) * V.height;
-  for (uint64_t q = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; q < npix; q += uint64_t(gridDim.x) * blockDim.x) {
-    const uint32_t px = uint32_t(q % V.width), py = uint32_t(q / V.width);
+// Pixels go to threads in 16 x 8 tiles per block, 8 x 4 per warp: rays of
+// one warp start close together and stay in step longer than along a row.
+constexpr int kRayThreads = 128;
+constexpr uint32_t kTileW = 16, kTileH = 8;
+
+__global__ void __launch_bounds__(kRayThreads, SVDAG_RAY_MIN_BLOCKS)
+    k_raycast(RayView V, svdag_ray_hit* __restrict__ out, uint32_t* __restrict__ bad) {
+  const uint32_t tiles_x = (V.width + kTileW - 1) / kTileW;
+  const uint64_t tiles = uint64_t(tiles_x) * ((V.height + kTileH - 1) / kTileH);
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t ox = (warp & 1) * 8 + (lane & 7), oy = (warp >> 1) * 4 + (lane >> 3);
+  for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const uint32_t px = uint32_t(tile % tiles_x) * kTileW + ox, py = uint32_t(tile / tiles_x) * kTileH + oy;
+    if (px >= V.width || py >= V.height) continue;
+    const uint64_t q = uint64_t(py) * V.width + px;
     svdag_ray_hit h{};
     h.node = -1;
     // computeCameraRay
@@ -478,8 +493,10 @@ extern "C" int svdag_ssvdag_raycast(svdag_ssvdag* h, const svdag_camera* cam, vo
       tmp = svdag::DBuf<svdag_ray_hit>(npix, st);
       dst = tmp.get();
     }
-    const unsigned grid = unsigned(std::min<uint64_t>((npix + 127) / 128, 152ull * 32));
-    svdag::k_raycast<<<grid, 128, 0, st>>>(V, dst, d_bad.get());
+    const uint64_t tiles = uint64_t((cam->width + svdag::kTileW - 1) / svdag::kTileW) *
+                           ((cam->height + svdag::kTileH - 1) / svdag::kTileH);
+    const unsigned grid = unsigned(std::min<uint64_t>(tiles, 152ull * 32));
+    svdag::k_raycast<<<grid, svdag::kRayThreads, 0, st>>>(V, dst, d_bad.get());
     SVDAG_CUDA(cudaPeekAtLastError());
     if (!device_buffer)
       SVDAG_CUDA(cudaMemcpyAsync(hits, dst, sizeof(svdag_ray_hit) * npix, cudaMemcpyDeviceToHost, st));
