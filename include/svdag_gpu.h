@@ -190,6 +190,20 @@ typedef struct svdag_ray_hit {
 int svdag_ssvdag_raycast(svdag_ssvdag* s, const svdag_camera* cam, void* stream, svdag_ray_hit* hits,
                          int device_buffer);
 
+/* GeomOctree::hiddenGeometryFloodfill (src/symvox/geom_octree_extension.cpp:
+ * 1651-1891) on an SVO (state SVO, before toDAG): each node's outsideMask --
+ * bit c set when child slot c is an empty cell face-connected through empty
+ * cells to the start cell (slot 7 of the deepest node on the child-7 path),
+ * a set voxel sharing a face with such a cell, or a child node with any
+ * outside bit.  n_outside_empty counts the empty cells reached (the start
+ * included), n_outside_surface the set voxels marked; either may be NULL.
+ * SVDAG_ERR_INVALID_STATE when the start cell is set (the reference aborts)
+ * or the octree is not an SVO.  The masks are read per level with
+ * svdag_download_outside_masks (one byte per node) while the SVO is
+ * unchanged; toDAG and the other reductions do not use them. */
+int svdag_flood_fill(svdag_ctx* ctx, uint64_t* n_outside_empty, uint64_t* n_outside_surface);
+int svdag_download_outside_masks(svdag_ctx* ctx, uint32_t level, uint8_t* masks);
+
 /* Per-kernel device timing (no counterpart in the reference, whose Stats
  * hold phase times only, src/symvox/geom_octree.hpp:54).  While enabled,
  * every kernel launch of the context is bracketed by CUDA events on its

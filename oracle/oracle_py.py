@@ -40,6 +40,8 @@ _SIGS = {
     "ora_ssvdag_traverse": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, _VP, _U64, _VP]),
     "ora_ssvdag_raycast": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, _VP, _VP, _U32, _U32,
                                 _U32, _U32, ctypes.c_float, ctypes.c_float, ctypes.c_float, _VP]),
+    "ora_flood_fill": (_I, [_VP, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
+    "ora_get_outside": (_I, [_VP, _U32, _VP]),
     "ora_to_dag": (_I, [_VP]),
     "ora_to_sdag": (_I, [_VP]),
     "ora_init_child_levels": (_I, [_VP]),
@@ -105,6 +107,22 @@ class OracleOctree:
         m = ctypes.c_uint64()
         assert self.L.ora_lossy_exact(self.h, min_above, max_above, max_error, ctypes.byref(m)) == 0
         return m.value
+
+    def hiddenGeometryFloodfill(self):
+        """Outside masks of the SVO (list of u8 arrays, one per level) and the
+        counts (empty cells reached, surface voxels marked); None when the
+        start corner cell is set."""
+        e, s = ctypes.c_uint64(), ctypes.c_uint64()
+        r = self.L.ora_flood_fill(self.h, ctypes.byref(e), ctypes.byref(s))
+        if r == -3:
+            return None
+        assert r == 0, r
+        masks = []
+        for l in range(self.stats()["levels"]):
+            m = np.zeros(self.L.ora_level_count(self.h, l), np.uint8)
+            self.L.ora_get_outside(self.h, l, m.ctypes.data)
+            masks.append(m)
+        return masks, e.value, s.value
 
     def toDAG(self):
         assert self.L.ora_to_dag(self.h) == 0

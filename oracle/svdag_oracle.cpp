@@ -176,6 +176,7 @@ struct ora_octree {
   double root_side = 0;
   uint64_t n_voxels = 0, n_nodes = 0;
   ora_stats st{};
+  std::vector<std::vector<uint8_t>> outside;  // outsideMask per node after the flood fill
 };
 
 namespace {
@@ -588,9 +589,153 @@ void build_dag_chunked(ora_octree* o, const float* tris, uint64_t n_tris, const 
   to_dag(o);
 }
 
+// GeomOctree::hiddenGeometryFloodfill (src/symvox/geom_octree_extension.cpp:
+// 1651-1891) restated.  A traversal node is a cell: (depth, node of the
+// level above, child slot); its parent cell follows from the SVO's single
+// parent per node.  Neighbours are the leaf cells sharing a face
+// (getNeighbourGrtrEqSz + getNeighboursSmSz, :1702-1775); the fill starts at
+// the deepest cell on the child-7 path (:1788-1814) and, from every cell it
+// reaches, marks each neighbour outside and continues through the empty ones
+// (:1822-1843); then non-empty children with any outside bit are marked
+// bottom-up (:1846-1860).
+struct FloodFill {
+  ora_octree* o;
+  std::vector<std::vector<uint32_t>> par;   // parent node of each node
+  std::vector<std::vector<uint8_t>> slot;   // its child slot in the parent
+  struct Cell {
+    int level;       // depth (0 = the root itself)
+    uint32_t pidx;   // node at level - 1
+    int c;           // child slot
+    bool valid;
+  };
+  static Cell null_cell() { return Cell{-1, 0, 0, false}; }
+  // getChildIndexForDirection (:1690-1699): directions NX NY NZ PX PY PZ
+  static int dir_child(int dir, int i) {
+    int c = i;
+    if (dir % 3 == 1) c = i + 2 * (i / 2);
+    else if (dir % 3 == 2) c = i * 2;
+    if (dir == 3) c += 4;
+    else if (dir == 4) c += 2;
+    else if (dir == 5) c += 1;
+    return c;
+  }
+  const Node& node_of(const Cell& t) const {  // getNode (:1678-1683)
+    if (t.level == 0) return o->d[0][0];
+    return o->d[t.level][o->d[t.level - 1][t.pidx].ch[t.c]];
+  }
+  uint32_t node_id(const Cell& t) const { return t.level == 0 ? 0 : o->d[t.level - 1][t.pidx].ch[t.c]; }
+  bool is_leaf(const Cell& t) const {  // isLeaf (:1686-1692)
+    if (uint32_t(t.level) == o->levels) return true;
+    const Node& p = o->d[t.level - 1][t.pidx];
+    if (p.has_ptr(t.c)) return node_of(t).mask == 0;
+    return true;
+  }
+  Cell parent(const Cell& t) const {
+    if (t.level <= 1) return Cell{0, 0, 0, true};
+    return Cell{t.level - 1, par[t.level - 1][t.pidx], slot[t.level - 1][t.pidx], true};
+  }
+  Cell neighbour_ge(const Cell& t, int dir) const {  // getNeighbourGrtrEqSz
+    if (t.level == 0) return null_cell();
+    const int opp = (dir + 3) % 6;
+    for (int i = 0; i < 4; ++i)
+      if (t.c == dir_child(opp, i)) return Cell{t.level, t.pidx, dir_child(dir, i), true};
+    const Cell pn = neighbour_ge(parent(t), dir);
+    if (!pn.valid || is_leaf(pn)) return pn;
+    const uint32_t pid = node_id(pn);
+    for (int i = 0; i < 4; ++i)
+      if (t.c == dir_child(dir, i)) return Cell{pn.level + 1, pid, dir_child(opp, i), true};
+    return null_cell();
+  }
+  void neighbours_small(const Cell& nb, int dir, std::vector<Cell>& out) const {  // getNeighboursSmSz
+    std::vector<Cell> st;
+    if (nb.valid) st.push_back(nb);
+    const int opp = (dir + 3) % 6;
+    while (!st.empty()) {
+      const Cell can = st.back();
+      st.pop_back();
+      if (is_leaf(can)) {
+        out.push_back(can);
+      } else {
+        const uint32_t id = node_id(can);
+        for (int i = 0; i < 4; ++i) st.push_back(Cell{can.level + 1, id, dir_child(opp, i), true});
+      }
+    }
+  }
+  bool bit(const Cell& t) const { return (o->outside[t.level - 1][t.pidx] >> t.c) & 1u; }
+  void set_bit(const Cell& t) { o->outside[t.level - 1][t.pidx] |= uint8_t(1u << t.c); }
+
+  int run(uint64_t* n_empty, uint64_t* n_surface) {
+    const uint32_t L = o->levels;
+    par.assign(L, {});
+    slot.assign(L, {});
+    o->outside.assign(L, {});
+    for (uint32_t l = 0; l < L; ++l) {
+      par[l].assign(o->d[l].size(), 0);
+      slot[l].assign(o->d[l].size(), 0);
+      o->outside[l].assign(o->d[l].size(), 0);
+    }
+    for (uint32_t l = 0; l + 1 < L; ++l)
+      for (uint32_t i = 0; i < o->d[l].size(); ++i)
+        for (int c = 0; c < 8; ++c)
+          if (o->d[l][i].has_ptr(c)) {
+            par[l + 1][o->d[l][i].ch[c]] = i;
+            slot[l + 1][o->d[l][i].ch[c]] = uint8_t(c);
+          }
+    // the start cell: slot 7 of the deepest node on the child-7 path
+    Cell start{1, 0, 7, true};
+    uint32_t cur = 0;
+    for (uint32_t lev = 0; lev < L; ++lev) {
+      start = Cell{int(lev) + 1, cur, 7, true};
+      if (!o->d[lev][cur].has_ptr(7)) break;
+      cur = o->d[lev][cur].ch[7];
+    }
+    if (o->d[start.level - 1][start.pidx].has_child(7)) return -3;  // the reference aborts here
+    std::vector<Cell> stack{start};
+    set_bit(start);
+    uint64_t empty = 1, surface = 0;
+    std::vector<Cell> nbs;
+    while (!stack.empty()) {
+      const Cell t = stack.back();
+      stack.pop_back();
+      nbs.clear();
+      for (int dir = 0; dir < 6; ++dir) neighbours_small(neighbour_ge(t, dir), dir, nbs);
+      for (const Cell& nb : nbs) {
+        if (bit(nb)) continue;
+        set_bit(nb);
+        if (!o->d[nb.level - 1][nb.pidx].has_child(nb.c)) {
+          stack.push_back(nb);
+          ++empty;
+        } else {
+          ++surface;
+        }
+      }
+    }
+    for (int lev = int(L) - 2; lev >= 0; --lev)
+      for (uint32_t i = 0; i < o->d[lev].size(); ++i)
+        for (int c = 0; c < 8; ++c)
+          if (o->d[lev][i].has_ptr(c) && o->outside[lev + 1][o->d[lev][i].ch[c]] != 0)
+            o->outside[lev][i] |= uint8_t(1u << c);
+    if (n_empty) *n_empty = empty;
+    if (n_surface) *n_surface = surface;
+    return 0;
+  }
+};
+
 }  // namespace
 
 extern "C" {
+
+int ora_flood_fill(ora_octree* o, uint64_t* n_empty, uint64_t* n_surface) {
+  if (!o || o->state != 1 || o->levels < 1) return -1;
+  FloodFill f{o, {}, {}};
+  return f.run(n_empty, n_surface);
+}
+
+int ora_get_outside(const ora_octree* o, uint32_t level, uint8_t* out) {
+  if (!o || level >= o->outside.size()) return -1;
+  std::memcpy(out, o->outside[level].data(), o->outside[level].size());
+  return 0;
+}
 
 ora_octree* ora_create(void) { return new ora_octree(); }
 void ora_destroy(ora_octree* o) { delete o; }

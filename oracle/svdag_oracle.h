@@ -53,6 +53,10 @@ int ora_ssvdag_raycast(const uint16_t* inner, uint64_t n_inner, const uint8_t* l
                        float root_side, const float view_inv[16], const float proj_inv[16], uint32_t width,
                        uint32_t height, uint32_t max_iters, uint32_t draw_level, float projection_factor,
                        float t_min, float t_max, void* hits);
+/* GeomOctree::hiddenGeometryFloodfill (geom_octree_extension.cpp:1651-1891)
+ * on an SVO: outside masks per node; -3 when the start corner cell is set */
+int ora_flood_fill(ora_octree* o, uint64_t* n_empty, uint64_t* n_surface);
+int ora_get_outside(const ora_octree* o, uint32_t level, uint8_t* out);
 int ora_to_dag(ora_octree* o);                 /* geom_octree.cpp:462-548 */
 int ora_to_sdag(ora_octree* o);                /* geom_octree.cpp:551-697 (greedy, symmetry on) */
 int ora_init_child_levels(ora_octree* o);      /* geom_octree_extension.cpp:21-30 */

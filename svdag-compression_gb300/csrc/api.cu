@@ -55,6 +55,7 @@ void copy_level(const Ctx& src, svdag::Level& dst, const svdag::Level& s, cudaSt
   cp(dst.ch, s.ch);
   cp(dst.inv, s.inv);
   cp(dst.clev, s.clev);
+  cp(dst.outm, s.outm);
   (void)src;
 }
 
@@ -191,7 +192,10 @@ int svdag_build_dag(svdag_ctx* h, uint32_t levels, uint32_t step_level, const do
 }
 
 int svdag_reduce_dag(svdag_ctx* h) {
-  return guarded(h, [&](Ctx& c) { c.st.dag_ms = timed(c, [&] { svdag::phase_reduce_dag(c); }); });
+  return guarded(h, [&](Ctx& c) {
+    c.st.dag_ms = timed(c, [&] { svdag::phase_reduce_dag(c); });
+    for (auto& L : c.lev) L.outm.release();  // outside masks belong to the SVO
+  });
 }
 
 int svdag_init_child_levels(svdag_ctx* h) {

@@ -17,6 +17,7 @@ namespace svdag {
 //   clev[8n]    : child levels (CSVDAG only; empty otherwise)
 //   ctr[3n]     : fp64 node centre (SVO build only)
 //   nbox[8n]    : fp32 child-box centres of the node (SVO build only)
+//   outm[n]     : outside mask of the hidden-geometry flood fill (SVO only)
 struct Level {
   uint64_t n = 0;
   DBuf<uint32_t> hdr;
@@ -25,6 +26,7 @@ struct Level {
   DBuf<uint8_t> clev;
   DBuf<double> ctr;
   DBuf<float> nbox;
+  DBuf<uint8_t> outm;
 };
 
 struct Ctx {
@@ -61,6 +63,8 @@ void phase_build_dag(Ctx& c, uint32_t levels, uint32_t step_level, const double 
 void phase_reduce_dag(Ctx& c);
 void phase_reduce_sdag(Ctx& c);
 void phase_cross_level_merge(Ctx& c);
+// GeomOctree::hiddenGeometryFloodfill: outside masks of an SVO (floodfill.cu).
+void phase_flood_fill(Ctx& c, uint64_t* n_empty, uint64_t* n_surface);
 // toDAG with every temporary in caller-provided device scratch (no allocation).
 void phase_reduce_dag_scratch(Ctx& c, uint8_t* scratch, uint64_t capacity);
 

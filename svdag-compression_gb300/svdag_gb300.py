@@ -77,6 +77,8 @@ GPU_SYMBOLS = {
     "svdag_profile_enable": (_I, [_VP, _I]),
     "svdag_profile_report": (_I, [_VP, ctypes.c_char_p, _U64]),
     "svdag_reduce_dag_noalloc": (_I, [_VP]),
+    "svdag_flood_fill": (_I, [_VP, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
+    "svdag_download_outside_masks": (_I, [_VP, _U32, _VP]),
     "svdag_synth_noise_bricks": (_I, [_VP, _U32, _U64, ctypes.c_double, _VP, ctypes.POINTER(ctypes.c_float)]),
     "svdag_import_bricks": (_I, [_VP, _U32, _VP]),
     "svdag_batch_create": (_I, [ctypes.POINTER(_VP), _I, _VP]),
@@ -328,6 +330,22 @@ class Octree:
         """Node pools of a voxel-brick chunk (a torch uint8 CUDA tensor of
         8^(depth-1) Morton-ordered bricks), DAG state."""
         self._check(self._lib.svdag_import_bricks(self._h, depth, ctypes.c_void_p(bricks.data_ptr())))
+
+    def hiddenGeometryFloodfill(self):
+        """Outside masks of the SVO (GeomOctree::hiddenGeometryFloodfill):
+        one u8 array per level, and the counts (empty cells reached, surface
+        voxels marked)."""
+        e, s = _U64(), _U64()
+        self._check(self._lib.svdag_flood_fill(self._h, ctypes.byref(e), ctypes.byref(s)))
+        masks = []
+        for l in range(self.stats()["levels"]):
+            n = _U64()
+            self._check(self._lib.svdag_level_count(self._h, l, ctypes.byref(n)))
+            m = np.zeros(n.value, np.uint8)
+            if n.value:
+                self._check(self._lib.svdag_download_outside_masks(self._h, l, m.ctypes.data))
+            masks.append(m)
+        return masks, e.value, s.value
 
     def toDAG(self):
         self._check(self._lib.svdag_reduce_dag(self._h))
