@@ -63,6 +63,14 @@ unsigned GeomOctree::mergeAcrossAllLevels() {
   return unsigned(getStats().nCrossLevelMerged);
 }
 
+uint64_t GeomOctree::hiddenGeometryFloodfill() {
+  uint64_t empty = 0, surface = 0;
+  check(svdag_flood_fill(ctx_, &empty, &surface));
+  invalidate();
+  outside_ = true;
+  return empty ? empty - 1 : 0;
+}
+
 void GeomOctree::initChildLevels() {
   check(svdag_init_child_levels(ctx_));
   invalidate();
@@ -114,6 +122,11 @@ const NodeData& GeomOctree::getNodeData() const {
       std::memcpy(d.children, &ch[8 * i], 32);
       for (int c = 0; c < 8; ++c) d.childLevels[c] = (cl[8 * i + c] == 0xFF) ? 0xFFFFFFFFu : cl[8 * i + c];
       d.invariantBitmask = inv[i];
+    }
+    if (outside_ && n) {
+      std::vector<uint8_t> om(n);
+      check(svdag_download_outside_masks(ctx_, l, om.data()));
+      for (uint64_t i = 0; i < n; ++i) out[i].outsideMask = om[i];
     }
   }
   cached_ = true;

@@ -68,6 +68,11 @@ class GeomOctree {
   void toSDAG();
   unsigned mergeAcrossAllLevels();
   void initChildLevels();
+  // hiddenGeometryFloodfill (geom_octree_extension.cpp:1651-1891) on the SVO:
+  // fills each node's outsideMask (read through getNodeData until the next
+  // build step); returns the reference's count of empty leaves reached
+  // besides the start cell.  Throws when the start corner cell is set.
+  uint64_t hiddenGeometryFloodfill();
   // GeomOctree(NodeData, bbox, rootSide, levels, stats) (geom_octree.cpp:49-60)
   void importDAG(const NodeData& data, const float bbox[6], double rootSide, uint64_t nVoxels);
 
@@ -86,7 +91,11 @@ class GeomOctree {
 
  private:
   void check(int status) const;
-  void invalidate() { cached_ = false; }
+  void invalidate() {
+    cached_ = false;
+    outside_ = false;
+  }
+  bool outside_ = false;  // outside masks of the current SVO are on the device
   Scene* scene_ = nullptr;
   svdag_ctx* ctx_ = nullptr;
   float bbox_[6] = {0, 0, 0, 0, 0, 0};

@@ -88,6 +88,10 @@ int main(int argc, char** argv) {
   }
   std::printf("Lossy: %d, Cross-level: %d, Hidden geom: %d\n", lossy, multiLevel, hidden);
   if (lossy || hidden) {
+    // the MCL clustering of --lossy is an external program; of --hidden-geometry
+    // the flood fill is GeomOctree::hiddenGeometryFloodfill, but the
+    // reference's hidden-geometry DAG reduction does not terminate once a
+    // correspondence stays unresolved (geom_octree_extension.cpp:2059-2070)
     std::printf("%s is not available in this build\n", lossy ? "--lossy" : "--hidden-geometry");
     return 2;
   }
