@@ -177,19 +177,21 @@ __device__ __forceinline__ T warp_incl_scan(T v) {
 
 // Block-wide exclusive scan of one value per thread; returns the block total
 // in *total (all threads).
+// Any block size that is a multiple of 32 (up to 1024).
 template <class T>
 __device__ __forceinline__ T block_excl_scan(T v, T* total) {
-  __shared__ T warp_sums[kScanThreads / 32];
+  __shared__ T warp_sums[32];
   __shared__ T tot;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int nw = int(blockDim.x >> 5);
   T inc = warp_incl_scan(v);
   if (lane == 31) warp_sums[w] = inc;
   __syncthreads();
   if (w == 0) {
-    T s = (lane < kScanThreads / 32) ? warp_sums[lane] : T(0);
+    T s = (lane < nw) ? warp_sums[lane] : T(0);
     T si = warp_incl_scan(s);
-    if (lane < kScanThreads / 32) warp_sums[lane] = si - s;
-    if (lane == kScanThreads / 32 - 1) tot = si;
+    if (lane < nw) warp_sums[lane] = si - s;
+    if (lane == nw - 1) tot = si;
   }
   __syncthreads();
   T excl = warp_sums[w] + inc - v;

@@ -453,6 +453,37 @@ SAT_HD void pair_plane(Pair32& P, float h) {
   P.nh = fmul(fadd(fadd(fabsf_(P.n[0]), fabsf_(P.n[1])), fabsf_(P.n[2])), h);
 }
 
+// Edge vectors and plane constants of a pair (only the full test uses them).
+SAT_HD void pair_edges(Pair32& P) {
+  const float* t = P.t;
+  for (int q = 0; q < 3; ++q) {
+    P.e[0][q] = fsub(t[3 + q], t[q]);
+    P.e[1][q] = fsub(t[6 + q], t[3 + q]);
+    P.e[2][q] = fsub(t[q], t[6 + q]);
+    for (int j = 0; j < 3; ++j) P.ae[j][q] = fabsf_(P.e[j][q]);
+  }
+  pair_plane(P, P.h);
+}
+
+// Triangle and node data of a pair (no edges, no slab classification).
+SAT_HD void pair_core(const float t[9], const float* tp, const double* c, const NodeBoxes& nb, double k,
+                      Pair32& P) {
+  P.tp = tp;
+  bool ok = nb.ok != 0.f;
+  for (int i = 0; i < 9; ++i) {
+    P.t[i] = t[i];
+    ok = ok && (fabsf_(t[i]) < 1.0e18f);  // also false for NaN
+  }
+  P.nb = nb;
+  P.h = float(k);
+  P.fast = ok;
+  P.c = c;
+  P.k = k;
+  P.slab = 0;
+  P.tang = 0;
+  P.flat = 0;
+}
+
 // Triangle, node and edge data of a pair (no slab classification).
 SAT_HD void pair_basic(const float t[9], const float* tp, const double* c, const NodeBoxes& nb, double k,
                        Pair32& P) {

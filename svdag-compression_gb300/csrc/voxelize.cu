@@ -51,10 +51,18 @@ __host__ __device__ __forceinline__ double child_half_side(double root_side, uin
 //      full certified test.
 // Then each pair publishes its hit mask: OR into the node mask, first-pair
 // index per created child, and the mask for the next frontier.
-constexpr int kExpandThreads = 256;
+// 192 threads and 4 resident blocks per SM (24 warps, 85 registers) measured
+// fastest among 128-256 threads x 2-6 blocks on the depth-12 terrain: the
+// kernel is latency bound, and more, smaller blocks keep warps issuing
+// across the tile barriers despite a few spilled registers.
+#ifndef SVDAG_EXPAND_THREADS
+#define SVDAG_EXPAND_THREADS 192
+#endif
+constexpr int kExpandThreads = SVDAG_EXPAND_THREADS;
+static_assert(kExpandThreads % 32 == 0 && kExpandThreads <= 256, "tile: whole warps, static shared memory <= 48 KB");
 
 #ifndef SVDAG_EXPAND_MIN_BLOCKS
-#define SVDAG_EXPAND_MIN_BLOCKS 1
+#define SVDAG_EXPAND_MIN_BLOCKS 4
 #endif
 __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_expand(VoxParams P, const float* __restrict__ tris,
                                                            const uint32_t* __restrict__ f_tri,
@@ -97,32 +105,36 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
       nb.chi[0] = a.x; nb.chi[1] = a.y; nb.chi[2] = a.z; nb.chi[3] = a.w;
       nb.chi[4] = b.x; nb.chi[5] = b.y; nb.clo = b.z; nb.ok = b.w;
       sat::Pair32 PP;
-      sat::pair_setup(tri, tp, ctr + 3ull * node, nb, k, PP);
+      sat::pair_core(tri, tp, ctr + 3ull * node, nb, k, PP);
+      sat::pair_slabs(PP);
       uint32_t full = 0;
       for (int ci = 7; ci >= 0; --ci) {
         const int f = sat::child_fast(PP, ci);
         if (f == 1) hits |= 1u << ci;
         else if (f == 2) full |= 1u << ci;
       }
-      if (full) {  // this pair's undecided children in consecutive queue slots
+      s_node[tid] = node;
+      if (full) {
+        // this pair's undecided children in consecutive queue slots, and the
+        // pair data the full test reads (pairs the slabs decide skip both)
         uint32_t slot = atomicAdd(&s_qn, uint32_t(__popc(full)));
         for (uint32_t m = full; m; m &= m - 1) s_queue[slot++] = uint16_t((tid << 3) | (__ffs(m) - 1));
+        sat::pair_edges(PP);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) s_e[j][tid] = PP.e[j / 3][j % 3];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) s_t[j][tid] = tri[j];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) { s_nb[j][tid] = nb.chi[j]; s_vmax[j][tid] = PP.vmax[j]; }
+        s_nb[6][tid] = nb.clo;
+        s_nb[7][tid] = nb.ok;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) { s_pl[j][tid] = PP.n[j]; s_pl[3 + j][tid] = PP.sn[j]; }
+        s_pl[6][tid] = PP.nh;
+        s_tri[tid] = t;
+        // slab classes, tangency, axis-aligned triangle, fp32 path
+        s_slab[tid] = PP.slab | (PP.tang << 16) | (PP.flat << 24) | (PP.fast ? 0x80000000u : 0u);
       }
-#pragma unroll
-      for (int j = 0; j < 9; ++j) s_e[j][tid] = PP.e[j / 3][j % 3];
-#pragma unroll
-      for (int j = 0; j < 9; ++j) s_t[j][tid] = tri[j];
-#pragma unroll
-      for (int j = 0; j < 6; ++j) { s_nb[j][tid] = nb.chi[j]; s_vmax[j][tid] = PP.vmax[j]; }
-      s_nb[6][tid] = nb.clo;
-      s_nb[7][tid] = nb.ok;
-#pragma unroll
-      for (int j = 0; j < 3; ++j) { s_pl[j][tid] = PP.n[j]; s_pl[3 + j][tid] = PP.sn[j]; }
-      s_pl[6][tid] = PP.nh;
-      s_tri[tid] = t;
-      s_node[tid] = node;
-      // slab classes, tangency, axis-aligned triangle, fp32 path
-      s_slab[tid] = PP.slab | (PP.tang << 16) | (PP.flat << 24) | (PP.fast ? 0x80000000u : 0u);
     }
     s_hits[tid] = hits;
     __syncthreads();
@@ -297,8 +309,8 @@ __global__ void k_assign_children(const uint32_t* __restrict__ firstq, uint64_t 
   }
 }
 
-// Next frontier in (pair, child ascending) order, one 256-pair tile of the
-// expansion per block: a block scan of the hit counts plus the tile's offset.
+// Next frontier in (pair, child ascending) order, one tile of the expansion
+// per block: a block scan of the hit counts plus the tile's offset.
 __global__ void __launch_bounds__(kExpandThreads) k_emit_frontier(const uint32_t* __restrict__ f_tri,
                                                                   const uint32_t* __restrict__ f_node, uint64_t F,
                                                                   const uint8_t* __restrict__ hits,
