@@ -17,6 +17,7 @@ toSDAG and mergeAcrossAllLevels, as restated by the oracle, on a bounded
 sample (the first rows of the same terrain) so the run ends in minutes.
 """
 import argparse
+import ctypes
 import datetime
 import json
 import os
@@ -40,12 +41,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["terrain", "city", "batch", "lossy", "raycast"], default="terrain",
+    ap.add_argument("--workload", choices=["terrain", "city", "batch", "lossy", "raycast", "floodfill"],
+                    default="terrain",
                     help="terrain: 2048^2 fBm terrain at depth 12 (the headline); city: 4096^2 terrain + 200,000 "
                          "boxes at depth 15, chunked build with step level 1; batch: 256 voxel-brick chunks of "
                          "depths 7-11 (value noise, 5-40%% fill), batched SSVDAG + CSVDAG; lossy: 2048^2 terrain + "
                          "5,000 boxes at depth 11, lossy LSVDAG with exact and learned pair proposals; raycast: "
-                         "1920x1080 frames of the depth-12 terrain's encoded SSVDAG, the viewer's DDA traversal")
+                         "1920x1080 frames of the depth-12 terrain's encoded SSVDAG, the viewer's DDA traversal; "
+                         "floodfill: hidden-geometry flood fill of the depth-12 terrain's SVO")
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--pixel-tolerance", type=float, default=1.0)
@@ -175,7 +178,7 @@ R = 36
 # workload (the 12 k_expand launches of one timed step, averaged; per-launch
 # figures in profiles/k_expand_terrain2048_L12_dram.txt).  Valid for the
 # default terrain workload only.
-KERNEL_DRAM_BYTES_PER_LAUNCH = {"k_expand": 564155413}
+KERNEL_DRAM_BYTES_PER_LAUNCH = {"k_expand": 566186453}
 
 
 def model_bytes(info, T):
@@ -334,8 +337,8 @@ def run_ours(args, rank, local, world):
             pairs = info["frontier"][0]
             roof["algorithmic_bytes"] = "B_vox = 36 T + 36 sum_l N_l per build, spread over its %d launches" % args.levels
             roof["note"] = ("k_expand is instruction-issue / latency bound (SAT box tests), not HBM bound: ncu on "
-                            "its two largest launches of terrain 1024 depth 11 shows issue slots 38-51% busy at 16 "
-                            "warps/SM, ALU pipe 35-48%, FMA 9-13%, FP64 <1%, DRAM 3% of peak "
+                            "its two largest launches of terrain 1024 depth 11 shows issue slots 53-63% busy at 23 "
+                            "warps/SM, ALU pipe 45-55%, FMA 14-17%, FP64 <1%, DRAM 3-4% of peak "
                             "(profiles/k_expand_terrain1024_L11.txt)")
             roof["sat"] = {"frontier_pairs_per_s": pairs / (ms / args.steps / 1e3),
                            "child_box_tests_per_s": 8 * pairs / (ms / args.steps / 1e3)}
@@ -815,9 +818,81 @@ def raycast_cpu(args, f, cams, frac=4):
                 cams[0]["width"] // frac, cams[0]["height"] // frac, frac * frac)}
 
 
+def run_floodfill(args, rank, local, world):
+    """Hidden-geometry flood fill (outside masks) of the depth-12 terrain's
+    SVO, K runs on the resident SVO; value = SVO leaf cells (8 per node)
+    per second."""
+    import torch
+
+    import svdag_gb300 as sv
+
+    torch.cuda.set_device(local)
+    o = sv.Octree(device=local)
+    o.upload_triangles(sv.terrain(args.grid, 8, 0.3, args.seed))
+    o.buildSVO(args.levels)
+    lib = o._lib
+    e, s_ = ctypes.c_uint64(), ctypes.c_uint64()
+    for _ in range(max(args.warmup, 0)):
+        assert lib.svdag_flood_fill(o._h, ctypes.byref(e), ctypes.byref(s_)) == 0
+    nodes = o.stats()["n_nodes_svo"]
+    l0 = o.stats()["gpu_launches"]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    clocks.mark()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        assert lib.svdag_flood_fill(o._h, ctypes.byref(e), ctypes.byref(s_)) == 0
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    clk = clocks.stop()
+    launches = (o.stats()["gpu_launches"] - l0) // max(1, args.steps)
+    # e2e: the fill plus every level's masks copied to the host
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        o.hiddenGeometryFloodfill()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps // 2)
+    cells = 8 * nodes
+    res = {
+        "metric": METRIC, "value": cells / (ms / 1e3) / 1e6, "unit": "Mcells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32 links", "data": "synthetic",
+        "config": {"workload": "floodfill: outside masks of the %dx%d terrain's SVO at depth %d (%d nodes, %d leaf "
+                               "cells)" % (args.grid, args.grid, args.levels, nodes, cells),
+                   "outside_empty_cells": e.value, "outside_surface_voxels": s_.value,
+                   "l2": "SVO pools and union-find array (%d MB) exceed L2" % ((44 * nodes) // 10**6),
+                   "parallelism": "single GPU"},
+        "clocks": clk, "gpu_launches": int(launches),
+        "e2e": {"value": cells / (e2e_ms / 1e3) / 1e6, "unit": "Mcells/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(nodes)},
+    }
+    o.close()
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py
+
+        g = max(65, args.grid // 4)
+        oo = oracle_py.OracleOctree()
+        oo.buildSVO(sv.terrain(g, 8, 0.3, args.seed), args.levels - 2)
+        n_cpu = oo.stats()["n_nodes_svo"]
+        t0 = time.perf_counter()
+        oo.hiddenGeometryFloodfill()
+        t = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": 8 * n_cpu / t / 1e6, "unit": "Mcells/s", "cores": 1, "kind": "port",
+                               "sample": "the %dx%d terrain's SVO at depth %d (%d nodes), the restated reference "
+                                         "traversal on one thread" % (g, g, args.levels - 2, n_cpu)}
+    return res
+
+
 def main():
     args = parse()
     rank, local, world = rank_info()
+    if args.workload == "floodfill" and args.impl != "reference":
+        res = run_floodfill(args, rank, local, world)
+        if rank == 0:
+            print(json.dumps(res))
+        return
     if args.workload == "raycast" and args.impl != "reference":
         res = run_raycast(args, rank, local, world)
         if rank == 0:
