@@ -446,8 +446,11 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
 
     def one():
         assert lib.svdag_upload_triangles(o._h, ptr, T) == 0
-        o.buildSVO(args.levels)
-        o.toDAG()
+        if args.step_level:
+            o.buildDAG(args.levels, args.step_level)
+        else:
+            o.buildSVO(args.levels)
+            o.toDAG()
         o.initChildLevels()
         s = o.clone()
         s.toSDAG()
