@@ -656,8 +656,24 @@ SAT_HD int child_fast(const Pair32& P, int ci) {
   return 2;
 }
 
-// The full test of child `ci` for a child child_fast() left undecided.
-SAT_HD bool child_full(const Pair32& P, int ci, unsigned* fallbacks) {
+// Edge and plane data of a pair, read from the Pair32 itself; the kernel
+// passes a source that reads them from shared memory where they are used.
+struct PairSrc {
+  const Pair32& P;
+  SAT_HD float t(int i) const { return P.t[i]; }
+  SAT_HD float chi(int i) const { return P.nb.chi[i]; }
+  SAT_HD float clo() const { return P.nb.clo; }
+  SAT_HD float vmax(int i) const { return P.vmax[i]; }
+  SAT_HD float e(int j, int q) const { return P.e[j][q]; }
+  SAT_HD float n(int q) const { return P.n[q]; }
+  SAT_HD float sn(int q) const { return P.sn[q]; }
+  SAT_HD float nh() const { return P.nh; }
+};
+
+// The full test of child `ci` for a child child_fast() left undecided (the
+// edges and plane constants from S, everything else from P).
+template <class Src>
+SAT_HD bool child_full_src(const Pair32& P, const Src& S, int ci, unsigned* fallbacks) {
   const bool sx = (ci >> 2) & 1, sy = (ci >> 1) & 1, sz = ci & 1;
   if (!P.fast) {
     if (fallbacks) ++*fallbacks;
@@ -668,16 +684,16 @@ SAT_HD bool child_full(const Pair32& P, int ci, unsigned* fallbacks) {
   const uint32_t cy = (P.slab >> (2 * (2 + sy))) & 3u;
   const uint32_t cz = (P.slab >> (2 * (4 + sz))) & 3u;
   const float h = P.h;
-  const float clo = P.nb.clo;
+  const float clo = S.clo();
   // fp32 vertex offsets v = t - fl32(c); |v_f - (t - c)| <= 1.01 u32 |v_f| + 1.01 clo
   float v[3][3];
-  const float chi[3] = {sx ? P.nb.chi[1] : P.nb.chi[0], sy ? P.nb.chi[3] : P.nb.chi[2], sz ? P.nb.chi[5] : P.nb.chi[4]};
+  const float chi[3] = {S.chi(sx ? 1 : 0), S.chi(sy ? 3 : 2), S.chi(sz ? 5 : 4)};
   for (int i = 0; i < 3; ++i)
-    for (int q = 0; q < 3; ++q) v[i][q] = fsub(P.t[3 * i + q], chi[q]);
+    for (int q = 0; q < 3; ++q) v[i][q] = fsub(S.t(3 * i + q), chi[q]);
   // V >= |t - c| and >= |v_f| over this box
-  float V = sx ? P.vmax[1] : P.vmax[0];
-  V = fmax_(V, sy ? P.vmax[3] : P.vmax[2]);
-  V = fmax_(V, sz ? P.vmax[5] : P.vmax[4]);
+  float V = S.vmax(sx ? 1 : 0);
+  V = fmax_(V, S.vmax(sy ? 3 : 2));
+  V = fmax_(V, S.vmax(sz ? 5 : 4));
   V = ffma(V, 1.0000003f, 1.01f * clo);
   // fp64-side and absolute error terms: 2^-47 (V^2 + V h) + 2^-100
   const float cd = ffma(kD64, fmul(V, fadd(V, h)), kTiny);
@@ -719,22 +735,21 @@ SAT_HD bool child_full(const Pair32& P, int ci, unsigned* fallbacks) {
     if ((k == 1 || k == 4 || k == 7) && passY) continue;
     if ((k == 2 || k == 5 || k == 8) && passZ) continue;
     const int j = k / 3;
-    const float* e = P.e[j];
-    const float* ae = P.ae[j];
+    const float e[3] = {S.e(j, 0), S.e(j, 1), S.e(j, 2)};
     int r;
     switch (k) {
       case 0: case 3:  // X01: a=e.z, b=e.y over v0, v2 on (y, z)
-        r = edge_test_box(e[Z], e[Y], false, v[0][Y], v[0][Z], v[2][Y], v[2][Z], fadd(ae[Z], ae[Y]), hW, hmW, cd); break;
+        r = edge_test_box(e[Z], e[Y], false, v[0][Y], v[0][Z], v[2][Y], v[2][Z], fadd(fabsf_(e[Z]), fabsf_(e[Y])), hW, hmW, cd); break;
       case 1: case 4:  // Y02: -a*v.x + b*v.z, a=e.z, b=e.x over v0, v2
-        r = edge_test_box(e[Z], e[X], true, v[0][X], v[0][Z], v[2][X], v[2][Z], fadd(ae[Z], ae[X]), hW, hmW, cd); break;
+        r = edge_test_box(e[Z], e[X], true, v[0][X], v[0][Z], v[2][X], v[2][Z], fadd(fabsf_(e[Z]), fabsf_(e[X])), hW, hmW, cd); break;
       case 2: case 8:  // Z12: a=e.y, b=e.x over v1, v2 on (x, y)
-        r = edge_test_box(e[Y], e[X], false, v[1][X], v[1][Y], v[2][X], v[2][Y], fadd(ae[Y], ae[X]), hW, hmW, cd); break;
+        r = edge_test_box(e[Y], e[X], false, v[1][X], v[1][Y], v[2][X], v[2][Y], fadd(fabsf_(e[Y]), fabsf_(e[X])), hW, hmW, cd); break;
       case 5:          // Z0: over v0, v1
-        r = edge_test_box(e[Y], e[X], false, v[0][X], v[0][Y], v[1][X], v[1][Y], fadd(ae[Y], ae[X]), hW, hmW, cd); break;
+        r = edge_test_box(e[Y], e[X], false, v[0][X], v[0][Y], v[1][X], v[1][Y], fadd(fabsf_(e[Y]), fabsf_(e[X])), hW, hmW, cd); break;
       case 6:          // X2: over v0, v1
-        r = edge_test_box(e[Z], e[Y], false, v[0][Y], v[0][Z], v[1][Y], v[1][Z], fadd(ae[Z], ae[Y]), hW, hmW, cd); break;
+        r = edge_test_box(e[Z], e[Y], false, v[0][Y], v[0][Z], v[1][Y], v[1][Z], fadd(fabsf_(e[Z]), fabsf_(e[Y])), hW, hmW, cd); break;
       default:         // 7, Y1: over v0, v1
-        r = edge_test_box(e[Z], e[X], true, v[0][X], v[0][Z], v[1][X], v[1][Z], fadd(ae[Z], ae[X]), hW, hmW, cd); break;
+        r = edge_test_box(e[Z], e[X], true, v[0][X], v[0][Z], v[1][X], v[1][Z], fadd(fabsf_(e[Z]), fabsf_(e[X])), hW, hmW, cd); break;
     }
     rej |= uint32_t(r == 1) << k;
     unk |= uint32_t(r == 2) << k;
@@ -754,14 +769,16 @@ SAT_HD bool child_full(const Pair32& P, int ci, unsigned* fallbacks) {
   //   |d_f - d*| <= 8.2 u32 h sum sn + 9.2 u32 sum sn_q |v0_q| + clo sum sn
   //   fp64 side <= 2^-42 V^2 (V + h)
   const float tn0 = ffma(kD64, fmul(V, V), kTiny);
+  const float n[3] = {S.n(0), S.n(1), S.n(2)}, sn[3] = {S.sn(0), S.sn(1), S.sn(2)};
   bool sure = true;
-  for (int q = 0; q < 3; ++q) sure = sure && (fabsf_(P.n[q]) > ffma(4.2f * kU32, P.sn[q], tn0));
+  for (int q = 0; q < 3; ++q) sure = sure && (fabsf_(n[q]) > ffma(4.2f * kU32, sn[q], tn0));
   if (sure) {
-    const float nd = fadd(fadd(fmul(P.n[0], v[0][0]), fmul(P.n[1], v[0][1])), fmul(P.n[2], v[0][2]));
-    const float dmin = -fadd(P.nh, nd);
-    const float dmax = fsub(P.nh, nd);
-    const float snsum = fadd(fadd(P.sn[0], P.sn[1]), P.sn[2]);
-    const float snv = ffma(P.sn[0], fabsf_(v[0][0]), ffma(P.sn[1], fabsf_(v[0][1]), fmul(P.sn[2], fabsf_(v[0][2]))));
+    const float nh = S.nh();
+    const float nd = fadd(fadd(fmul(n[0], v[0][0]), fmul(n[1], v[0][1])), fmul(n[2], v[0][2]));
+    const float dmin = -fadd(nh, nd);
+    const float dmax = fsub(nh, nd);
+    const float snsum = fadd(fadd(sn[0], sn[1]), sn[2]);
+    const float snv = ffma(sn[0], fabsf_(v[0][0]), ffma(sn[1], fabsf_(v[0][1]), fmul(sn[2], fabsf_(v[0][2]))));
     const float td = ffma(8.7f * kU32 * h, snsum,
                           ffma(9.7f * kU32, snv, ffma(1.06f * clo, snsum,
                                                      ffma(32.f * kD64, fmul(fmul(V, V), fadd(V, h)), kTiny))));
@@ -772,6 +789,10 @@ SAT_HD bool child_full(const Pair32& P, int ci, unsigned* fallbacks) {
     }
   }
   return !need64(12);
+}
+
+SAT_HD bool child_full(const Pair32& P, int ci, unsigned* fallbacks) {
+  return child_full_src(P, PairSrc{P}, ci, fallbacks);
 }
 
 // Overlap decision for child `ci` (index 4x+2y+z) of the pair: true when the

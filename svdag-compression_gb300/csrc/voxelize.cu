@@ -59,6 +59,25 @@ __host__ __device__ __forceinline__ double child_half_side(double root_side, uin
 #define SVDAG_EXPAND_THREADS 192
 #endif
 constexpr int kExpandThreads = SVDAG_EXPAND_THREADS;
+
+// A queued pair's edge and plane constants, read from the tile's shared
+// memory at their use in the full test.
+struct SmemPairSrc {
+  const float (*st)[kExpandThreads];
+  const float (*snb)[kExpandThreads];
+  const float (*svm)[kExpandThreads];
+  const float (*se)[kExpandThreads];
+  const float (*spl)[kExpandThreads];
+  uint32_t slot;
+  __device__ __forceinline__ float t(int i) const { return st[i][slot]; }
+  __device__ __forceinline__ float chi(int i) const { return snb[i][slot]; }
+  __device__ __forceinline__ float clo() const { return snb[6][slot]; }
+  __device__ __forceinline__ float vmax(int i) const { return svm[i][slot]; }
+  __device__ __forceinline__ float e(int j, int q) const { return se[3 * j + q][slot]; }
+  __device__ __forceinline__ float n(int q) const { return spl[q][slot]; }
+  __device__ __forceinline__ float sn(int q) const { return spl[3 + q][slot]; }
+  __device__ __forceinline__ float nh() const { return spl[6][slot]; }
+};
 static_assert(kExpandThreads % 32 == 0 && kExpandThreads <= 256, "tile: whole warps, static shared memory <= 48 KB");
 
 #ifndef SVDAG_EXPAND_MIN_BLOCKS
@@ -162,23 +181,11 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
       const uint32_t item = s_queue[i];
       const uint32_t slot = item >> 3;
       const int ci = int(item & 7u);
-      float tri[9];
-#pragma unroll
-      for (int j = 0; j < 9; ++j) tri[j] = s_t[j][slot];
-      sat::NodeBoxes nb;
-#pragma unroll
-      for (int j = 0; j < 6; ++j) nb.chi[j] = s_nb[j][slot];
-      nb.clo = s_nb[6][slot];
-      nb.ok = s_nb[7][slot];
       const uint32_t node = s_node[slot];
       const uint32_t word = s_slab[slot];
+      // the scalars of the pair; triangle, boxes, edges and plane are read
+      // from shared memory where the full test uses them
       sat::Pair32 PP;
-#pragma unroll
-      for (int j = 0; j < 9; ++j) {
-        PP.t[j] = tri[j];
-        PP.e[j / 3][j % 3] = s_e[j][slot];
-      }
-      PP.nb = nb;
       PP.h = hf;
       PP.fast = (word >> 31) != 0u;
       PP.slab = word & 0xFFFFu;
@@ -187,12 +194,8 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
       PP.tp = tris + 9ull * s_tri[slot];
       PP.c = ctr + 3ull * node;
       PP.k = k;
-#pragma unroll
-      for (int j = 0; j < 6; ++j) PP.vmax[j] = s_vmax[j][slot];
-#pragma unroll
-      for (int j = 0; j < 3; ++j) { PP.n[j] = s_pl[j][slot]; PP.sn[j] = s_pl[3 + j][slot]; }
-      PP.nh = s_pl[6][slot];
-      if (sat::child_full(PP, ci, &fb)) atomicOr(&s_hits[slot], 1u << ci);
+      const SmemPairSrc src{s_t, s_nb, s_vmax, s_e, s_pl, slot};
+      if (sat::child_full_src(PP, src, ci, &fb)) atomicOr(&s_hits[slot], 1u << ci);
     }
     __syncthreads();
     {
