@@ -51,12 +51,12 @@ __host__ __device__ __forceinline__ double child_half_side(double root_side, uin
 //      full certified test.
 // Then each pair publishes its hit mask: OR into the node mask, first-pair
 // index per created child, and the mask for the next frontier.
-// 192 threads and 4 resident blocks per SM (24 warps, 85 registers) measured
+// 224 threads and 4 resident blocks per SM (28 warps, 73 registers) measured
 // fastest among 128-256 threads x 2-6 blocks on the depth-12 terrain: the
-// kernel is latency bound, and more, smaller blocks keep warps issuing
+// kernel is latency bound, and more warps in more blocks keep the SM issuing
 // across the tile barriers despite a few spilled registers.
 #ifndef SVDAG_EXPAND_THREADS
-#define SVDAG_EXPAND_THREADS 192
+#define SVDAG_EXPAND_THREADS 224
 #endif
 constexpr int kExpandThreads = SVDAG_EXPAND_THREADS;
 
