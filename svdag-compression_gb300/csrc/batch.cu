@@ -227,72 +227,85 @@ __device__ __forceinline__ uint64_t key_hash(uint32_t chunk, uint32_t m, const u
 constexpr int kGBits = 40;  // cell index bits in a slot (the rest: hash tag)
 constexpr uint64_t kGMask = (1ull << kGBits) - 1;
 
+// Probe for the key of cell g; returns its slot (inserted, or found holding
+// an equal key, lowered to g when g is smaller), or ~0 when the table is full.
+__device__ __forceinline__ uint64_t batch_probe(const HeightView& V, uint64_t g, uint32_t chunk, uint32_t m,
+                                                const uint32_t ids[8], uint64_t hk,
+                                                unsigned long long* __restrict__ slots, uint64_t mask) {
+  const uint64_t tag = hk >> kGBits;
+  const unsigned long long mine = (tag << kGBits) | g;
+  uint64_t pos = hk & mask;
+  for (uint64_t probe = 0; probe <= mask; ++probe) {
+    unsigned long long cur = __ldcg(&slots[pos]);
+    if (cur == kEmpty64) {
+      const unsigned long long prev = atomicCAS(&slots[pos], kEmpty64, mine);
+      if (prev == kEmpty64) return pos;
+      cur = prev;
+    }
+    if ((cur >> kGBits) == tag) {
+      const uint64_t g2 = cur & kGMask;
+      uint32_t e2, ids2[8];
+      const uint32_t m2 = cell_key(V, g2, e2, ids2);
+      bool eq = (V.part[e2] == chunk) && (m2 == m);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) eq &= (ids2[k] == ids[k]);
+      if (eq) {
+        if (g < g2) atomicMin(&slots[pos], mine);
+        return pos;
+      }
+    }
+    pos = (pos + 1) & mask;
+  }
+  return ~0ull;
+}
+
+// Inserts every non-empty cell's key and records in slot_of[g] the slot that
+// holds it (~0 for empty cells).  Lanes of a warp with the same key -- runs
+// of identical cells are common in solid or empty regions -- probe once: the
+// lowest such lane (also the smallest cell index) probes for all of them.
 __global__ void k_batch_insert(HeightView V, uint64_t total, unsigned long long* __restrict__ slots, uint64_t mask,
-                               int* err) {
-  for (uint64_t g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; g < total; g += uint64_t(gridDim.x) * blockDim.x) {
-    uint32_t e, ids[8];
-    const uint32_t m = cell_key(V, g, e, ids);
-    if (!m && !V.is_top[e]) continue;
+                               uint64_t* __restrict__ slot_of, int* err) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t warps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t w = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; (w << 5) < total; w += warps) {
+    const uint64_t g = (w << 5) + lane;
+    uint32_t e = 0, ids[8], m = 0;
+    bool part = false;
+    if (g < total) {
+      m = cell_key(V, g, e, ids);
+      part = m || V.is_top[e];
+    }
+    const unsigned act = __ballot_sync(0xFFFFFFFFu, part);
+    if (!part) {
+      if (g < total) slot_of[g] = ~0ull;
+      continue;
+    }
     const uint32_t chunk = V.part[e];
     const uint64_t hk = key_hash(chunk, m, ids);
-    const uint64_t tag = hk >> kGBits;
-    const unsigned long long mine = (tag << kGBits) | g;
-    uint64_t pos = hk & mask;
-    bool done = false;
-    for (uint64_t probe = 0; probe <= mask && !done; ++probe) {
-      unsigned long long cur = __ldcg(&slots[pos]);
-      if (cur == kEmpty64) {
-        const unsigned long long prev = atomicCAS(&slots[pos], kEmpty64, mine);
-        if (prev == kEmpty64) { done = true; break; }
-        cur = prev;
-      }
-      if ((cur >> kGBits) == tag) {
-        const uint64_t g2 = cur & kGMask;
-        uint32_t e2, ids2[8];
-        const uint32_t m2 = cell_key(V, g2, e2, ids2);
-        bool eq = (V.part[e2] == chunk) && (m2 == m);
+    const unsigned grp = __match_any_sync(act, hk);
+    const int lead = __ffs(int(grp)) - 1;
+    // the leader's key, to confirm equal keys behind equal hashes
+    bool same = true;
+    same &= __shfl_sync(act, chunk, lead) == chunk;
+    same &= __shfl_sync(act, m, lead) == m;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) eq &= (ids2[k] == ids[k]);
-        if (eq) {
-          if (g < g2) atomicMin(&slots[pos], mine);
-          done = true;
-          break;
-        }
-      }
-      pos = (pos + 1) & mask;
-    }
-    if (!done) atomicExch(err, 1);
+    for (int k = 0; k < 8; ++k) same &= __shfl_sync(act, ids[k], lead) == ids[k];
+    uint64_t pos = 0;
+    if (int(lane) == lead) pos = batch_probe(V, g, chunk, m, ids, hk, slots, mask);
+    const uint64_t lpos = __shfl_sync(act, pos, lead);
+    if (int(lane) != lead) pos = same ? lpos : batch_probe(V, g, chunk, m, ids, hk, slots, mask);
+    if (pos == ~0ull) atomicExch(err, 1);
+    slot_of[g] = pos;
   }
 }
 
 // The representative (smallest index with the same key) of every non-empty
-// cell, found by a lookup of its own key.
-__global__ void k_batch_rep(HeightView V, uint64_t total, const unsigned long long* __restrict__ slots, uint64_t mask,
+// cell: the index its slot holds once every insert is done.
+__global__ void k_batch_rep(uint64_t total, const unsigned long long* __restrict__ slots,
                             uint64_t* __restrict__ rep) {
   for (uint64_t g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; g < total; g += uint64_t(gridDim.x) * blockDim.x) {
-    uint32_t e, ids[8];
-    const uint32_t m = cell_key(V, g, e, ids);
-    if (!m && !V.is_top[e]) { rep[g] = ~0ull; continue; }
-    const uint32_t chunk = V.part[e];
-    const uint64_t hk = key_hash(chunk, m, ids);
-    const uint64_t tag = hk >> kGBits;
-    uint64_t pos = hk & mask;
-    uint64_t r = ~0ull;
-    for (uint64_t probe = 0; probe <= mask; ++probe) {
-      const unsigned long long cur = slots[pos];
-      if (cur == kEmpty64) break;
-      if ((cur >> kGBits) == tag) {
-        const uint64_t g2 = cur & kGMask;
-        uint32_t e2, ids2[8];
-        const uint32_t m2 = cell_key(V, g2, e2, ids2);
-        bool eq = (V.part[e2] == chunk) && (m2 == m);
-#pragma unroll
-        for (int k = 0; k < 8; ++k) eq &= (ids2[k] == ids[k]);
-        if (eq) { r = g2; break; }
-      }
-      pos = (pos + 1) & mask;
-    }
-    rep[g] = r;
+    const uint64_t p = rep[g];
+    rep[g] = p == ~0ull ? ~0ull : (slots[p] & kGMask);
   }
 }
 
@@ -333,12 +346,18 @@ __global__ void k_batch_leaf_first(const uint8_t* const* __restrict__ bricks, co
   __shared__ uint32_t sf[256];
   for (int m = threadIdx.x; m < 256; m += blockDim.x) sf[m] = kNone;
   __syncthreads();
+  // 8 bricks per load (the brick arrays are 8-byte aligned, n a multiple of 8)
+  const uint64_t* w8 = reinterpret_cast<const uint64_t*>(b);
   unsigned long long s = 0;
-  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
-    const uint32_t m = b[i];
-    if (m) {
-      s += __popc(m);
-      if (sf[m] > uint32_t(i)) atomicMin(&sf[m], uint32_t(i));
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n / 8; i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t w = w8[i];
+    if (!w) continue;
+    s += __popcll(w);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const uint32_t m = uint32_t(w >> (8 * k)) & 0xFFu;
+      const uint32_t at = uint32_t(8 * i + k);
+      if (m && sf[m] > at) atomicMin(&sf[m], at);
     }
   }
   __syncthreads();
@@ -473,7 +492,7 @@ void build_wave(Batch& B, const std::vector<uint32_t>& sel) {
   {
     uint64_t mx = 0;
     for (auto v : hn) mx = std::max(mx, v);
-    const unsigned gx = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((mx + 255) / 256, 2048)));
+    const unsigned gx = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((mx / 8 + 255) / 256, 2048)));
     SVDAG_LAUNCH(ex, k_batch_leaf_first, dim3(gx, N), 256, 0, d_bricks.get(), d_nb.get(), first.get(), vox.get());
   }
   SVDAG_LAUNCH(ex, k_batch_leaf_rank, N, 256, 0, first.get(), rank.get(), leaf_hdr.get(), leaf_cnt.get());
@@ -561,9 +580,10 @@ void build_wave(Batch& B, const std::vector<uint32_t>& sel) {
     DBuf<unsigned long long> slots(size, st);
     SVDAG_CUDA(cudaMemsetAsync(slots.get(), 0xFF, 8 * size, st));
     const unsigned tb = B.tuning.threads;
-    SVDAG_LAUNCH(ex, k_batch_insert, grid_for(ex, total, tb, 8), tb, 0, V, total, slots.get(), size - 1, d_err.get());
     DBuf<uint64_t> rep(total, st), newid(total, st);
-    SVDAG_LAUNCH(ex, k_batch_rep, grid_for(ex, total, tb, 8), tb, 0, V, total, slots.get(), size - 1, rep.get());
+    SVDAG_LAUNCH(ex, k_batch_insert, grid_for(ex, total, tb, 8), tb, 0, V, total, slots.get(), size - 1, rep.get(),
+                 d_err.get());
+    SVDAG_LAUNCH(ex, k_batch_rep, grid_for(ex, total, tb, 8), tb, 0, total, slots.get(), rep.get());
     slots.release();
     DBuf<uint64_t> d_total(1, st);
     device_exclusive_scan<uint64_t>(ex, RepIn{rep.get()}, total, U64Out{newid.get()}, d_total.get());
@@ -759,6 +779,7 @@ void run_batch(Batch& B, uint32_t flags) {
   B.reduce_ms = wall_ms(t1);
 }
 
+
 }  // namespace
 
 extern "C" {
@@ -819,6 +840,17 @@ int svdag_batch_create(svdag_batch** out, int device, void* stream) {
   }
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  // keep freed blocks of the stream-ordered allocator cached between waves
+  // and builds (as svdag_create does): every wave allocates and frees tens
+  // of GB, which the pool would otherwise unmap and map again each time
+  cudaMemPool_t pool;
+  uint64_t keep = ~0ull;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) != cudaSuccess ||
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+    if (B.own_stream) cudaStreamDestroy(B.stream);
+    delete h;
+    return SVDAG_ERR_CUDA;
+  }
   B.ex.stream = B.stream;
   B.ex.sm_count = sms;
   B.ex.launches = &B.launches;
