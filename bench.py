@@ -17,6 +17,7 @@ toSDAG and mergeAcrossAllLevels, as restated by the oracle, on a bounded
 sample (the first rows of the same terrain) so the run ends in minutes.
 """
 import argparse
+import concurrent.futures
 import ctypes
 import datetime
 import json
@@ -178,7 +179,7 @@ R = 36
 # workload (the 12 k_expand launches of one timed step, averaged; per-launch
 # figures in profiles/k_expand_terrain2048_L12_dram.txt).  Valid for the
 # default terrain workload only.
-KERNEL_DRAM_BYTES_PER_LAUNCH = {"k_expand": 566186453}
+KERNEL_DRAM_BYTES_PER_LAUNCH = {"k_expand": 543215189}
 
 
 def model_bytes(info, T):
@@ -203,6 +204,8 @@ def run_ours(args, rank, local, world):
     T = tris.shape[0]
     d_tris = torch.from_numpy(tris).to(dev)
     stream = torch.cuda.Stream(device=dev)
+    red_streams = [torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)]
+    red_pool = concurrent.futures.ThreadPoolExecutor(2)
     base = sv.Octree(device=local, stream=stream.cuda_stream)
     base.set_device_triangles(d_tris.data_ptr(), T, keepalive=d_tris)
     have_csv = True
@@ -229,24 +232,33 @@ def run_ours(args, rank, local, world):
         octree.initChildLevels()
         if profile:
             collect("dag", octree)
-        s = octree.clone()
-        if profile:
-            s.profile(True)
-        s.toSDAG()
-        if profile:
-            collect("sdag", s)
-        c = None
-        if have_csv:
-            c = octree.clone()
-            if profile:
-                c.profile(True)
+        # the SSVDAG and CSVDAG reductions of the same DAG are independent:
+        # two clones on their own streams, driven from two host threads
+        s = octree.clone(stream=red_streams[0].cuda_stream)
+        c = octree.clone(stream=red_streams[1].cuda_stream) if have_csv else None
+        for o in (s, c):
+            if profile and o is not None:
+                o.profile(True)
+
+        def merge():
             try:
                 c.mergeAcrossAllLevels()
+                return True
             except sv.SvdagError:
-                have_csv = False
-                c = None
-            if profile and c is not None:
+                return False
+
+        fs = red_pool.submit(s.toSDAG)
+        fc = red_pool.submit(merge) if c is not None else None
+        fs.result()
+        if fc is not None and not fc.result():
+            have_csv = False
+            c = None
+        if profile:
+            collect("sdag", s)
+            if c is not None:
                 collect("csv", c)
+        stream.wait_stream(red_streams[0])
+        stream.wait_stream(red_streams[1])
         return s, c
 
     for _ in range(max(args.warmup, 0)):
@@ -337,8 +349,8 @@ def run_ours(args, rank, local, world):
             pairs = info["frontier"][0]
             roof["algorithmic_bytes"] = "B_vox = 36 T + 36 sum_l N_l per build, spread over its %d launches" % args.levels
             roof["note"] = ("k_expand is instruction-issue / latency bound (SAT box tests), not HBM bound: ncu on "
-                            "its two largest launches of terrain 1024 depth 11 shows issue slots 53-63% busy at 23 "
-                            "warps/SM, ALU pipe 45-55%, FMA 14-17%, FP64 <1%, DRAM 3-4% of peak "
+                            "its two largest launches of terrain 1024 depth 11 shows issue slots 60-71% busy at 28 "
+                            "warps/SM, ALU pipe 51-62%, FMA 16-20%, FP64 <1%, DRAM 3-4% of peak "
                             "(profiles/k_expand_terrain1024_L11.txt)")
             roof["sat"] = {"frontier_pairs_per_s": pairs / (ms / args.steps / 1e3),
                            "child_box_tests_per_s": 8 * pairs / (ms / args.steps / 1e3)}
@@ -415,6 +427,8 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
     ptr = pinned.data_ptr()
     T = tris.shape[0]
     o = sv.Octree(device=local, stream=stream.cuda_stream)
+    red_streams = [torch.cuda.Stream(device=local), torch.cuda.Stream(device=local)]
+    red_pool = concurrent.futures.ThreadPoolExecutor(2)
     lib = sv.load_gpu()
     cap = [0]
     host = {}
@@ -452,13 +466,18 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
             o.buildSVO(args.levels)
             o.toDAG()
         o.initChildLevels()
-        s = o.clone()
-        s.toSDAG()
+        s = o.clone(stream=red_streams[0].cuda_stream)
+        c = o.clone(stream=red_streams[1].cuda_stream) if have_csv else None
+        fs = red_pool.submit(s.toSDAG)
+        fc = red_pool.submit(c.mergeAcrossAllLevels) if c is not None else None
+        fs.result()
+        if fc is not None:
+            fc.result()
         d2h = download(s, True)
-        if have_csv:
-            c = o.clone()
-            c.mergeAcrossAllLevels()
+        if c is not None:
             d2h += download(c, False)
+        stream.wait_stream(red_streams[0])
+        stream.wait_stream(red_streams[1])
         return d2h
 
     for _ in range(max(1, args.warmup)):

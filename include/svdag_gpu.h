@@ -76,6 +76,10 @@ int svdag_destroy(svdag_ctx* ctx);
  * SSVDAG and the CSVDAG reductions, as GeomOctree's copy constructor does
  * (src/symvox/geom_octree.cpp:40-45). */
 int svdag_clone(const svdag_ctx* src, svdag_ctx** out);
+/* The same copy on `stream` (a cudaStream_t, or NULL for a new one), so that
+ * two clones of one DAG -- the SSVDAG and the CSVDAG reductions -- can run
+ * concurrently from two host threads. */
+int svdag_clone_on(const svdag_ctx* src, void* stream, svdag_ctx** out);
 const char* svdag_last_error(const svdag_ctx* ctx);
 const char* svdag_status_string(int status);
 int svdag_synchronize(svdag_ctx* ctx);

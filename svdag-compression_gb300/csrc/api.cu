@@ -133,9 +133,14 @@ int svdag_destroy(svdag_ctx* h) {
 }
 
 int svdag_clone(const svdag_ctx* src, svdag_ctx** out) {
+  if (!src) return SVDAG_ERR_INVALID_ARG;
+  return svdag_clone_on(src, src->c.own_stream ? nullptr : src->c.stream, out);
+}
+
+int svdag_clone_on(const svdag_ctx* src, void* stream, svdag_ctx** out) {
   if (!src || !out) return SVDAG_ERR_INVALID_ARG;
   const Ctx& s = src->c;
-  int r = svdag_create(out, s.device, s.own_stream ? nullptr : s.stream);
+  int r = svdag_create(out, s.device, stream);
   if (r != SVDAG_OK) return r;
   return guarded(*out, [&](Ctx& c) {
     c.tris = s.owned_tris.get() ? nullptr : s.tris;

@@ -57,6 +57,7 @@ GPU_SYMBOLS = {
     "svdag_create": (_I, [ctypes.POINTER(_VP), _I, _VP]),
     "svdag_destroy": (_I, [_VP]),
     "svdag_clone": (_I, [_VP, ctypes.POINTER(_VP)]),
+    "svdag_clone_on": (_I, [_VP, _VP, ctypes.POINTER(_VP)]),
     "svdag_last_error": (ctypes.c_char_p, [_VP]),
     "svdag_status_string": (ctypes.c_char_p, [_I]),
     "svdag_synchronize": (_I, [_VP]),
@@ -409,9 +410,14 @@ class Octree:
                 ch = np.ascontiguousarray(lev[1], np.uint32)
             self._check(self._lib.svdag_import_level(self._h, l, len(hdr), hdr.ctypes.data, ch.ctypes.data))
 
-    def clone(self):
+    def clone(self, stream=None):
+        """Device-side copy (GeomOctree's copy constructor); on `stream` (a
+        cudaStream_t handle) when given."""
         h = ctypes.c_void_p()
-        self._check(self._lib.svdag_clone(self._h, ctypes.byref(h)))
+        if stream is None:
+            self._check(self._lib.svdag_clone(self._h, ctypes.byref(h)))
+        else:
+            self._check(self._lib.svdag_clone_on(self._h, stream, ctypes.byref(h)))
         return Octree(_handle=h)
 
     # results
