@@ -118,17 +118,18 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
   const int tid = threadIdx.x;
   unsigned fb = 0;
   // tiles: a grid-stride walk, or (tile_ctr) taken one at a time from a
-  // counter so that blocks finishing early take more
+  // counter so that blocks finishing early take more.  Three barriers per
+  // tile: after the classification, after the queue, and at the end (which
+  // also publishes the next tile and the cleared queue count).
   uint64_t base = uint64_t(blockIdx.x) * kExpandThreads;
-  if (tile_ctr) {
-    if (tid == 0) s_base = atomicAdd(tile_ctr, 1ull) * kExpandThreads;
-    __syncthreads();
-    base = s_base;
+  if (tid == 0) {
+    s_qn = 0;
+    if (tile_ctr) s_base = atomicAdd(tile_ctr, 1ull) * kExpandThreads;
   }
+  __syncthreads();
+  if (tile_ctr) base = s_base;
   for (; base < F;) {
     const uint64_t q = base + tid;
-    if (tid == 0) s_qn = 0;
-    __syncthreads();
     uint32_t hits = 0;
     if (q < F) {
       const uint32_t t = f_tri ? f_tri[q] : uint32_t(q);
@@ -197,7 +198,7 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
       const SmemPairSrc src{s_t, s_nb, s_vmax, s_e, s_pl, slot};
       if (sat::child_full_src(PP, src, ci, &fb)) atomicOr(&s_hits[slot], 1u << ci);
     }
-    __syncthreads();
+    if (nq) __syncthreads();  // nq is the same for the whole block; no queue, no hits to wait for
     {
       // Publish per warp: lanes of the same node combine their hit masks and
       // first pair indices (pair index = q - lane + lane', increasing with the
@@ -232,20 +233,20 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
         if (lane == 0) s_wsum[tid >> 5] = wsum;
       }
     }
+    // every thread is past the queue (s_qn) and has published (s_wsum)
+    if (tid == 0) {
+      s_qn = 0;
+      if (tile_ctr) s_base = atomicAdd(tile_ctr, 1ull) * kExpandThreads;
+    }
     __syncthreads();
     if (!leaf && tid == 0) {
+      // s_wsum is rewritten only after two more barriers this thread joins
       uint32_t t = 0;
 #pragma unroll
       for (int w = 0; w < kExpandThreads / 32; ++w) t += s_wsum[w];
       tile_hits[base / kExpandThreads] = t;
     }
-    if (tile_ctr) {
-      if (tid == 0) s_base = atomicAdd(tile_ctr, 1ull) * kExpandThreads;
-      __syncthreads();
-      base = s_base;
-    } else {
-      base += uint64_t(gridDim.x) * kExpandThreads;
-    }
+    base = tile_ctr ? s_base : base + uint64_t(gridDim.x) * kExpandThreads;
   }
   unsigned long long sum = fb;
   for (int o = 16; o; o >>= 1) sum += __shfl_down_sync(0xFFFFFFFFu, sum, o);
