@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
       const SmemPairSrc src{s_t, s_nb, s_vmax, s_e, s_pl, slot};
       if (sat::child_full_src(PP, src, ci, &fb)) atomicOr(&s_hits[slot], 1u << ci);
     }
-    if (nq) __syncthreads();  // nq is the same for the whole block; no queue, no hits to wait for
+    __syncthreads();
     {
       // Publish per warp: lanes of the same node combine their hit masks and
       // first pair indices (pair index = q - lane + lane', increasing with the
