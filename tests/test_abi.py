@@ -42,6 +42,22 @@ def test_status_strings_and_null_handles():
     assert lib.svdag_get_stats(None, None) == 1
 
 
+def test_null_arguments_are_rejected_before_any_device_work():
+    lib = sv.load_gpu()
+    h = ctypes.c_void_p()
+    assert lib.svdag_clone_on(None, None, ctypes.byref(h)) == 1
+    assert lib.svdag_flood_fill(None, None, None) == 1
+    assert lib.svdag_download_outside_masks(None, 0, None) == 1
+    assert lib.svdag_encode(None, 0, None, 0, None) == 1
+    assert lib.svdag_ssvdag_free(None) == 1
+    assert lib.svdag_ssvdag_raycast(None, None, None, None, 0) == 1
+    bb = (ctypes.c_float * 6)(0, 0, 0, 1, 1, 1)
+    # arrays missing while their sizes say otherwise
+    assert lib.svdag_ssvdag_upload(None, 4, None, 8, None, 1, 5, bb, 1.0, ctypes.byref(h)) == 1
+    assert lib.svdag_ssvdag_upload(None, 0, None, 0, None, 0, 5, bb, 1.0, None) == 1
+    assert lib.svdag_ssvdag_traverse(None, 0, None, 0, None, 0, 5, bb, 1.0, None, 0, None) == 1
+
+
 def test_create_fails_loudly_without_device():
     import torch
 
