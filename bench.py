@@ -430,10 +430,13 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
     red_streams = [torch.cuda.Stream(device=local), torch.cuda.Stream(device=local)]
     red_pool = concurrent.futures.ThreadPoolExecutor(2)
     lib = sv.load_gpu()
-    cap = [0]
-    host = {}
+    # one set of pinned host buffers per result, so that each result is read
+    # back by its own host thread as soon as its reduction ends
+    caps = [[0], [0]]
+    hosts = [{}, {}]
 
-    def buffers(n):
+    def buffers(n, k):
+        cap, host = caps[k], hosts[k]
         if n > cap[0]:
             cap[0] = max(n, 2 * cap[0])
             host["hdr"] = torch.empty(cap[0], dtype=torch.int32).pin_memory()
@@ -449,7 +452,7 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
             assert lib.svdag_level_count(x._h, l, ctypes.byref(n)) == 0
             if n.value == 0:
                 continue
-            b = buffers(n.value)
+            b = buffers(n.value, 0 if sdag else 1)
             leaf = l == args.levels - 1
             ch = None if leaf else b["ch"].data_ptr()
             cl = None if (leaf or sdag) else b["cl"].data_ptr()
@@ -468,14 +471,20 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
         o.initChildLevels()
         s = o.clone(stream=red_streams[0].cuda_stream)
         c = o.clone(stream=red_streams[1].cuda_stream) if have_csv else None
-        fs = red_pool.submit(s.toSDAG)
-        fc = red_pool.submit(c.mergeAcrossAllLevels) if c is not None else None
-        fs.result()
+
+        def sdag():
+            s.toSDAG()
+            return download(s, True)
+
+        def csv():
+            c.mergeAcrossAllLevels()
+            return download(c, False)
+
+        fs = red_pool.submit(sdag)
+        fc = red_pool.submit(csv) if c is not None else None
+        d2h = fs.result()
         if fc is not None:
-            fc.result()
-        d2h = download(s, True)
-        if c is not None:
-            d2h += download(c, False)
+            d2h += fc.result()
         stream.wait_stream(red_streams[0])
         stream.wait_stream(red_streams[1])
         return d2h
