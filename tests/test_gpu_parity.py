@@ -207,3 +207,28 @@ def test_build_dag_rejects_bad_step_levels():
         with pytest.raises(sv.SvdagError) as e:
             o.buildDAG(6, step)
         assert e.value.status == 1
+
+
+def test_concurrent_reductions_on_two_streams():
+    """The SSVDAG and CSVDAG reductions of one DAG on two clones placed on
+    their own streams (svdag_clone_on), driven from two host threads at once,
+    give the golden digests."""
+    import concurrent.futures
+
+    import torch
+
+    name = "terrain65_L8"
+    g = G[name]
+    o = gpu_build(SCENES[name](), g["levels"])
+    o.toDAG()
+    o.initChildLevels()
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    s = o.clone(stream=s1.cuda_stream)
+    c = o.clone(stream=s2.cuda_stream)
+    with concurrent.futures.ThreadPoolExecutor(2) as pool:
+        fs = pool.submit(s.toSDAG)
+        fc = pool.submit(c.mergeAcrossAllLevels)
+        fs.result()
+        assert fc.result() == g["nCrossLevelMerged"]
+    assert oracle_py.pool_digest(s.pool()) == g["sdag"]["digest"]
+    assert oracle_py.pool_digest(c.pool()) == g["csv"]["digest"]
