@@ -140,6 +140,19 @@ int svdag_level_device_ptrs(const svdag_ctx* ctx, uint32_t level, const uint32_t
 enum { SVDAG_FORMAT_SVDAG = 0, SVDAG_FORMAT_USSVDAG = 1 };
 int svdag_encode(svdag_ctx* ctx, uint32_t format, uint32_t* host_words, uint64_t capacity, uint64_t* n_words);
 
+/* EncodedSSVDAG::encode (src/symvox/encoded_ssvdag.cpp:194-466) on the GPU
+ * (DAG or SDAG state, not cross-level merged): the arrays of a .ssvdag file,
+ * byte-identical to the reference's -- the level order uses the reference's
+ * std::sort over the pointer counts (run on the host over counts gathered on
+ * the GPU), the packing runs on the GPU.  svdag_encode_ssvdag encodes and
+ * reports the sizes (u16 inner words, leaf bytes, level offsets); the
+ * result stays in the context until svdag_download_ssvdag copies it to host
+ * buffers of those sizes (any may be NULL to skip it).  The file is: bbox
+ * (6 floats), rootSide (float), levels (u32), nNodes (u32), then u32 count +
+ * data for the inner words, the leaf bytes and the level offsets. */
+int svdag_encode_ssvdag(svdag_ctx* ctx, uint64_t* n_inner_words, uint64_t* n_leaf_bytes, uint32_t* n_level_offsets);
+int svdag_download_ssvdag(svdag_ctx* ctx, uint16_t* inner, uint8_t* leaves, uint32_t* level_offsets);
+
 /* EncodedSSVDAG::traverse (src/symvox/encoded_ssvdag.cpp:527-574) on the
  * GPU, one point query per thread: the depth each point reaches in an encoded
  * SSVDAG (the arrays of a .ssvdag file), `levels` when its voxel is set, -1

@@ -9,6 +9,36 @@ using svdag::Error;
 
 namespace {
 
+// Imported node records: every set mask bit has a child below `limit`, and
+// no pointer sits under a clear bit (what the reductions' kernels rely on).
+__global__ void k_child_range(const uint32_t* __restrict__ hdr, const uint32_t* __restrict__ ch, uint64_t n,
+                              uint64_t limit, int* __restrict__ bad) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t m = hdr[i] & 0xFFu;
+    for (int c = 0; c < 8; ++c) {
+      const uint32_t v = ch[8 * i + c];
+      const bool set = (m >> c) & 1u;
+      if (set ? (v == svdag::kNull || v >= limit) : (v != svdag::kNull)) atomicExch(bad, 1);
+    }
+  }
+}
+
+// Checks level l's children against level l+1 once both are imported.
+void check_children(Ctx& c, uint32_t l) {
+  if (l + 1 >= c.lev.size()) return;
+  const svdag::Level& P = c.lev[l];
+  const svdag::Level& Q = c.lev[l + 1];
+  if (!P.hdr.get() || !Q.hdr.get() || !P.n) return;
+  svdag::DBuf<int> bad(1, c.stream);
+  SVDAG_CUDA(cudaMemsetAsync(bad.get(), 0, 4, c.stream));
+  SVDAG_LAUNCH(c.ex, k_child_range, svdag::grid_for(c.ex, P.n, 256), 256, 0, P.hdr.get(), P.ch.get(), P.n, Q.n,
+               bad.get());
+  if (svdag::read_scalar(c.ex, bad.get())) {
+    c.state = SVDAG_S_EMPTY;
+    throw Error(SVDAG_ERR_INVALID_ARG, "import_level: a child pointer does not match the mask or the level below");
+  }
+}
+
 int fail(svdag_ctx* h, int code, const std::string& msg) {
   if (h) h->c.last_error = msg;
   return code;
@@ -122,8 +152,11 @@ int svdag_destroy(svdag_ctx* h) {
   if (!h) return SVDAG_ERR_INVALID_ARG;
   Ctx& c = h->c;
   cudaSetDevice(c.device);
+  // every stream-ordered buffer goes back before its stream is destroyed
   c.lev.clear();
   c.owned_tris.release();
+  c.ss_inner.clear();
+  c.ss_leaves.release();
   cudaStreamSynchronize(c.stream);
   if (c.ev0) cudaEventDestroy(c.ev0);
   if (c.ev1) cudaEventDestroy(c.ev1);
@@ -252,6 +285,8 @@ int svdag_import_level(svdag_ctx* h, uint32_t level, uint64_t count, const uint3
       if (count) SVDAG_CUDA(cudaMemcpyAsync(L.ch.get(), children, 32 * count, cudaMemcpyHostToDevice, c.stream));
     }
     SVDAG_CUDA(cudaStreamSynchronize(c.stream));
+    check_children(c, level);
+    if (level > 0) check_children(c, level - 1);
     uint64_t n = 1;
     for (size_t l = 1; l < c.lev.size(); ++l) n += c.lev[l].n;
     c.st.n_nodes = n;

@@ -52,6 +52,13 @@ struct Ctx {
 
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   Profiler prof;
+
+  // the last SSVDAG encoding (svdag_encode_ssvdag), read by
+  // svdag_download_ssvdag: inner words per level, leaf bricks
+  std::vector<DBuf<uint16_t>> ss_inner;
+  std::vector<uint64_t> ss_words;
+  DBuf<uint64_t> ss_leaves;
+  uint64_t ss_bricks = 0;
 };
 
 // Phases (each throws svdag::Error on failure).

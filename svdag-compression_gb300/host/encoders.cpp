@@ -113,6 +113,22 @@ bool EncodedUSSVDAG::encode(const GeomOctree& o) {
   return true;
 }
 
+bool EncodedSSVDAG::encode(const GeomOctree& o) {
+  if (o.getState() != S_SDAG && o.getState() != S_DAG) return false;  // encoded_ssvdag.cpp:218-221
+  uint64_t ni = 0, nl = 0;
+  uint32_t no = 0;
+  if (svdag_encode_ssvdag(o.handle(), &ni, &nl, &no) != SVDAG_OK) return false;
+  inner.resize(ni);
+  leaves.resize(nl);
+  levelOffsets.resize(no);
+  if (svdag_download_ssvdag(o.handle(), inner.data(), leaves.data(), levelOffsets.data()) != SVDAG_OK) return false;
+  std::memcpy(bbox, o.getSceneBBox(), sizeof(bbox));
+  rootSide = o.getRootSide();
+  levels = o.getLevels();
+  nNodes = o.getNNodes();
+  return true;
+}
+
 bool EncodedSVDAG::save(const std::string& path) const {
   std::ofstream f(path, std::ios::binary);
   if (!f) return false;

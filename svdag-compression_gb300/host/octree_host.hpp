@@ -155,6 +155,9 @@ struct EncodedSSVDAG {
   std::vector<uint8_t> leaves;
   std::vector<uint32_t> levelOffsets;
   bool encode(const NodeData& d, const float bbox[6], float rootSide, uint64_t nNodes, State st);
+  // the same arrays built on the GPU (svdag_encode_ssvdag; the ref-count
+  // order is the same std::sort on the host)
+  bool encode(const GeomOctree& o);
   bool save(const std::string& path) const;
   size_t getDataSize() const { return inner.size() * 2 + leaves.size() + levelOffsets.size() * 4; }
 };

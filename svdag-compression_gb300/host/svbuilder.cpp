@@ -137,8 +137,8 @@ int main(int argc, char** argv) {
   octree.initChildLevels();
   const std::string basePath = dir_of(input) + "/" + base_of(input) + "_" + std::to_string(nLevels);
 
-  // the SVDAG / USSVDAG pointer streams are built on the GPU; the SSVDAG
-  // (reference-count order, libstdc++ sort) is encoded on the host
+  // every encoding is built on the GPU; the SSVDAG's reference-count order
+  // is the reference's std::sort, run on the host over counts from the GPU
   EncodedSVDAG svdag2;
   svdag2.encode(octree);
   svdag2.save(basePath + ".svdag");
@@ -148,16 +148,13 @@ int main(int argc, char** argv) {
   EncodedSVDAG svdag;
   svdag.encode(octree);
   EncodedSSVDAG esvdag;
-  if (!multiLevel)
-    esvdag.encode(octree.getNodeData(), octree.getSceneBBox(), octree.getRootSide(), octree.getNNodes(),
-                  octree.getState());
+  if (!multiLevel) esvdag.encode(octree);
   if (!multiLevel) octree.toSDAG();
   EncodedUSSVDAG ussvdag;
   EncodedSSVDAG ssvdag;
   if (!multiLevel) {
     ussvdag.encode(octree);
-    ssvdag.encode(octree.getNodeData(), octree.getSceneBBox(), octree.getRootSide(), octree.getNNodes(),
-                  octree.getState());
+    ssvdag.encode(octree);
   }
   const std::string infix = multiLevel ? "-multi" : "";
   svdag.save(basePath + infix + ".svdag");

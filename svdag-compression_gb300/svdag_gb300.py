@@ -96,6 +96,8 @@ GPU_SYMBOLS = {
     "svdag_batch_get_stats": (_I, [_VP, _VP]),
     "svdag_lossy_dag": (_I, [_VP, _VP, _VP]),
     "svdag_encode": (_I, [_VP, _U32, _VP, _U64, ctypes.POINTER(_U64)]),
+    "svdag_encode_ssvdag": (_I, [_VP, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_U32)]),
+    "svdag_download_ssvdag": (_I, [_VP, _VP, _VP, _VP]),
     "svdag_ssvdag_traverse": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, _VP, _U64, _VP]),
     "svdag_ssvdag_upload": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, ctypes.POINTER(_VP)]),
     "svdag_ssvdag_free": (_I, [_VP]),
@@ -360,6 +362,28 @@ class Octree:
         out = np.empty(n.value, np.uint32)
         self._check(self._lib.svdag_encode(self._h, f, out.ctypes.data, n.value, ctypes.byref(n)))
         return out
+
+    def encode_ssvdag(self):
+        """EncodedSSVDAG::encode on the GPU (svdag_encode_ssvdag): the inner
+        u16 words, the leaf bytes and the level offsets of the .ssvdag file."""
+        ni, nl, no = _U64(), _U64(), _U32()
+        self._check(self._lib.svdag_encode_ssvdag(self._h, ctypes.byref(ni), ctypes.byref(nl), ctypes.byref(no)))
+        inner = np.empty(ni.value, np.uint16)
+        leaves = np.empty(nl.value, np.uint8)
+        offs = np.empty(no.value, np.uint32)
+        self._check(self._lib.svdag_download_ssvdag(self._h, inner.ctypes.data, leaves.ctypes.data, offs.ctypes.data))
+        return inner, leaves, offs
+
+    def save_ssvdag(self, path, bbox=UNIT_BOX, root_side=1.0):
+        """The .ssvdag file of this octree (EncodedSSVDAG::save layout)."""
+        inner, leaves, offs = self.encode_ssvdag()
+        head = np.array(bbox, np.float32).tobytes() + np.array([root_side], np.float32).tobytes()
+        head += np.array([self.getLevels(), self.stats()["n_nodes"] & 0xFFFFFFFF], np.uint32).tobytes()
+        with open(path, "wb") as f:
+            f.write(head)
+            for a in (inner, leaves, offs):
+                f.write(np.array([a.size], np.uint32).tobytes())
+                f.write(a.tobytes())
 
     def save_encoded(self, path, fmt="svdag", bbox=UNIT_BOX, root_side=1.0):
         """Writes the file the reference's saver writes for this stream."""
