@@ -74,7 +74,8 @@ __global__ void k_ff_links(FFView V, uint32_t l) {
 // neighbour of equal size is subdivided.
 constexpr uint64_t kNone64 = ~0ull;
 
-__device__ uint64_t face_neighbour(const FFView& V, uint32_t l, uint64_t node, int c, int a, int s) {
+__device__ uint64_t face_neighbour(const FFView& V, uint32_t l, uint64_t node, int c, int a, int s,
+                                   uint32_t* found_level = nullptr) {
   const uint32_t d = l + 1;  // depth of the cell
   const uint64_t p = V.coord[l][node];
   uint32_t x[3] = {2 * axis_of(p, 0) + ((c >> 2) & 1), 2 * axis_of(p, 1) + ((c >> 1) & 1), 2 * axis_of(p, 2) + (c & 1)};
@@ -91,6 +92,7 @@ __device__ uint64_t face_neighbour(const FFView& V, uint32_t l, uint64_t node, i
   for (;;) {
     const uint32_t sh = d - 1 - m;
     const int cc = int((((x[0] >> sh) & 1u) << 2) | (((x[1] >> sh) & 1u) << 1) | ((x[2] >> sh) & 1u));
+    if (found_level) *found_level = m;
     if (m + 1 == V.levels) return V.base[m] + 8 * nd + cc;
     const uint32_t q = V.ch[m][8 * nd + cc];
     if (q == kNull) return V.base[m] + 8 * nd + cc;
@@ -149,8 +151,10 @@ __global__ void k_ff_unite(FFView V, uint32_t l, uint32_t* P, uint32_t* err) {
     if (!is_leaf(V, l, node, c) || is_set(V, l, node, c)) continue;
     const uint32_t g = uint32_t(V.base[l] + r);
     for (int dir = 0; dir < 6; ++dir) {
-      const uint64_t nb = face_neighbour(V, l, node, c, dir % 3, dir < 3 ? -1 : 1);
-      if (nb == kNone64 || !empty_leaf_cell(V, nb)) continue;
+      uint32_t fl = 0;
+      const uint64_t nb = face_neighbour(V, l, node, c, dir % 3, dir < 3 ? -1 : 1, &fl);
+      // a neighbour of the same size links to this cell across its + face
+      if (nb == kNone64 || (dir < 3 && fl == l) || !empty_leaf_cell(V, nb)) continue;
       uf_unite(P, g, uint32_t(nb), err);
     }
   }
