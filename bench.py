@@ -39,7 +39,9 @@ UNIT = "Mvoxels/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 20; 300 frames for raycast and 25 fills for floodfill, about a "
+                         "second of timed work so that the clock sampler sees it)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["terrain", "city", "batch", "lossy", "raycast", "floodfill"],
@@ -67,6 +69,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-json", default="")
     a = ap.parse_args()
+    if a.steps is None:
+        a.steps = {"raycast": 300, "floodfill": 25}.get(a.workload, 20)
     city = a.workload == "city"
     if a.grid is None:
         a.grid = 4096 if city else 2048
