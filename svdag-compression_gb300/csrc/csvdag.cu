@@ -62,7 +62,7 @@ __global__ void k_tid0_first(TreeView T, uint32_t g0, uint32_t g1, uint32_t* __r
     const uint32_t g = g0 + uint32_t(k);
     const uint32_t l = level_of(T, g);
     const uint32_t m = T.hdr[l][g - T.off[l]] & 0xFFu;
-    atomicMin(&sf[m], g);
+    if (sf[m] > g) atomicMin(&sf[m], g);  // read first: common masks repeat
   }
   __syncthreads();
   for (int m = threadIdx.x; m < 256; m += blockDim.x)
@@ -126,9 +126,11 @@ __global__ void k_check_level(TreeView T, uint32_t l, const uint32_t* __restrict
     uint32_t c[8];
     load_children(T.ch[l], i, c);
     const uint32_t base = T.off[l + 1];
+    // shared children are reached from many parents: write only a byte that
+    // does not hold the mark yet (same-address stores serialise in L2)
 #pragma unroll
     for (int j = 0; j < 8; ++j)
-      if ((m >> j) & 1u) in_check[base + c[j]] = 1;
+      if (((m >> j) & 1u) && !in_check[base + c[j]]) in_check[base + c[j]] = 1;
   }
 }
 
@@ -151,7 +153,7 @@ __global__ void k_owner_min(TreeView T, uint32_t l, const uint32_t* __restrict__
     const uint32_t base = T.off[l + 1];
 #pragma unroll
     for (int j = 0; j < 8; ++j)
-      if ((m >> j) & 1u) atomicMin(&owner[base + c[j]], e);
+      if (((m >> j) & 1u) && __ldcg(&owner[base + c[j]]) > e) atomicMin(&owner[base + c[j]], e);
   }
 }
 
@@ -171,7 +173,8 @@ __global__ void k_owner_path(TreeView T, uint32_t l, const uint32_t* __restrict_
     for (int j = 0; j < 8; ++j)
       if ((m >> j) & 1u) {
         const uint32_t x = base + c[j];
-        if (owner[x] == e) atomicMax(&best[x], (pp << 3) | uint32_t(j));
+        const unsigned long long v = (pp << 3) | uint32_t(j);
+        if (owner[x] == e && __ldcg(&best[x]) < v) atomicMax(&best[x], v);
       }
   }
 }

@@ -83,7 +83,7 @@ __global__ void k_leaf_first(const uint32_t* __restrict__ hdr, uint64_t n, uint3
   __syncthreads();
   for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
     const uint32_t m = hdr[i] & 0xFFu;
-    if (m) atomicMin(&sf[m], uint32_t(i));
+    if (m && sf[m] > uint32_t(i)) atomicMin(&sf[m], uint32_t(i));  // read first: common masks repeat
   }
   __syncthreads();
   for (int m = threadIdx.x; m < 256; m += blockDim.x)
