@@ -311,16 +311,17 @@ __global__ void k_batch_rep(uint64_t total, const unsigned long long* __restrict
 
 struct RepIn {
   const uint64_t* rep;
-  __device__ __forceinline__ uint64_t operator()(uint64_t g) const { return rep[g] == g ? 1u : 0u; }
+  __device__ __forceinline__ uint32_t operator()(uint64_t g) const { return rep[g] == g ? 1u : 0u; }
 };
-struct U64Out {
-  uint64_t* a;
-  __device__ __forceinline__ void operator()(uint64_t i, uint64_t v) const { a[i] = v; }
+struct U32Out {
+  uint32_t* a;
+  __device__ __forceinline__ void operator()(uint64_t i, uint32_t v) const { a[i] = v; }
 };
 
-// DAG id (within the chunk) of every cell, and the DAG nodes of this height.
+// DAG id (within the chunk) of every cell, and the DAG nodes of this height
+// (node numbers of a wave fit 32 bits: a wave has at most 2^30 cells).
 __global__ void k_batch_emit(HeightView V, uint64_t total, const uint64_t* __restrict__ rep,
-                             const uint64_t* __restrict__ newid, const uint64_t* __restrict__ rep_base,
+                             const uint32_t* __restrict__ newid, const uint64_t* __restrict__ rep_base,
                              uint32_t* __restrict__ ids_out, uint32_t* __restrict__ hdr, uint32_t* __restrict__ ch) {
   for (uint64_t g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; g < total; g += uint64_t(gridDim.x) * blockDim.x) {
     const uint64_t r = rep[g];
@@ -580,23 +581,24 @@ void build_wave(Batch& B, const std::vector<uint32_t>& sel) {
     DBuf<unsigned long long> slots(size, st);
     SVDAG_CUDA(cudaMemsetAsync(slots.get(), 0xFF, 8 * size, st));
     const unsigned tb = B.tuning.threads;
-    DBuf<uint64_t> rep(total, st), newid(total, st);
+    if (total >= (1ull << 32)) throw Error(SVDAG_ERR_OVERFLOW, "batch: more than 2^32 cells on one height");
+    DBuf<uint64_t> rep(total, st);
+    DBuf<uint32_t> newid(total, st);
     SVDAG_LAUNCH(ex, k_batch_insert, grid_for(ex, total, tb, 8), tb, 0, V, total, slots.get(), size - 1, rep.get(),
                  d_err.get());
     SVDAG_LAUNCH(ex, k_batch_rep, grid_for(ex, total, tb, 8), tb, 0, total, slots.get(), rep.get());
     slots.release();
-    DBuf<uint64_t> d_total(1, st);
-    device_exclusive_scan<uint64_t>(ex, RepIn{rep.get()}, total, U64Out{newid.get()}, d_total.get());
+    DBuf<uint32_t> d_total(1, st);
+    device_exclusive_scan<uint32_t>(ex, RepIn{rep.get()}, total, U32Out{newid.get()}, d_total.get());
     // DAG nodes of each entry: newid range [newid at its first cell, next entry's)
     std::vector<uint64_t> rep_base(n + 1);
     {
-      DBuf<uint64_t> d_rb(n, st);
-      std::vector<uint64_t> h_nid(n);
+      std::vector<uint32_t> h_nid(n + 1);
       for (uint32_t e = 0; e < n; ++e)
-        SVDAG_CUDA(cudaMemcpyAsync(&h_nid[e], newid.get() + base[e], 8, cudaMemcpyDeviceToHost, st));
-      SVDAG_CUDA(cudaMemcpyAsync(&rep_base[n], d_total.get(), 8, cudaMemcpyDeviceToHost, st));
+        SVDAG_CUDA(cudaMemcpyAsync(&h_nid[e], newid.get() + base[e], 4, cudaMemcpyDeviceToHost, st));
+      SVDAG_CUDA(cudaMemcpyAsync(&h_nid[n], d_total.get(), 4, cudaMemcpyDeviceToHost, st));
       SVDAG_CUDA(cudaStreamSynchronize(st));
-      for (uint32_t e = 0; e < n; ++e) rep_base[e] = h_nid[e];
+      for (uint32_t e = 0; e <= n; ++e) rep_base[e] = h_nid[e];
     }
     DBuf<uint64_t> d_rep_base(n, st);
     SVDAG_CUDA(cudaMemcpyAsync(d_rep_base.get(), rep_base.data(), 8ull * n, cudaMemcpyHostToDevice, st));
