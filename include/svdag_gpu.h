@@ -142,9 +142,10 @@ int svdag_encode(svdag_ctx* ctx, uint32_t format, uint32_t* host_words, uint64_t
 
 /* EncodedSSVDAG::encode (src/symvox/encoded_ssvdag.cpp:194-466) on the GPU
  * (DAG or SDAG state, not cross-level merged): the arrays of a .ssvdag file,
- * byte-identical to the reference's -- the level order uses the reference's
- * std::sort over the pointer counts (run on the host over counts gathered on
- * the GPU), the packing runs on the GPU.  svdag_encode_ssvdag encodes and
+ * byte-identical to the reference's -- the level order is the one the
+ * reference's std::sort over the pointer counts leaves (reproduced on the
+ * GPU, see svdag_refcount_order), the packing runs on the GPU; nothing goes
+ * through the host.  svdag_encode_ssvdag encodes and
  * reports the sizes (u16 inner words, leaf bytes, level offsets); the
  * result stays in the context until svdag_download_ssvdag copies it to host
  * buffers of those sizes (any may be NULL to skip it).  The file is: bbox
@@ -152,6 +153,15 @@ int svdag_encode(svdag_ctx* ctx, uint32_t format, uint32_t* host_words, uint64_t
  * data for the inner words, the leaf bytes and the level offsets. */
 int svdag_encode_ssvdag(svdag_ctx* ctx, uint64_t* n_inner_words, uint64_t* n_leaf_bytes, uint32_t* n_level_offsets);
 int svdag_download_ssvdag(svdag_ctx* ctx, uint16_t* inner, uint8_t* leaves, uint32_t* level_offsets);
+
+/* The per-level node order of EncodedSSVDAG::encode
+ * (src/symvox/encoded_ssvdag.cpp:259-276): the (index, count) pairs
+ * (i, counts[i]), sorted by std::sort with "count(a) > count(b)", exactly as
+ * libstdc++'s (GCC 13) introsort orders them -- equal counts included, whose
+ * order that unstable sort decides.  order[k] = index of the k-th pair.
+ * Device buffers of n u32 each; runs on `stream` (0 = default) and returns
+ * when the order is written.  n <= 2^31. */
+int svdag_refcount_order(void* stream, const uint32_t* device_counts, uint64_t n, uint32_t* device_order);
 
 /* EncodedSSVDAG::traverse (src/symvox/encoded_ssvdag.cpp:527-574) on the
  * GPU, one point query per thread: the depth each point reaches in an encoded

@@ -37,6 +37,7 @@ _SIGS = {
     "ora_build_dag_chunked": (_I, [_VP, _VP, _U64, _VP, _U32, _U32, _I]),
     "ora_build_from_bricks": (_I, [_VP, _U32, _VP]),
     "ora_lossy_exact": (_I, [_VP, _U32, _U32, ctypes.c_double, ctypes.POINTER(_U64)]),
+    "ora_refcount_order": (_I, [_VP, _U64, _VP]),
     "ora_ssvdag_traverse": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, _VP, _U64, _VP]),
     "ora_ssvdag_raycast": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, _VP, _VP, _U32, _U32,
                                 _U32, _U32, ctypes.c_float, ctypes.c_float, ctypes.c_float, _VP]),
@@ -202,6 +203,15 @@ def read_ssvdag(path):
     offs = np.frombuffer(raw, np.uint32, n, o).copy()
     return {"bbox": bbox.copy(), "root_side": root_side, "levels": int(levels), "n_nodes": int(n_nodes),
             "inner": inner, "leaves": leaves, "level_offsets": offs}
+
+
+def refcount_order(counts):
+    """EncodedSSVDAG::encode's per-level order: std::sort of (index, count)
+    pairs by count, descending (libstdc++, as the reference)."""
+    c = np.ascontiguousarray(counts, np.uint32)
+    out = np.empty(c.size, np.uint32)
+    assert load().ora_refcount_order(c.ctypes.data, c.size, out.ctypes.data) == 0
+    return out
 
 
 def ssvdag_traverse(f, pts):

@@ -933,6 +933,18 @@ int ora_lossy_exact(ora_octree* o, uint32_t min_above, uint32_t max_above, doubl
   return 0;
 }
 
+// The per-level node order of EncodedSSVDAG::encode
+// (src/symvox/encoded_ssvdag.cpp:259-276): (index, count) pairs in index
+// order, sorted by libstdc++'s std::sort with the reference's comparator.
+int ora_refcount_order(const uint32_t* counts, uint64_t n, uint32_t* order) {
+  std::vector<std::pair<uint32_t, uint32_t>> hist(n);
+  for (uint64_t i = 0; i < n; ++i) hist[i] = std::make_pair(uint32_t(i), counts[i]);
+  std::sort(hist.begin(), hist.end(),
+            [](std::pair<uint32_t, uint32_t> a, std::pair<uint32_t, uint32_t> b) { return a.second > b.second; });
+  for (uint64_t k = 0; k < n; ++k) order[k] = hist[k].first;
+  return 0;
+}
+
 // EncodedSSVDAG::traverse (src/symvox/encoded_ssvdag.cpp:527-574) with
 // getChild / getChildMask (:587-625) and getHalfSide (encoded_octree.hpp:68):
 // the depth a point query reaches in an encoded SSVDAG (levels = voxel set).

@@ -42,6 +42,9 @@ int ora_build_dag_chunked(ora_octree* o, const float* tris, uint64_t n_tris, con
 int ora_build_from_bricks(ora_octree* o, uint32_t depth, const uint8_t* bricks);
 /* lossy LSVDAG, exact-proposer form (project-defined; see the .cpp) */
 int ora_lossy_exact(ora_octree* o, uint32_t min_above, uint32_t max_above, double max_err, uint64_t* merged);
+/* the per-level node order of EncodedSSVDAG::encode (encoded_ssvdag.cpp:259-276):
+ * std::sort of (index, count) pairs by count, descending */
+int ora_refcount_order(const uint32_t* counts, uint64_t n, uint32_t* order);
 /* EncodedSSVDAG::traverse (encoded_ssvdag.cpp:527-574): depth reached per point */
 int ora_ssvdag_traverse(const uint16_t* inner, uint64_t n_inner, const uint8_t* leaves, uint64_t n_leaves,
                         const uint32_t* level_off, uint32_t n_level_off, uint32_t levels, const float bbox[6],

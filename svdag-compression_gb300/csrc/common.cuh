@@ -158,8 +158,9 @@ inline uint64_t next_pow2(uint64_t x) {
 
 // ---------------------------------------------------------------------------
 // Device-wide exclusive scan.  `In` maps an index to a value; `Out` receives
-// (index, exclusive prefix, value) for every index.  Three kernels: tile
-// reduce, (recursive) scan of tile sums, tile scan + emit.
+// (index, exclusive prefix) for every index.  One tile: one kernel (scan +
+// emit + total).  More tiles: tile reduce, (recursive) scan of the tile sums,
+// tile scan + emit; the last tile of the emit writes the grand total.
 
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
@@ -215,7 +216,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(In in, uint64_t
 }
 
 template <class T, class In, class Out>
-__global__ void __launch_bounds__(kScanThreads) k_scan_tile_emit(In in, uint64_t n, const T* offs, Out out) {
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile_emit(In in, uint64_t n, const T* offs, Out out,
+                                                                   T* total) {
   __shared__ T sv[kScanTile];
   const uint64_t base = uint64_t(blockIdx.x) * kScanTile;
 #pragma unroll
@@ -232,7 +234,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tile_emit(In in, uint64_t
     run += loc[j];
   }
   T tot;
-  T pre = block_excl_scan<T>(run, &tot) + (offs ? offs[blockIdx.x] : T(0));
+  const T off = offs ? offs[blockIdx.x] : T(0);
+  T pre = block_excl_scan<T>(run, &tot) + off;
+  if (total && threadIdx.x == 0 && blockIdx.x == gridDim.x - 1) *total = off + tot;
   __syncthreads();
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) {
@@ -259,11 +263,6 @@ struct ArrayOut {
   __device__ __forceinline__ void operator()(uint64_t i, T v) const { a[i] = v; }
 };
 
-template <class T>
-__global__ void k_store_total(const T* sums, const T* offs, uint64_t nb, T* total) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) *total = nb ? offs[nb - 1] + sums[nb - 1] : T(0);
-}
-
 // Exclusive scan of in(0..n-1); out(i, prefix) for every i; the grand total
 // is written to *d_total (device) when d_total != nullptr.
 template <class T, class In, class Out>
@@ -274,21 +273,14 @@ void device_exclusive_scan(const Exec& ex, In in, uint64_t n, Out out, T* d_tota
   }
   const uint64_t nb = (n + kScanTile - 1) / kScanTile;
   if (nb == 1) {
-    DBuf<T> s(1, ex.stream);
-    SVDAG_LAUNCH(ex, (k_scan_tile_sums<T, In>), 1, kScanThreads, 0, in, n, s.get());
-    SVDAG_LAUNCH(ex, (k_scan_tile_emit<T, In, Out>), 1, kScanThreads, 0, in, n, (const T*)nullptr, out);
-    if (d_total) {
-      DBuf<T> z(1, ex.stream);
-      SVDAG_CUDA(cudaMemsetAsync(z.get(), 0, sizeof(T), ex.stream));
-      SVDAG_LAUNCH(ex, k_store_total<T>, 1, 32, 0, s.get(), z.get(), 1, d_total);
-    }
+    SVDAG_LAUNCH(ex, (k_scan_tile_emit<T, In, Out>), 1, kScanThreads, 0, in, n, (const T*)nullptr, out, d_total);
     return;
   }
   DBuf<T> sums(nb, ex.stream), offs(nb, ex.stream);
   SVDAG_LAUNCH(ex, (k_scan_tile_sums<T, In>), unsigned(nb), kScanThreads, 0, in, n, sums.get());
   device_exclusive_scan<T>(ex, ArrayIn<T>{sums.get()}, nb, ArrayOut<T>{offs.get()}, (T*)nullptr);
-  SVDAG_LAUNCH(ex, (k_scan_tile_emit<T, In, Out>), unsigned(nb), kScanThreads, 0, in, n, (const T*)offs.get(), out);
-  if (d_total) SVDAG_LAUNCH(ex, k_store_total<T>, 1, 32, 0, sums.get(), offs.get(), nb, d_total);
+  SVDAG_LAUNCH(ex, (k_scan_tile_emit<T, In, Out>), unsigned(nb), kScanThreads, 0, in, n, (const T*)offs.get(), out,
+               d_total);
 }
 
 template <class T>

@@ -72,6 +72,9 @@ void phase_reduce_sdag(Ctx& c);
 void phase_cross_level_merge(Ctx& c);
 // GeomOctree::hiddenGeometryFloodfill: outside masks of an SVO (floodfill.cu).
 void phase_flood_fill(Ctx& c, uint64_t* n_empty, uint64_t* n_surface);
+// Reference-count order of a level, exactly as the reference's std::sort of
+// (index, count) pairs leaves it (refsort.cu): order[k] = k-th node.
+void refcount_order(const Exec& ex, const uint32_t* counts, uint64_t n, uint32_t* order);
 // toDAG with every temporary in caller-provided device scratch (no allocation).
 void phase_reduce_dag_scratch(Ctx& c, uint8_t* scratch, uint64_t capacity);
 

@@ -117,11 +117,10 @@ uint64_t encode_stream(Ctx& c, bool ussvdag, uint32_t* host_out, uint64_t capaci
 // ---------------------------------------------------------------------------
 // EncodedSSVDAG::encode (src/symvox/encoded_ssvdag.cpp:194-466).  Bottom-up
 // from the level above the leaves: each level's nodes are ordered by how many
-// pointers reach them from the level above, with the reference's own
-// std::sort over (index, count) pairs -- an unstable sort whose order for
-// equal counts is that implementation's, so it runs on the host over counts
-// the GPU gathers (4 bytes per node each way); everything else runs on the
-// GPU.  The level above the leaves becomes 4^3 bricks of 8 bytes (the 8
+// pointers reach them from the level above, in the order the reference's
+// std::sort over (index, count) pairs leaves them -- an unstable sort whose
+// order for equal counts is libstdc++'s introsort's, reproduced on the GPU
+// (refsort.cu).  The level above the leaves becomes 4^3 bricks of 8 bytes (the 8
 // children's masks, mirrored, in voxel-matrix order: octree voxel (X, Y, Z)
 // of the brick at bit Z + 4Y + 16X); every other level becomes u16 nodes (a
 // header with 2 bits per child, then 16- or 32-bit pointers, high half
@@ -137,6 +136,11 @@ __global__ void k_ss_refcount(const uint32_t* __restrict__ pch, uint64_t np, uin
       if (k != kNull) atomicAdd(&cnt[k], 1u);
     }
   }
+}
+
+__global__ void k_ss_iota(uint32_t* __restrict__ perm, uint64_t n) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    perm[i] = uint32_t(i);
 }
 
 __device__ __forceinline__ uint32_t mirror_mask8(uint32_t m, uint32_t flip) {
@@ -247,32 +251,22 @@ void encode_ssvdag(Ctx& c) {
   DBuf<uint32_t> addr_child, addr_cur;
   DBuf<int> d_err(1, st);
   SVDAG_CUDA(cudaMemsetAsync(d_err.get(), 0, 4, st));
-  std::vector<uint32_t> counts;
-  std::vector<std::pair<uint32_t, uint32_t>> hist;
-  std::vector<uint32_t> perm_h;
   for (int lev = int(L) - 2; lev >= 0; --lev) {
     const Level& Lv = c.lev[lev];
     const uint64_t n = Lv.n;
     if (n > (1ull << 30)) throw Error(SVDAG_ERR_OVERFLOW, "encode SSVDAG: a level above 2^30 nodes");
     // order: std::sort of (index, pointers reaching it) by count, descending
-    hist.resize(n);
-    for (uint32_t i = 0; i < n; ++i) hist[i] = std::make_pair(i, 0u);
-    if (lev > 0 && n) {
+    // (reproduced on the device, refsort.cu); the root level keeps index order
+    DBuf<uint32_t> perm(n ? n : 1, st);
+    if (n && lev > 0) {
       DBuf<uint32_t> cnt(n, st);
       SVDAG_CUDA(cudaMemsetAsync(cnt.get(), 0, 4 * n, st));
       const Level& P = c.lev[lev - 1];
       if (P.n) SVDAG_LAUNCH(ex, k_ss_refcount, grid_for(ex, P.n, 256), 256, 0, P.ch.get(), P.n, cnt.get());
-      counts.resize(n);
-      SVDAG_CUDA(cudaMemcpyAsync(counts.data(), cnt.get(), 4 * n, cudaMemcpyDeviceToHost, st));
-      SVDAG_CUDA(cudaStreamSynchronize(st));
-      for (uint32_t i = 0; i < n; ++i) hist[i].second = counts[i];
-      std::sort(hist.begin(), hist.end(),
-                [](std::pair<uint32_t, uint32_t> a, std::pair<uint32_t, uint32_t> b) { return a.second > b.second; });
+      refcount_order(ex, cnt.get(), n, perm.get());
+    } else if (n) {
+      SVDAG_LAUNCH(ex, k_ss_iota, grid_for(ex, n, 256), 256, 0, perm.get(), n);
     }
-    perm_h.resize(n);
-    for (uint64_t k = 0; k < n; ++k) perm_h[k] = hist[k].first;
-    DBuf<uint32_t> perm(n ? n : 1, st);
-    if (n) SVDAG_CUDA(cudaMemcpyAsync(perm.get(), perm_h.data(), 4 * n, cudaMemcpyHostToDevice, st));
     addr_cur = DBuf<uint32_t>(n ? n : 1, st);
     if (lev == int(L) - 2) {
       c.ss_leaves = DBuf<uint64_t>(n ? n : 1, st);

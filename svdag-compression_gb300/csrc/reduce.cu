@@ -493,14 +493,14 @@ void scan_in_scratch(const Exec& ex, In in, uint64_t n, Out out, T* d_total, T* 
     return;
   }
   const uint64_t nb = (n + kScanTile - 1) / kScanTile;
+  if (nb == 1) {
+    SVDAG_LAUNCH(ex, (k_scan_tile_emit<T, In, Out>), 1, kScanThreads, 0, in, n, (const T*)nullptr, out, d_total);
+    return;
+  }
   SVDAG_LAUNCH(ex, (k_scan_tile_sums<T, In>), unsigned(nb), kScanThreads, 0, in, n, sums);
-  if (nb == 1)
-    SVDAG_CUDA(cudaMemsetAsync(offs, 0, sizeof(T), ex.stream));
-  else
-    SVDAG_LAUNCH(ex, (k_scan_tile_emit<T, ArrayIn<T>, ArrayOut<T>>), 1, kScanThreads, 0, ArrayIn<T>{sums}, nb,
-                 (const T*)nullptr, ArrayOut<T>{offs});
-  SVDAG_LAUNCH(ex, (k_scan_tile_emit<T, In, Out>), unsigned(nb), kScanThreads, 0, in, n, (const T*)offs, out);
-  SVDAG_LAUNCH(ex, k_store_total<T>, 1, 32, 0, sums, offs, nb, d_total);
+  SVDAG_LAUNCH(ex, (k_scan_tile_emit<T, ArrayIn<T>, ArrayOut<T>>), 1, kScanThreads, 0, ArrayIn<T>{sums}, nb,
+               (const T*)nullptr, ArrayOut<T>{offs}, (T*)nullptr);
+  SVDAG_LAUNCH(ex, (k_scan_tile_emit<T, In, Out>), unsigned(nb), kScanThreads, 0, in, n, (const T*)offs, out, d_total);
 }
 
 }  // namespace

@@ -98,6 +98,7 @@ GPU_SYMBOLS = {
     "svdag_encode": (_I, [_VP, _U32, _VP, _U64, ctypes.POINTER(_U64)]),
     "svdag_encode_ssvdag": (_I, [_VP, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_U32)]),
     "svdag_download_ssvdag": (_I, [_VP, _VP, _VP, _VP]),
+    "svdag_refcount_order": (_I, [_VP, _VP, _U64, _VP]),
     "svdag_ssvdag_traverse": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, _VP, _U64, _VP]),
     "svdag_ssvdag_upload": (_I, [_VP, _U64, _VP, _U64, _VP, _U32, _U32, _VP, ctypes.c_float, ctypes.POINTER(_VP)]),
     "svdag_ssvdag_free": (_I, [_VP]),
@@ -643,6 +644,27 @@ def ssvdag_traverse(f, pts):
     if r != 0:
         raise SvdagError(r, "ssvdag traverse failed")
     return out
+
+
+def refcount_order(counts, device=0):
+    """The order EncodedSSVDAG::encode gives one level's nodes: the indices of
+    (index, count) pairs after the reference's std::sort by count, descending
+    (src/symvox/encoded_ssvdag.cpp:266-276), computed on the GPU.  `counts`:
+    host array of u32 pointer counts; returns the u32 order on the host."""
+    import torch
+
+    c = np.ascontiguousarray(counts, np.uint32)
+    n = c.size
+    dev = "cuda:%d" % device
+    d_counts = torch.from_numpy(c.view(np.int32)).to(dev)
+    d_order = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+    lib = load_gpu()
+    st = torch.cuda.current_stream(device).cuda_stream
+    r = lib.svdag_refcount_order(ctypes.c_void_p(st), ctypes.c_void_p(d_counts.data_ptr()), n,
+                                 ctypes.c_void_p(d_order.data_ptr()))
+    if r != 0:
+        raise SvdagError(r, "refcount order failed")
+    return d_order[:n].cpu().numpy().view(np.uint32)
 
 
 # --------------------------------------------------------------------------
