@@ -108,11 +108,8 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
   __shared__ float s_pl[7][kExpandThreads];  // plane normal, |m1|+|m2| per component, |n|_1 h
   __shared__ uint32_t s_tri[kExpandThreads], s_node[kExpandThreads], s_slab[kExpandThreads];
   __shared__ uint32_t s_hits[kExpandThreads];
-  // undecided (pair, child) items: first tests from the front, deferred
-  // ones (leaf level) from the back; item = slot << 8 | leader lane << 3 | child
-  constexpr uint32_t kQueue = 8 * kExpandThreads;
-  __shared__ uint16_t s_queue[kQueue];
-  __shared__ uint32_t s_qn, s_qb;
+  __shared__ uint16_t s_queue[8 * kExpandThreads];
+  __shared__ uint32_t s_qn;
   __shared__ uint32_t s_wsum[kExpandThreads / 32];
   __shared__ uint64_t s_base;
   const double k = child_half_side(P.root_side, P.level);
@@ -127,18 +124,16 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
   uint64_t base = uint64_t(blockIdx.x) * kExpandThreads;
   if (tid == 0) {
     s_qn = 0;
-    s_qb = 0;
     if (tile_ctr) s_base = atomicAdd(tile_ctr, 1ull) * kExpandThreads;
   }
   __syncthreads();
   if (tile_ctr) base = s_base;
   for (; base < F;) {
     const uint64_t q = base + tid;
-    uint32_t hits = 0, full = 0;
-    uint32_t node = 0xFFFFFFFFu;
+    uint32_t hits = 0;
     if (q < F) {
       const uint32_t t = f_tri ? f_tri[q] : uint32_t(q);
-      node = f_node ? f_node[q] : 0u;
+      const uint32_t node = f_node ? f_node[q] : 0u;
       const float* tp = tris + 9ull * t;
       float tri[9];
 #pragma unroll
@@ -151,6 +146,7 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
       sat::Pair32 PP;
       sat::pair_core(tri, tp, ctr + 3ull * node, nb, k, PP);
       sat::pair_slabs(PP);
+      uint32_t full = 0;
       for (int ci = 7; ci >= 0; --ci) {
         const int f = sat::child_fast(PP, ci);
         if (f == 1) hits |= 1u << ci;
@@ -158,7 +154,10 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
       }
       s_node[tid] = node;
       if (full) {
-        // the pair data the full test reads (pairs the slabs decide skip it)
+        // this pair's undecided children in consecutive queue slots, and the
+        // pair data the full test reads (pairs the slabs decide skip both)
+        uint32_t slot = atomicAdd(&s_qn, uint32_t(__popc(full)));
+        for (uint32_t m = full; m; m &= m - 1) s_queue[slot++] = uint16_t((tid << 3) | (__ffs(m) - 1));
         sat::pair_edges(PP);
 #pragma unroll
         for (int j = 0; j < 9; ++j) s_e[j][tid] = PP.e[j / 3][j % 3];
@@ -176,55 +175,13 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
         s_slab[tid] = PP.slab | (PP.tang << 16) | (PP.flat << 24) | (PP.fast ? 0x80000000u : 0u);
       }
     }
-    // Leaf level: only the node's mask bits come out, so among the lanes of
-    // the warp holding the same node a voxel the slabs set for one lane
-    // needs no full test on the others, and a voxel undecided for several
-    // lanes is tested first for the lowest of them; the others queue it
-    // behind all first tests and skip it once that test has set the voxel
-    // (a skipped test could only have set a bit that is already set).
-    // Neighbouring triangles share most of their voxels.
-    uint32_t defer = 0;
-    uint64_t leads = 0;
-    if (leaf) {
-      const unsigned grp = __match_any_sync(0xFFFFFFFFu, node);
-      const int lane = tid & 31;
-#pragma unroll
-      for (int ci = 0; ci < 8; ++ci) {
-        if (__ballot_sync(0xFFFFFFFFu, (hits >> ci) & 1u) & grp) full &= ~(1u << ci);
-        const unsigned bf = __ballot_sync(0xFFFFFFFFu, (full >> ci) & 1u) & grp;
-        const int first = __ffs(int(bf)) - 1;
-        if (((full >> ci) & 1u) && first != lane) {
-          defer |= 1u << ci;
-          leads |= uint64_t(first) << (5 * ci);
-        }
-      }
-    }
-    // this pair's undecided children in consecutive queue slots
-    const uint32_t now = full & ~defer;
-    if (now) {
-      uint32_t slot = atomicAdd(&s_qn, uint32_t(__popc(now)));
-      for (uint32_t m = now; m; m &= m - 1) s_queue[slot++] = uint16_t((tid << 8) | (__ffs(m) - 1));
-    }
-    if (defer) {
-      uint32_t slot = atomicAdd(&s_qb, uint32_t(__popc(defer)));
-      for (uint32_t m = defer; m; m &= m - 1) {
-        const int ci = __ffs(m) - 1;
-        s_queue[kQueue - 1 - slot++] = uint16_t((tid << 8) | (uint32_t((leads >> (5 * ci)) & 31u) << 3) | ci);
-      }
-    }
     s_hits[tid] = hits;
     __syncthreads();
-    const uint32_t nq = s_qn, nd = s_qb;
-    for (uint32_t i = tid; i < nq + nd; i += kExpandThreads) {
-      const bool deferred = i >= nq;
-      const uint32_t item = deferred ? s_queue[kQueue - 1 - (i - nq)] : s_queue[i];
-      const uint32_t slot = item >> 8;
+    const uint32_t nq = s_qn;
+    for (uint32_t i = tid; i < nq; i += kExpandThreads) {
+      const uint32_t item = s_queue[i];
+      const uint32_t slot = item >> 3;
       const int ci = int(item & 7u);
-      if (deferred) {
-        // the lane that tests this voxel first (same warp, same node)
-        const uint32_t first = (slot & ~31u) | ((item >> 3) & 31u);
-        if ((*static_cast<volatile uint32_t*>(&s_hits[first]) >> ci) & 1u) continue;
-      }
       const uint32_t node = s_node[slot];
       const uint32_t word = s_slab[slot];
       // the scalars of the pair; triangle, boxes, edges and plane are read
@@ -279,7 +236,6 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
     // every thread is past the queue (s_qn) and has published (s_wsum)
     if (tid == 0) {
       s_qn = 0;
-      s_qb = 0;
       if (tile_ctr) s_base = atomicAdd(tile_ctr, 1ull) * kExpandThreads;
     }
     __syncthreads();
