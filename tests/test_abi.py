@@ -56,6 +56,7 @@ def test_null_arguments_are_rejected_before_any_device_work():
     assert lib.svdag_ssvdag_upload(None, 4, None, 8, None, 1, 5, bb, 1.0, ctypes.byref(h)) == 1
     assert lib.svdag_ssvdag_upload(None, 0, None, 0, None, 0, 5, bb, 1.0, None) == 1
     assert lib.svdag_ssvdag_traverse(None, 0, None, 0, None, 0, 5, bb, 1.0, None, 0, None) == 1
+    assert lib.svdag_refcount_order(None, None, 16, None) == 1
 
 
 def test_create_fails_loudly_without_device():
