@@ -66,6 +66,9 @@ def parse():
     ap.add_argument("--boxes", type=int, default=200000)
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-pipeline", action="store_true",
+                    help="terrain/city: run the timed steps one after another instead of overlapping a step's "
+                         "SSVDAG / CSVDAG reductions with the next step's voxelization")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-json", default="")
     a = ap.parse_args()
@@ -222,8 +225,7 @@ def run_ours(args, rank, local, world):
             a[0] += n
             a[1] += ms
 
-    def step(octree, profile=False):
-        nonlocal have_csv
+    def build(octree, profile=False):
         if args.step_level:
             octree.buildDAG(args.levels, args.step_level)
             if profile:
@@ -236,8 +238,12 @@ def run_ours(args, rank, local, world):
         octree.initChildLevels()
         if profile:
             collect("dag", octree)
+
+    def start_reductions(octree, profile=False):
         # the SSVDAG and CSVDAG reductions of the same DAG are independent:
-        # two clones on their own streams, driven from two host threads
+        # two clones on their own streams, driven from two host threads (a
+        # clone is complete when clone() returns, so the octree may be
+        # rebuilt while they run)
         s = octree.clone(stream=red_streams[0].cuda_stream)
         c = octree.clone(stream=red_streams[1].cuda_stream) if have_csv else None
         for o in (s, c):
@@ -253,6 +259,11 @@ def run_ours(args, rank, local, world):
 
         fs = red_pool.submit(s.toSDAG)
         fc = red_pool.submit(merge) if c is not None else None
+        return s, c, fs, fc
+
+    def finish(pending, profile=False):
+        nonlocal have_csv
+        s, c, fs, fc = pending
         fs.result()
         if fc is not None and not fc.result():
             have_csv = False
@@ -265,6 +276,10 @@ def run_ours(args, rank, local, world):
         stream.wait_stream(red_streams[1])
         return s, c
 
+    def step(octree, profile=False):
+        build(octree, profile)
+        return finish(start_reductions(octree, profile), profile)
+
     for _ in range(max(args.warmup, 0)):
         step(base)
     torch.cuda.synchronize()
@@ -273,10 +288,12 @@ def run_ours(args, rank, local, world):
     st = base.stats()
     voxels = st["n_total_voxels"]
 
-    def timed_region(events):
+    def timed_region(events, pipelined=False):
         """K steps between two CUDA events on the build stream.  With events,
         every kernel launch is also bracketed by CUDA events on that stream
-        (per-kernel durations for the roofline), collected per phase."""
+        (per-kernel durations for the roofline), collected per phase.
+        Pipelined: each step's reductions run while the next step voxelizes
+        (the last step's reductions end inside the region)."""
         launches0 = base.stats()["gpu_launches"]
         base.profile(events)
         base.profile_report()
@@ -289,12 +306,22 @@ def run_ours(args, rank, local, world):
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         outs = []
+        pending = None
         for _ in range(args.steps):
-            s, c = step(base, profile=events)
+            if pipelined:
+                # step i+1's voxelization overlaps step i's reductions
+                build(base)
+                if pending is not None:
+                    outs.append(finish(pending))
+                pending = start_reductions(base)
+            else:
+                outs.append(step(base, profile=events))
+        if pending is not None:
+            outs.append(finish(pending))
+        for s, c in outs:
             for o in (s, c):
                 if o is not None:
                     extra += o.stats()["gpu_launches"]
-            outs.append((s, c))
         e1.record(stream)
         torch.cuda.synchronize()
         ms_total = e0.elapsed_time(e1)
@@ -316,10 +343,12 @@ def run_ours(args, rank, local, world):
     clocks.start()
     time.sleep(0.5)  # the sampler is running before the timed region opens
     clocks.mark()
-    ms_total, _, launches, outs = timed_region(events=False)
+    ms_total, _, launches, outs = timed_region(events=False, pipelined=not args.no_pipeline)
     clk = clocks.stop()
     ms_step = ms_total / args.steps
     value = world * voxels / (ms_step / 1e3) / 1e6
+    # one build at a time (no overlap between steps): the latency of a build
+    ms_seq = timed_region(events=False, pipelined=False)[0] / args.steps
     # the same K steps again with every launch bracketed by CUDA events on the
     # build stream: per-kernel durations for the roofline (the events add host
     # work per launch, so this region is not the one `value` comes from)
@@ -388,6 +417,8 @@ def run_ours(args, rank, local, world):
                    "l2": "inputs larger than L2 (triangles %d MB, node pools > 129 MB)" % (36 * T // 10**6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clk, "gpu_launches": int(launches), "roofline": roof, "reduction_roofline": red, "e2e": e2e,
+        "pipelined": not args.no_pipeline,
+        "sequential_ms_per_step": ms_seq,
         "kernel_events_region_ms_per_step": ms_events / args.steps,
         "kernel_ms_per_step": sum(v[1] for v in prof.values()) / args.steps,
         "kernels": {k: {"launches": v[0], "ms_per_step": v[1] / args.steps} for k, v in
@@ -465,7 +496,7 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
             nbytes += n.value * (4 + (0 if leaf else 32) + (0 if (leaf or sdag) else 8) + (1 if sdag else 0))
         return nbytes
 
-    def one():
+    def build_one():
         assert lib.svdag_upload_triangles(o._h, ptr, T) == 0
         if args.step_level:
             o.buildDAG(args.levels, args.step_level)
@@ -473,6 +504,8 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
             o.buildSVO(args.levels)
             o.toDAG()
         o.initChildLevels()
+
+    def start_one():
         s = o.clone(stream=red_streams[0].cuda_stream)
         c = o.clone(stream=red_streams[1].cuda_stream) if have_csv else None
 
@@ -484,8 +517,10 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
             c.mergeAcrossAllLevels()
             return download(c, False)
 
-        fs = red_pool.submit(sdag)
-        fc = red_pool.submit(csv) if c is not None else None
+        return s, c, red_pool.submit(sdag), (red_pool.submit(csv) if c is not None else None)
+
+    def end_one(p):
+        _, _, fs, fc = p
         d2h = fs.result()
         if fc is not None:
             d2h += fc.result()
@@ -494,23 +529,38 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
         return d2h
 
     for _ in range(max(1, args.warmup)):
-        one()
+        build_one()
+        end_one(start_one())
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
     e0.record(stream)
     d2h = 0
+    pending = None
     for _ in range(args.steps):
-        d2h = one()
+        # the next step's upload and voxelization overlap the previous
+        # step's reductions and read-back, unless --no-pipeline
+        build_one()
+        if pending is not None:
+            d2h = end_one(pending)
+            pending = None
+        pending = start_one()
+        if args.no_pipeline:
+            d2h = end_one(pending)
+            pending = None
+    if pending is not None:
+        d2h = end_one(pending)
     e1.record(stream)
     torch.cuda.synchronize()
     wall = (time.perf_counter() - t0) * 1e3 / args.steps
     ms = e0.elapsed_time(e1) / args.steps
     return {"value": voxels / (ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms, "wall_ms_per_step": wall,
             "h2d_bytes_per_step": int(36 * T), "d2h_bytes_per_step": int(d2h),
+            "pipelined": not args.no_pipeline,
             "path": "C ABI: svdag_upload_triangles from pinned host memory, build, svdag_download_level of every "
-                    "level of the SSVDAG and the CSVDAG into pinned host buffers"}
+                    "level of the SSVDAG and the CSVDAG into pinned host buffers; a step's upload and "
+                    "voxelization overlap the previous step's reductions and read-back"}
 
 
 # ---------------------------------------------------------------------------
