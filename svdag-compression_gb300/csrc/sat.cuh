@@ -644,20 +644,6 @@ SAT_HD int edge_test_box(float a, float b, bool neg_a, float u0, float w0, float
   return 2;
 }
 
-// One edge-axis test as a single value.  The reference rejects on the axis
-// iff min p > rad or max p < -rad, i.e. iff m = max(min p, -max p) > rad;
-// negating p (the Y tests) leaves m unchanged.  With edge_test_box's
-// thresholds, m > hi is a certain reject and m < lo a certain keep.  The
-// differences m - hi and m - lo have the signs of those comparisons (IEEE
-// subtraction of finite values, subnormals kept), so running maxima of them
-// over the nine tests decide "some test rejects" and "every test keeps".
-SAT_HD float edge_m(float a, float b, float u0, float w0, float u1, float w1) {
-  const F2 x = f2mul(F2{a, a}, F2{u0, u1});
-  const F2 y = f2mul(F2{b, b}, F2{w0, w1});
-  const F2 p = f2add(x, F2{-y.x, -y.y});
-  return fmax_(fmin_(p.x, p.y), -fmax_(p.x, p.y));
-}
-
 // Decision from the slab classes alone: 0 no overlap, 1 overlap, 2 the
 // full test is needed.
 SAT_HD int child_fast(const Pair32& P, int ci) {
@@ -742,56 +728,35 @@ SAT_HD bool child_full_src(const Pair32& P, const Src& S, int ci, unsigned* fall
   const float Wp = ffma(4.7f * kU32, V, ffma(4.4f * kU32, h, 1.05f * clo));
   const float hW = fadd(h, Wp), hmW = fsub(h, Wp);
   const int X = 0, Y = 1, Z = 2;
-  // test k's m = max(min p, -max p) and ab = fl(|a| + |b|) (edge_m)
-  auto edge = [&](int k, float& ab) -> float {
-    const int j = k / 3;
-    const float e[3] = {S.e(j, 0), S.e(j, 1), S.e(j, 2)};
-    switch (k) {
-      case 0: case 3:  // X01: a=e.z, b=e.y over v0, v2 on (y, z)
-        ab = fadd(fabsf_(e[Z]), fabsf_(e[Y]));
-        return edge_m(e[Z], e[Y], v[0][Y], v[0][Z], v[2][Y], v[2][Z]);
-      case 1: case 4:  // Y02: -a*v.x + b*v.z, a=e.z, b=e.x over v0, v2
-        ab = fadd(fabsf_(e[Z]), fabsf_(e[X]));
-        return edge_m(e[Z], e[X], v[0][X], v[0][Z], v[2][X], v[2][Z]);
-      case 2: case 8:  // Z12: a=e.y, b=e.x over v1, v2 on (x, y)
-        ab = fadd(fabsf_(e[Y]), fabsf_(e[X]));
-        return edge_m(e[Y], e[X], v[1][X], v[1][Y], v[2][X], v[2][Y]);
-      case 5:          // Z0: over v0, v1
-        ab = fadd(fabsf_(e[Y]), fabsf_(e[X]));
-        return edge_m(e[Y], e[X], v[0][X], v[0][Y], v[1][X], v[1][Y]);
-      case 6:          // X2: over v0, v1
-        ab = fadd(fabsf_(e[Z]), fabsf_(e[Y]));
-        return edge_m(e[Z], e[Y], v[0][Y], v[0][Z], v[1][Y], v[1][Z]);
-      default:         // 7, Y1: over v0, v1
-        ab = fadd(fabsf_(e[Z]), fabsf_(e[X]));
-        return edge_m(e[Z], e[X], v[0][X], v[0][Z], v[1][X], v[1][Z]);
-    }
-  };
-  auto skipped = [&](int k) {
-    return ((k == 0 || k == 3 || k == 6) && passX) || ((k == 1 || k == 4 || k == 7) && passY) ||
-           ((k == 2 || k == 5 || k == 8) && passZ);
-  };
-  // running maxima of m - hi and m - lo over the tests (see edge_m)
-  float dhi = -INFINITY, dlo = -INFINITY;
+  uint32_t rej = 0, unk = 0;
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
-    if (skipped(k)) continue;
-    float ab;
-    const float m = edge(k, ab);
-    dhi = fmax_(dhi, fsub(m, ffma(ab, hW, cd)));
-    dlo = fmax_(dlo, fsub(m, ffma(ab, hmW, -cd)));
-  }
-  if (dhi > 0.f) return false;  // one certain reject decides the AND of the 13 tests
-  if (!(dlo < 0.f)) {
-    // some test is undecided: those, in order, through the exact tiers
-#pragma unroll 1
-    for (int k = 0; k < 9; ++k) {
-      if (skipped(k)) continue;
-      float ab;
-      const float m = edge(k, ab);
-      if (!(m < ffma(ab, hmW, -cd)) && need64(3 + k)) return false;
+    if ((k == 0 || k == 3 || k == 6) && passX) continue;
+    if ((k == 1 || k == 4 || k == 7) && passY) continue;
+    if ((k == 2 || k == 5 || k == 8) && passZ) continue;
+    const int j = k / 3;
+    const float e[3] = {S.e(j, 0), S.e(j, 1), S.e(j, 2)};
+    int r;
+    switch (k) {
+      case 0: case 3:  // X01: a=e.z, b=e.y over v0, v2 on (y, z)
+        r = edge_test_box(e[Z], e[Y], false, v[0][Y], v[0][Z], v[2][Y], v[2][Z], fadd(fabsf_(e[Z]), fabsf_(e[Y])), hW, hmW, cd); break;
+      case 1: case 4:  // Y02: -a*v.x + b*v.z, a=e.z, b=e.x over v0, v2
+        r = edge_test_box(e[Z], e[X], true, v[0][X], v[0][Z], v[2][X], v[2][Z], fadd(fabsf_(e[Z]), fabsf_(e[X])), hW, hmW, cd); break;
+      case 2: case 8:  // Z12: a=e.y, b=e.x over v1, v2 on (x, y)
+        r = edge_test_box(e[Y], e[X], false, v[1][X], v[1][Y], v[2][X], v[2][Y], fadd(fabsf_(e[Y]), fabsf_(e[X])), hW, hmW, cd); break;
+      case 5:          // Z0: over v0, v1
+        r = edge_test_box(e[Y], e[X], false, v[0][X], v[0][Y], v[1][X], v[1][Y], fadd(fabsf_(e[Y]), fabsf_(e[X])), hW, hmW, cd); break;
+      case 6:          // X2: over v0, v1
+        r = edge_test_box(e[Z], e[Y], false, v[0][Y], v[0][Z], v[1][Y], v[1][Z], fadd(fabsf_(e[Z]), fabsf_(e[Y])), hW, hmW, cd); break;
+      default:         // 7, Y1: over v0, v1
+        r = edge_test_box(e[Z], e[X], true, v[0][X], v[0][Z], v[1][X], v[1][Z], fadd(fabsf_(e[Z]), fabsf_(e[X])), hW, hmW, cd); break;
     }
+    rej |= uint32_t(r == 1) << k;
+    unk |= uint32_t(r == 2) << k;
   }
+  if (rej) return false;  // one certain reject decides the AND of the 13 tests
+  for (uint32_t m = unk; m; m &= m - 1)
+    if (need64(3 + (__builtin_ctz_(m)))) return false;
 
   if (tx || ty || tz) return true;  // the plane test passes on a tangent grid plane
   if (P.flat) return true;          // axis-aligned triangle: implied by the bounding-box test (pair_slabs)
