@@ -461,10 +461,7 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
     pinned = torch.from_numpy(tris).pin_memory()
     ptr = pinned.data_ptr()
     T = tris.shape[0]
-    # two octrees on two streams: a step's triangles are copied into one while
-    # the other builds (the copy engine runs beside the kernels)
-    stream_b = torch.cuda.Stream(device=local)
-    octs = [sv.Octree(device=local, stream=stream.cuda_stream), sv.Octree(device=local, stream=stream_b.cuda_stream)]
+    o = sv.Octree(device=local, stream=stream.cuda_stream)
     red_streams = [torch.cuda.Stream(device=local), torch.cuda.Stream(device=local)]
     red_pool = concurrent.futures.ThreadPoolExecutor(2)
     lib = sv.load_gpu()
@@ -499,10 +496,8 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
             nbytes += n.value * (4 + (0 if leaf else 32) + (0 if (leaf or sdag) else 8) + (1 if sdag else 0))
         return nbytes
 
-    def upload(o):
+    def build_one():
         assert lib.svdag_upload_triangles(o._h, ptr, T) == 0
-
-    def build_one(o):
         if args.step_level:
             o.buildDAG(args.levels, args.step_level)
         else:
@@ -510,7 +505,7 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
             o.toDAG()
         o.initChildLevels()
 
-    def start_one(o):
+    def start_one():
         s = o.clone(stream=red_streams[0].cuda_stream)
         c = o.clone(stream=red_streams[1].cuda_stream) if have_csv else None
 
@@ -533,41 +528,29 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
         stream.wait_stream(red_streams[1])
         return d2h
 
-    for w in range(max(1, args.warmup)):
-        o = octs[w % 2]
-        upload(o)
-        build_one(o)
-        end_one(start_one(o))
+    for _ in range(max(1, args.warmup)):
+        build_one()
+        end_one(start_one())
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
     e0.record(stream)
-    stream_b.wait_event(e0)
     d2h = 0
     pending = None
-    pipelined = not args.no_pipeline
-    if pipelined:
-        upload(octs[0])
-    for i in range(args.steps):
-        o = octs[i % 2]
-        if not pipelined:
-            upload(o)
-        elif i + 1 < args.steps:
-            # the next step's triangles go into the other octree during this build
-            upload(octs[(i + 1) % 2])
-        build_one(o)
-        # this step's reductions and read-back run during the next build
+    for _ in range(args.steps):
+        # the next step's upload and voxelization overlap the previous
+        # step's reductions and read-back, unless --no-pipeline
+        build_one()
         if pending is not None:
             d2h = end_one(pending)
             pending = None
-        pending = start_one(o)
-        if not pipelined:
+        pending = start_one()
+        if args.no_pipeline:
             d2h = end_one(pending)
             pending = None
     if pending is not None:
         d2h = end_one(pending)
-    stream.wait_stream(stream_b)
     e1.record(stream)
     torch.cuda.synchronize()
     wall = (time.perf_counter() - t0) * 1e3 / args.steps
@@ -576,9 +559,8 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
             "h2d_bytes_per_step": int(36 * T), "d2h_bytes_per_step": int(d2h),
             "pipelined": not args.no_pipeline,
             "path": "C ABI: svdag_upload_triangles from pinned host memory, build, svdag_download_level of every "
-                    "level of the SSVDAG and the CSVDAG into pinned host buffers; two octrees alternate: a "
-                    "step's triangles are copied in during the previous step's build, and its reductions and "
-                    "read-back run during the next step's build"}
+                    "level of the SSVDAG and the CSVDAG into pinned host buffers; a step's upload and "
+                    "voxelization overlap the previous step's reductions and read-back"}
 
 
 # ---------------------------------------------------------------------------
