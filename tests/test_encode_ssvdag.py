@@ -65,3 +65,21 @@ def test_import_rejects_inconsistent_children():
     ch0[0] = 0xFFFFFFFE
     assert lib.svdag_import_level(o._h, 1, 1, hdr1.ctypes.data, None) == 0
     assert lib.svdag_import_level(o._h, 0, 1, hdr0.ctypes.data, ch0.ctypes.data) == 1
+
+
+def test_gpu_ssvdag_large_levels_equal_host_encoder(tmp_path):
+    """A 1025^2 terrain at depth 11: levels of 10^5 nodes, so the GPU
+    ref-count order runs its parallel partition rounds on real pointer
+    counts (mostly 1-2, a long tail) before the bytes are compared."""
+    o = sv.Octree()
+    o.upload_triangles(sv.terrain(1025, 8, 0.3, 5))
+    o.buildSVO(11)
+    o.toDAG()
+    o.initChildLevels()
+    o.toSDAG()
+    assert max(o.level_count(l) for l in range(11)) > 100000
+    host = str(tmp_path / "host.ssvdag")
+    sv.write_encoded(host, "ssvdag", o.pool(), o.stats()["n_nodes"], 3)
+    gpu = str(tmp_path / "gpu.ssvdag")
+    o.save_ssvdag(gpu)
+    assert open(gpu, "rb").read() == open(host, "rb").read()
