@@ -20,6 +20,7 @@ import argparse
 import concurrent.futures
 import ctypes
 import datetime
+import hashlib
 import json
 import os
 import statistics
@@ -27,6 +28,8 @@ import subprocess
 import sys
 import tempfile
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "svdag-compression_gb300")
@@ -197,6 +200,49 @@ def model_bytes(info, T):
     b_sdag = sum((R + 13) * D[l] + R * S[l] + (64 * D[l - 1] if l else 0) for l in range(L))
     b_csv = sum((R + 16) * D[l] + R * C[l] for l in range(L)) if C else None
     return {"k_expand": b_vox, "vox": b_vox, "dag": b_dag, "sdag": b_sdag, "csv": b_csv}
+
+
+def pool_digest(pool):
+    """SHA-256 over a node pool's levels (u64 node count, then the 48-byte
+    records: hdr, children, child levels, invariant) -- the form of the
+    digests in tests/golden/golden.json, which the reference's own build
+    made on the same seeded scenes."""
+    import numpy as np
+
+    h = hashlib.sha256()
+    for lev in pool:
+        h.update(np.uint64(len(lev)).tobytes())
+        h.update(np.ascontiguousarray(lev).tobytes())
+    return h.hexdigest()
+
+
+def golden_case(args):
+    """The golden fixture of this workload, if the reference's build was run
+    on it (tests/golden/make_golden.py), else None."""
+    if args.workload != "terrain" or args.step_level:
+        return None
+    name = "terrain%d_L%d" % (args.grid, args.levels)
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+            g = json.load(f).get(name)
+    except (OSError, ValueError):
+        return None
+    # the fixture must be of this very scene (seed 7 is the fixture's seed)
+    if g is None or args.seed != 7 or g["levels"] != args.levels:
+        return None
+    return name, g
+
+
+def parity_check(args, digests, counts):
+    """Compares the digests of the last timed step's pools with the golden
+    fixture: "golden-match", "golden-mismatch: ..." or None (no fixture)."""
+    gc = golden_case(args)
+    if gc is None:
+        return None, None
+    name, g = gc
+    bad = [k for k in ("svo", "dag", "sdag", "csv") if k in digests and digests[k] != g[k]["digest"]]
+    bad += ["%s counts" % k for k in counts if counts[k] != g[k]["counts"]]
+    return ("golden-match" if not bad else "golden-mismatch: " + ", ".join(bad)), name
 
 
 def run_ours(args, rank, local, world):
@@ -398,6 +444,18 @@ def run_ours(args, rank, local, world):
                "phases_ms_per_step": {ph: sum(ms for _, ms in phase_prof.get(ph, {}).values()) / args.steps
                                       for ph in ("voxelize", "dag", "sdag", "csv")}}
 
+    # --- parity of the last timed step's pools with the reference's golden
+    # digests (after the timed regions; the SVO comes from level_info's build)
+    parity, parity_case = None, None
+    if golden_case(args) is not None:
+        digests = {"dag": pool_digest(base.pool()), "sdag": pool_digest(s_last.pool())}
+        if info.get("svo_digest"):
+            digests["svo"] = info["svo_digest"]
+        if c_last is not None:
+            digests["csv"] = pool_digest(c_last.pool())
+        counts = {k: info[k] for k in ("svo", "dag", "sdag", "csv") if info.get(k) is not None}
+        parity, parity_case = parity_check(args, digests, counts)
+
     # --- e2e through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
@@ -415,6 +473,11 @@ def run_ours(args, rank, local, world):
                    "csvdag_in_step": bool(have_csv),
                    "frontier_pairs": int(info["frontier"][0]), "sat_fp64_fallbacks": int(info["sat_fallbacks"]),
                    "l2": "inputs larger than L2 (triangles %d MB, node pools > 129 MB)" % (36 * T // 10**6),
+                   "parity": parity,
+                   "parity_detail": ("SHA-256 of the last timed step's SVO, DAG, SSVDAG and CSVDAG pools and their "
+                                     "per-level counts against the digests the reference's own build (compiled "
+                                     "from its sources) wrote for this scene: tests/golden/golden.json[%s]"
+                                     % parity_case) if parity_case else None,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clk, "gpu_launches": int(launches), "roofline": roof, "reduction_roofline": red, "e2e": e2e,
         "pipelined": not args.no_pipeline,
@@ -441,13 +504,15 @@ def level_info(sv, base, s_last, args):
     else:
         o.buildSVO(levels)
         svo = [o.level_count(l) for l in range(levels)]
+        svo_digest = pool_digest(o.pool()) if golden_case(args) else None
     st = o.stats()
     if not args.step_level:
         o.toDAG()
     dag = [o.level_count(l) for l in range(levels)]
     o.close()
     return {"svo": svo, "svo_total": st["n_nodes_svo"], "dag": dag, "frontier": [st["frontier_pairs"]],
-            "sdag": [s_last.level_count(l) for l in range(levels)], "sat_fallbacks": st["sat_fallbacks"]}
+            "sdag": [s_last.level_count(l) for l in range(levels)], "sat_fallbacks": st["sat_fallbacks"],
+            "svo_digest": None if args.step_level else svo_digest}
 
 
 def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
@@ -564,18 +629,28 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(args, frac_rows):
-    import numpy as np
-
-    import svdag_gb300 as sv
-
-    tris = scene(args, sv)  # the terrain rows come first (the city's boxes follow them)
+def cpu_scene(args, oracle_py, frac_rows=1.0):
+    """The workload's scene for the CPU legs, generated by the oracle library
+    (same generator source as the GPU arm's; no product library is loaded).
+    frac_rows < 1 keeps the first rows of the terrain (warm-up samples)."""
+    if args.workload == "city":
+        tris = oracle_py.city(args.grid, args.boxes, args.levels, args.seed)
+    else:
+        tris = oracle_py.terrain(args.grid, 8, 0.3, args.seed)
+    if frac_rows >= 1.0:
+        return tris, args.grid - 1
     g = args.grid - 1
     rows = max(1, int(g * frac_rows))
     return np.ascontiguousarray(tris[: 2 * g * rows]), rows
 
 
-def cpu_build(oracle_py, tris, levels, chunked, threads, step_level=2):
+def cpu_build(oracle_py, tris, levels, chunked, threads, step_level=2, csv=True):
+    """The reference's path on the host: buildDAG (chunked, OpenMP over the
+    sub-octrees as geom_octree.cpp:331 does) or buildSVO + toDAG, then
+    initChildLevels, and toSDAG and mergeAcrossAllLevels on two copies of
+    the DAG -- concurrently in two host threads when threads > 1 (each of
+    them is single-threaded in the reference).  Returns (voxels, seconds,
+    SVO/DAG/SDAG/CSVDAG node counts)."""
     o = oracle_py.OracleOctree()
     t0 = time.perf_counter()
     if chunked:
@@ -585,52 +660,87 @@ def cpu_build(oracle_py, tris, levels, chunked, threads, step_level=2):
         o.toDAG()
     o.initChildLevels()
     s = o.clone()
-    s.toSDAG()
-    c = o.clone()
-    c.mergeAcrossAllLevels()
+    c = o.clone() if csv else None
+    if threads > 1 and c is not None:
+        with concurrent.futures.ThreadPoolExecutor(2) as ex:
+            fs = ex.submit(s.toSDAG)
+            fc = ex.submit(c.mergeAcrossAllLevels)
+            fs.result()
+            fc.result()
+    else:
+        s.toSDAG()
+        if c is not None:
+            c.mergeAcrossAllLevels()
     dt = time.perf_counter() - t0
-    return o.stats()["n_total_voxels"], dt
+    st = o.stats()
+    counts = {"svo": st["n_nodes_svo"], "dag": st["n_nodes_dag"], "sdag": s.stats()["n_nodes_sdag"],
+              "csv": c.stats()["n_nodes"] if c is not None else None}
+    return st["n_total_voxels"], dt, counts
 
 
 def run_cpu_baseline(args):
+    """One full build of the workload's scene by the oracle port on all host
+    cores (chunked OpenMP buildDAG, step level 2, as the reference's
+    svbuilder runs it for numBuildSteps = 2)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
 
-    frac = 1.0 / 256 if args.workload == "city" else 1.0 / 8
-    tris, rows = cpu_sample(args, frac)
-    vox, dt = cpu_build(oracle_py, tris, args.levels, chunked=False, threads=1)
-    return {"value": vox / dt / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": "first %d of %d terrain rows (%d triangles, %d voxels) at depth %d, full path "
-                      "(buildSVO, toDAG, toSDAG, mergeAcrossAllLevels), single thread, %.1f s"
-                      % (rows, args.grid - 1, tris.shape[0], vox, args.levels, dt)}
+    cores = os.cpu_count() or 1
+    step = args.step_level or 2
+    if args.workload == "city":
+        # the depth-15 city is ~10^4 s of CPU work: a 1/64 slab of its rows
+        tris, rows = cpu_scene(args, oracle_py, 1.0 / 64)
+        what = "first %d of %d terrain rows of the city scene" % (rows, args.grid - 1)
+    else:
+        tris, rows = cpu_scene(args, oracle_py)
+        what = "the full scene"
+    vox, dt, counts = cpu_build(oracle_py, tris, args.levels, chunked=True, threads=cores, step_level=step)
+    return {"value": vox / dt / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%s (%d triangles, %d voxels) at depth %d, one build: chunked OpenMP buildDAG (step level "
+                      "%d) on %d threads, then toSDAG and mergeAcrossAllLevels concurrently on two threads, "
+                      "%.1f s" % (what, tris.shape[0], vox, args.levels, step, cores, dt)}
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU path (restated by the oracle: the reference's
+    sources are not present where the benchmark runs) on the same workload
+    as the GPU arm: every timed step is one full build of the full scene.
+    Warm-up steps run the same path on the first 1/16 of the terrain rows
+    (thread pool, allocator and caches warm; a full warm-up build would add
+    a quarter of a minute each)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
 
     if rank != 0:
         return None
     cores = os.cpu_count() or 1
-    frac = 1.0 / 256 if args.workload == "city" else 1.0 / 16
     step = args.step_level or 2
-    tris, rows = cpu_sample(args, frac)
+    full = args.workload != "city"
+    tris, rows = cpu_scene(args, oracle_py, 1.0 if full else 1.0 / 64)
+    warm, _ = cpu_scene(args, oracle_py, 1.0 / 16 if full else 1.0 / 256)
     for _ in range(max(args.warmup, 0)):
-        cpu_build(oracle_py, tris, args.levels, chunked=True, threads=cores, step_level=step)
+        cpu_build(oracle_py, warm, args.levels, chunked=True, threads=cores, step_level=step)
     times = []
     vox = 0
+    counts = None
     for _ in range(args.steps):
-        vox, dt = cpu_build(oracle_py, tris, args.levels, chunked=True, threads=cores, step_level=step)
+        vox, dt, counts = cpu_build(oracle_py, tris, args.levels, chunked=True, threads=cores, step_level=step)
         times.append(dt)
     dt = sum(times) / len(times)
     v = vox / dt / 1e6
-    sample = ("first %d of %d terrain rows (%d triangles, %d voxels) at depth %d: chunked OpenMP buildDAG "
-              "(step level %d) + toSDAG + mergeAcrossAllLevels, restated CPU port" %
-              (rows, args.grid - 1, tris.shape[0], vox, args.levels, step))
+    sample = ("%s (%d triangles, %d voxels) at depth %d, every step one full build: chunked OpenMP buildDAG (step "
+              "level %d, %d threads) + toSDAG and mergeAcrossAllLevels (concurrently, two threads), restated CPU "
+              "port of the reference's code; node counts SVO %d, DAG %d, SSVDAG %d, CSVDAG %s"
+              % ("the full scene" if full else "first %d of %d terrain rows" % (rows, args.grid - 1),
+                 tris.shape[0], vox, args.levels, step, cores, counts["svo"], counts["dag"], counts["sdag"],
+                 counts["csv"]))
     return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64-exact SAT (certified fp32 filter) + u32 keys", "data": "synthetic", "impl": "reference",
-            "config": {"workload": workload_name(args), "sample": sample},
+            "vs_baseline": None, "dtype": "f64 SAT + u32 keys (CPU)", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": workload_name(args), "sample": sample, "same_config": full,
+                       "warmup_sample": "first 1/16 of the terrain rows" if full else "first 1/256 of the rows",
+                       "step_seconds": times},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

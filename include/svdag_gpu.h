@@ -239,6 +239,11 @@ int svdag_download_outside_masks(svdag_ctx* ctx, uint32_t level, uint8_t* masks)
  * and reading it clears the accumulated records. */
 int svdag_profile_enable(svdag_ctx* ctx, int enable);
 int svdag_profile_report(svdag_ctx* ctx, char* buf, uint64_t capacity);
+/* Number of stream-ordered device allocations (cudaMallocAsync) this library
+ * has made in the process, over all contexts and threads; no counterpart in
+ * the reference.  A diagnostic: the difference across a call shows whether
+ * that call allocated device memory. */
+uint64_t svdag_device_alloc_count(void);
 
 /* ---- Voxel-brick chunks (no counterpart in the reference, which voxelizes
  * triangles only; a voxel grid enters it as node pools through
@@ -373,9 +378,22 @@ int svdag_mlp_embed(svdag_mlp* mlp, const float* x, uint32_t n, float* out);
  * it and corrupt each other; serialise them.  Its contents need not be zero:
  * each call clears what it reads first.  The first call on a device looks
  * the array up (cudaGetSymbolAddress, which can load the module and commit
- * its memory); make that first call before any stream capture begins.  Like
- * svdag_reduce_dag, the call synchronises its stream once per level and on
- * return.  Per-kernel profiling (svdag_profile_enable) does not cover it. */
+ * its 64 MiB); make that first call before any stream capture begins, and
+ * before the caller commits the GPU's memory to its own pools -- if the
+ * array cannot be committed then, the call returns SVDAG_ERR_OOM.  The
+ * device address is kept for the life of the process; after a
+ * cudaDeviceReset it is stale, so do not call this entry point again in that
+ * process.  Like svdag_reduce_dag, the call synchronises its stream once per
+ * level and on return.  Per-kernel profiling (svdag_profile_enable) does not
+ * cover it.
+ *
+ * On success the octree is left as svdag_reduce_dag leaves it, except that
+ * the SVO's outside masks (svdag_flood_fill), which no longer apply, are
+ * released by the next other call on the context or by svdag_destroy
+ * instead of at once.  If the hash table's probe limit is hit (only a
+ * pathological key set can do it) the levels have already been rewritten
+ * when the error is read: the call returns SVDAG_ERR_OVERFLOW with the
+ * octree in state SVDAG_S_EMPTY, to be rebuilt. */
 #define SVDAG_NOALLOC_SCRATCH_BYTES (64ull << 20)
 #define SVDAG_NOALLOC_MAX_LEVEL_NODES 1048576ull
 int svdag_reduce_dag_noalloc(svdag_ctx* ctx);

@@ -51,6 +51,10 @@ _SIGS = {
     "ora_get_level": (_I, [_VP, _U32, _VP]),
     "ora_get_stats": (_I, [_VP, ctypes.POINTER(_OraStats)]),
     "ora_tri_box": (_I, [_VP, ctypes.c_double, _VP]),
+    # seeded scene generators (the same source as the product's host library)
+    "svdag_synth_terrain_count": (_U64, [_U32]),
+    "svdag_synth_terrain": (_I, [_U32, _U32, ctypes.c_double, _U64, _VP]),
+    "svdag_synth_boxes": (_I, [_VP, _VP, _U64, _VP]),
 }
 _lib = None
 
@@ -68,6 +72,35 @@ def load():
             f.argtypes = a
         _lib = lib
     return _lib
+
+
+def terrain(grid=2048, octaves=8, height=0.3, seed=7):
+    """The seeded fBm terrain (float[9] per triangle), generated inside the
+    oracle library: the CPU legs need no product library for their input."""
+    L = load()
+    out = np.empty((L.svdag_synth_terrain_count(grid), 9), np.float32)
+    assert L.svdag_synth_terrain(grid, octaves, height, seed, out.ctypes.data) == 0
+    return out
+
+
+def boxes(lo, hi):
+    L = load()
+    lo = np.ascontiguousarray(lo, np.float32)
+    hi = np.ascontiguousarray(hi, np.float32)
+    out = np.empty((lo.shape[0] * 12, 9), np.float32)
+    assert L.svdag_synth_boxes(lo.ctypes.data, hi.ctypes.data, lo.shape[0], out.ctypes.data) == 0
+    return out
+
+
+def city(grid=4096, n_boxes=200000, levels=15, seed=15, octaves=8, height=0.3):
+    """The depth-15 city scene (terrain + boxes), as the product's generator
+    builds it; the box placement is the package's numpy code (no native
+    library is loaded by importing it)."""
+    import svdag_gb300 as sv  # pure Python at import time
+
+    t = terrain(grid, octaves, height, seed)
+    lo, hi = sv.city_box_extents(t, grid, n_boxes, levels, seed)
+    return np.concatenate([t, boxes(lo, hi)])
 
 
 class OracleOctree:

@@ -19,7 +19,9 @@ LIB = os.path.join(PKG, "lib")
 OBJ = os.path.join(PKG, "_build")
 INC = os.path.join(ROOT, "include")
 ORACLE = os.path.join(ROOT, "oracle")
-REFERENCE = "/root/reference"
+# The reference checkout: $SVDAG_REFERENCE, else a "reference" directory
+# beside this repository.  Only the checker's build (build_reference) reads it.
+REFERENCE = os.environ.get("SVDAG_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 
 NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
@@ -38,10 +40,12 @@ def _run(cmd, cwd=None):
 
 
 def _newer(target, deps):
+    """True when `target` exists and is newer than every dependency and than
+    this recipe (a change of sources or flags here rebuilds)."""
     if not os.path.exists(target):
         return False
     t = os.path.getmtime(target)
-    return all(os.path.getmtime(d) <= t for d in deps if os.path.exists(d))
+    return all(os.path.getmtime(d) <= t for d in list(deps) + [os.path.abspath(__file__)] if os.path.exists(d))
 
 
 def _cu_object(src):
@@ -92,10 +96,15 @@ def build_cli(gpu_lib):
 def build_oracle():
     d = os.path.join(ORACLE, "build")
     os.makedirs(d, exist_ok=True)
-    srcs = [os.path.join(ORACLE, "svdag_oracle.cpp"), os.path.join(ORACLE, "ssvdag_raycast.cpp")]
+    # the seeded scene generators are compiled in as well, so that the CPU
+    # legs (reference arm, CPU baseline) synthesise their inputs without
+    # loading the product's libraries
+    srcs = [os.path.join(ORACLE, "svdag_oracle.cpp"), os.path.join(ORACLE, "ssvdag_raycast.cpp"),
+            os.path.join(PKG, "host", "synth.cpp")]
     out = os.path.join(d, "liboracle.so")
-    if not _newer(out, srcs + [os.path.join(ORACLE, "svdag_oracle.h")]):
-        _run([CXX, "-O3", "-std=gnu++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"] + srcs + ["-o", out])
+    if not _newer(out, srcs + [os.path.join(ORACLE, "svdag_oracle.h"), os.path.join(PKG, "host", "svdag_host.h")]):
+        _run([CXX, "-O3", "-std=gnu++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+              "-I", os.path.join(PKG, "host")] + srcs + ["-o", out])
     return out
 
 

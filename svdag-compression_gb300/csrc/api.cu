@@ -1,4 +1,5 @@
 // C ABI of the SVDAG construction path (include/svdag_gpu.h).
+#include <algorithm>
 #include <cstring>
 #include <new>
 
@@ -49,6 +50,7 @@ int guarded(svdag_ctx* h, F&& f) {
   if (!h) return SVDAG_ERR_INVALID_ARG;
   try {
     SVDAG_CUDA(cudaSetDevice(h->c.device));
+    h->c.retired.clear();
     f(h->c);
     h->c.last_error.clear();
     return SVDAG_OK;
@@ -74,18 +76,23 @@ double timed(Ctx& c, F&& f) {
   return double(ms);
 }
 
+// Copies the live part of a level: `per_node` elements per node (at least one
+// node's worth, so that an empty level keeps a non-null buffer), not the
+// buffer's capacity -- a level reduced in place keeps its SVO-sized buffers.
 void copy_level(const Ctx& src, svdag::Level& dst, const svdag::Level& s, cudaStream_t st) {
   dst.n = s.n;
-  auto cp = [&](auto& d, const auto& v) {
+  const uint64_t nodes = s.n ? s.n : 1;
+  auto cp = [&](auto& d, const auto& v, uint64_t per_node) {
     if (!v.get()) return;
-    d.alloc(v.n, st);
-    SVDAG_CUDA(cudaMemcpyAsync(d.get(), v.get(), v.bytes(), cudaMemcpyDeviceToDevice, st));
+    const uint64_t cnt = std::min<uint64_t>(v.n, per_node * nodes);
+    d.alloc(cnt, st);
+    SVDAG_CUDA(cudaMemcpyAsync(d.get(), v.get(), cnt * sizeof(*v.get()), cudaMemcpyDeviceToDevice, st));
   };
-  cp(dst.hdr, s.hdr);
-  cp(dst.ch, s.ch);
-  cp(dst.inv, s.inv);
-  cp(dst.clev, s.clev);
-  cp(dst.outm, s.outm);
+  cp(dst.hdr, s.hdr, 1);
+  cp(dst.ch, s.ch, 8);
+  cp(dst.inv, s.inv, 1);
+  cp(dst.clev, s.clev, 8);
+  cp(dst.outm, s.outm, 1);
   (void)src;
 }
 
@@ -108,6 +115,8 @@ const char* svdag_status_string(int s) {
 }
 
 const char* svdag_last_error(const svdag_ctx* h) { return h ? h->c.last_error.c_str() : "null context"; }
+
+uint64_t svdag_device_alloc_count(void) { return svdag::g_device_allocs.load(std::memory_order_relaxed); }
 
 int svdag_create(svdag_ctx** out, int device, void* stream) {
   if (!out) return SVDAG_ERR_INVALID_ARG;
@@ -154,6 +163,7 @@ int svdag_destroy(svdag_ctx* h) {
   cudaSetDevice(c.device);
   // every stream-ordered buffer goes back before its stream is destroyed
   c.lev.clear();
+  c.retired.clear();
   c.owned_tris.release();
   c.ss_inner.clear();
   c.ss_leaves.release();

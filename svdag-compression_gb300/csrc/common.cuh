@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cstdio>
 #include <stdexcept>
 #include <string>
@@ -86,6 +87,11 @@ inline unsigned grid_for(const Exec& ex, uint64_t n, unsigned threads, unsigned 
     }                                                                    \
   } while (0)
 
+// Stream-ordered device allocations made by this library in the process
+// (every DBuf::alloc of a non-empty buffer); read by
+// svdag_device_alloc_count().
+inline std::atomic<uint64_t> g_device_allocs{0};
+
 // Stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync).
 template <class T>
 struct DBuf {
@@ -106,7 +112,10 @@ struct DBuf {
     release();
     s = st;
     n = count;
-    if (count) SVDAG_CUDA(cudaMallocAsync((void**)&p, sizeof(T) * (count ? count : 1), st));
+    if (count) {
+      g_device_allocs.fetch_add(1, std::memory_order_relaxed);
+      SVDAG_CUDA(cudaMallocAsync((void**)&p, sizeof(T) * (count ? count : 1), st));
+    }
   }
   void release() {
     if (p) cudaFreeAsync(p, s);

@@ -50,6 +50,11 @@ struct Ctx {
   svdag_stats st{};
   std::string last_error;
 
+  // Outside masks taken off the levels by svdag_reduce_dag_noalloc, which
+  // may not free device memory: released by a later call on the context
+  // (every entry point that can allocate) or by svdag_destroy.
+  std::vector<DBuf<uint8_t>> retired;
+
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   Profiler prof;
 

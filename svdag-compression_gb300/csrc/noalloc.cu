@@ -6,6 +6,7 @@
 // module loading, its device memory is committed only when this entry point
 // is first used.
 #include <mutex>
+#include <new>
 
 #include "ctx.cuh"
 
@@ -27,9 +28,14 @@ uint8_t* static_scratch(int device) {
   if (!g_addr[device]) {
     void* p = nullptr;
     const cudaError_t rc = cudaGetSymbolAddress(&p, g_dag_scratch);
-    if (rc != cudaSuccess || p == nullptr)
-      throw svdag::Error(SVDAG_ERR_CUDA, std::string("svdag_reduce_dag_noalloc: cudaGetSymbolAddress of the static "
-                                                     "scratch failed: ") + cudaGetErrorString(rc));
+    if (rc != cudaSuccess || p == nullptr) {
+      // loading the module commits the array; without room for it the
+      // lookup fails with an allocation error
+      const int code = rc == cudaErrorMemoryAllocation ? SVDAG_ERR_OOM : SVDAG_ERR_CUDA;
+      if (rc != cudaSuccess) cudaGetLastError();
+      throw svdag::Error(code, std::string("svdag_reduce_dag_noalloc: cudaGetSymbolAddress of the static "
+                                           "scratch failed: ") + cudaGetErrorString(rc));
+    }
     g_addr[device] = static_cast<uint8_t*>(p);
   }
   return g_addr[device];
@@ -50,11 +56,19 @@ extern "C" int svdag_reduce_dag_noalloc(svdag_ctx* h) {
     float ms = 0.f;
     SVDAG_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
     c.st.dag_ms = double(ms);
+    // The outside masks belong to the SVO (svdag_reduce_dag drops them too).
+    // Freeing is not allowed here, so they leave the levels and are released
+    // by a later call on the context or by svdag_destroy.
+    for (auto& L : c.lev)
+      if (L.outm.get()) c.retired.push_back(std::move(L.outm));
     c.last_error.clear();
     return SVDAG_OK;
   } catch (const svdag::Error& e) {
     c.last_error = e.what();
     return e.code;
+  } catch (const std::bad_alloc&) {
+    c.last_error = "svdag_reduce_dag_noalloc: host allocation failed";
+    return SVDAG_ERR_OOM;
   } catch (const std::exception& e) {
     c.last_error = e.what();
     return SVDAG_ERR_CUDA;

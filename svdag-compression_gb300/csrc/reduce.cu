@@ -576,7 +576,14 @@ void phase_reduce_dag_scratch(Ctx& c, uint8_t* scratch, uint64_t capacity) {
     }
     nnodes += L.n;
   }
-  check_err(ex, d_err, "toDAG");
+  try {
+    check_err(ex, d_err, "toDAG");
+  } catch (const Error&) {
+    // the levels were compacted in place before the error was read: the
+    // octree is no longer the SVO it was, and must be rebuilt
+    c.state = SVDAG_S_EMPTY;
+    throw;
+  }
   c.st.n_nodes_dag = nnodes;
   c.st.n_nodes = nnodes;
   c.state = SVDAG_S_DAG;

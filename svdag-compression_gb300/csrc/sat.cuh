@@ -16,7 +16,8 @@
 //
 // Error model: fl(a op b) = (a op b)(1 + d), |d| <= u (u32 = 2^-24,
 // u64 = 2^-53), plus an absolute slack of 2^-100 against fp32 underflow.
-// Bounds (exact-real anchors t - c, t_j - t_i; derivation in the design doc):
+// Bounds (exact-real anchors t - c, t_j - t_i; each follows from the model
+// above by adding the relative errors of the operations in order):
 //   edge-axis value p = a*u - b*w:  |p_f - p*| <= 4.1 u32 S + 1.02 (|a|+|b|) clo
 //                                   S = |a u| + |b w|,   clo = |c - fl32(c)|
 //   rad = (|a|+|b|) h:              |rad_f - rad*| <= 3.1 u32 rad

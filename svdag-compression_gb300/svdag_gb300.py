@@ -78,6 +78,7 @@ GPU_SYMBOLS = {
     "svdag_profile_enable": (_I, [_VP, _I]),
     "svdag_profile_report": (_I, [_VP, ctypes.c_char_p, _U64]),
     "svdag_reduce_dag_noalloc": (_I, [_VP]),
+    "svdag_device_alloc_count": (_U64, []),
     "svdag_flood_fill": (_I, [_VP, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     "svdag_download_outside_masks": (_I, [_VP, _U32, _VP]),
     "svdag_synth_noise_bricks": (_I, [_VP, _U32, _U64, ctypes.c_double, _VP, ctypes.POINTER(ctypes.c_float)]),
@@ -225,6 +226,13 @@ def city(grid=4096, n_boxes=200000, levels=15, seed=15, octaves=8, height=0.3):
     standing on the terrain (base 2 voxels below the lowest of the four
     terrain vertices around the box centre)."""
     t = terrain(grid, octaves, height, seed)
+    lo, hi = city_box_extents(t, grid, n_boxes, levels, seed)
+    return np.concatenate([t, boxes(lo, hi)])
+
+
+def city_box_extents(t, grid, n_boxes, levels, seed):
+    """The city's box corners (lo, hi: float arrays of n_boxes x 3) placed on
+    the terrain triangles `t` (numpy only)."""
     n = grid
     cells = t[: 2 * (n - 1) ** 2].reshape(n - 1, n - 1, 2, 9)
     hgt = np.empty((n, n), np.float32)  # [j, i] -> y at grid vertex (i, j)
@@ -245,7 +253,7 @@ def city(grid=4096, n_boxes=200000, levels=15, seed=15, octaves=8, height=0.3):
     base = np.maximum(base - 2 * vox, 0.0)
     lo = np.stack([cx - fx / 2, base, cz - fz / 2], axis=1)
     hi = np.stack([cx + fx / 2, np.minimum(base + hy, 1.0), cz + fz / 2], axis=1)
-    return np.concatenate([t, boxes(lo, hi)])
+    return lo, hi
 
 
 def write_obj(path, tris, pin_unit_cube=True):
@@ -497,6 +505,12 @@ class Octree:
 
 # --------------------------------------------------------------------------
 # voxel-brick chunks
+
+def device_alloc_count():
+    """Stream-ordered device allocations the library has made in this process
+    (svdag_device_alloc_count)."""
+    return int(load_gpu().svdag_device_alloc_count())
+
 
 def noise_bricks(depth, seed, fill, device=0):
     """Seeded synthetic chunk: a torch uint8 CUDA tensor of 8^(depth-1)

@@ -29,7 +29,12 @@ SCENES = {
     "terrain129_L9_step1": lambda: sv.terrain(129, 8, 0.3, 11),
     "terrain257_L10": lambda: sv.terrain(257, 8, 0.3, 3),
     "boxes_L8": lambda: box_scene(300, 8, 21),
+    # the benchmark's headline workload (8,396,796 triangles, depth 12)
+    "terrain2048_L12": lambda: sv.terrain(2048, 8, 0.3, 7),
 }
+
+# golden cases too large for the CPU suite's single-threaded oracle runs
+HEAVY = {"terrain2048_L12"}
 
 
 def golden():

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import oracle_py
-from _scenes import SCENES, golden
+from _scenes import HEAVY, SCENES, golden
 
 G = golden()
 
@@ -18,7 +18,9 @@ def test_scene_generator_is_reproducible(name):
     assert hashlib.sha256(np.ascontiguousarray(tris).tobytes()).hexdigest() == G[name]["tris_sha256"]
 
 
-@pytest.mark.parametrize("name", sorted(G))
+# the headline scene's single-threaded oracle run takes minutes; its GPU
+# build is checked against the same golden digests in the GPU suite
+@pytest.mark.parametrize("name", sorted(set(G) - HEAVY))
 def test_oracle_matches_reference_pools(name):
     g = G[name]
     tris = SCENES[name]()

@@ -1,9 +1,12 @@
 """svdag_reduce_dag_noalloc -- toDAG on the library's static device scratch,
-no allocation -- against svdag_reduce_dag: the same pools and counts, call
-after call (big and small trees in a row, so what one call leaves in the
-scratch cannot leak into the next), the in-place levels read by the later
-phases like freshly allocated ones, and a tree too big for the scratch
-rejected with the octree unchanged."""
+for callers that cannot allocate device memory mid-work -- against
+svdag_reduce_dag: the same pools and counts, call after call (big and small
+trees in a row, so what one call leaves in the scratch cannot leak into the
+next), no device allocation during the call (the library's allocation
+counter stands still across it and moves across svdag_reduce_dag), the same
+octree state afterwards (the SVO's outside masks gone, clones the same size),
+the in-place levels read by the later phases like freshly allocated ones,
+and a tree too big for the scratch rejected with the octree unchanged."""
 import numpy as np
 import pytest
 
@@ -47,6 +50,37 @@ def test_two_calls_in_a_row_match_reduce_dag():
             _same_pool(o.pool(), want.pool())
             o.initChildLevels()  # the reference digests carry child levels
             assert oracle_py.pool_digest(o.pool()) == g["dag"]["digest"]
+
+
+def test_no_device_allocation_and_same_state():
+    name = "terrain257_L10"
+    g = G[name]
+    svo = _svo(SCENES[name](), g["levels"])
+    svo.hiddenGeometryFloodfill()  # outside masks on the SVO's levels
+    want, o = svo.clone(), svo.clone()
+    o.toDAG_noalloc()  # the first call on the device looks the array up
+    o = svo.clone()
+    n0 = sv.device_alloc_count()
+    o.toDAG_noalloc()
+    assert sv.device_alloc_count() == n0, "svdag_reduce_dag_noalloc allocated device memory"
+    n1 = sv.device_alloc_count()
+    want.toDAG()
+    assert sv.device_alloc_count() > n1  # the counter does see the allocating path
+    _same_pool(o.pool(), want.pool())
+    for oc in (o, want):
+        with pytest.raises(sv.SvdagError) as e:  # outside masks belong to the SVO only
+            _masks(oc, 1)
+        assert e.value.status == 2  # SVDAG_ERR_INVALID_STATE
+    # a clone copies only the reduced levels' live nodes, whichever path reduced them
+    a, b = o.clone(), want.clone()
+    _same_pool(a.pool(), b.pool())
+    assert a.stats()["n_nodes_dag"] == b.stats()["n_nodes_dag"] == g["nNodesDAG"]
+
+
+def _masks(o, level):
+    out = np.zeros(max(o.level_count(level), 1), np.uint8)
+    o._check(o._lib.svdag_download_outside_masks(o._h, level, out.ctypes.data))
+    return out
 
 
 def test_later_phases_read_the_reduced_levels():
