@@ -100,6 +100,17 @@ int svdag_voxelize(svdag_ctx* ctx, uint32_t levels, const double bbox[6]);
  * reference's order and reduced by one toDAG; leaves the octree in DAG state
  * with the reference's node order.  1 <= stepLevel < levels - 1. */
 int svdag_build_dag(svdag_ctx* ctx, uint32_t levels, uint32_t step_level, const double bbox[6]);
+/* testTriBox (src/symvox/test_triangle_box.cpp:105-184), as buildSVO calls
+ * it for the 8 children of a visited node (geom_octree.cpp:222-262), for n
+ * arbitrary (triangle, node) pairs: triangle i = tris[9i..9i+8], node centre
+ * centers[3i..3i+2], child half side half_sides[i] (children centred at
+ * centre +- half side per axis, child index 4x+2y+z).  Bit ci of masks[i] is
+ * set when child ci overlaps the triangle.  The decisions come from the same
+ * device code and the same decision sequence as the voxelizer's (certified
+ * fp32 filter, fp64 fallback); fallbacks (may be NULL) receives the number of
+ * predicates decided in fp64.  Host buffers; synchronous. */
+int svdag_tri_box_children(svdag_ctx* ctx, const float* tris, const double* centers, const double* half_sides,
+                           uint64_t n, uint8_t* masks, uint64_t* fallbacks);
 /* GeomOctree::toDAG (src/symvox/geom_octree.cpp:462-548) */
 int svdag_reduce_dag(svdag_ctx* ctx);
 /* GeomOctree::initChildLevels (src/symvox/geom_octree_extension.cpp:21-30) */

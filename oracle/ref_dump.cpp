@@ -3,7 +3,24 @@
 // dumps every intermediate node pool.  Test infrastructure: it produces the
 // golden vectors the restated oracle and the CUDA path are checked against.
 //
-//   ref_dump <scene.obj> <levels> <out_prefix> [step_levels]
+//   ref_dump <scene.obj> <levels> <out_prefix> [step_levels] [options]
+//
+// Options (each adds an output; the reference code they run is named):
+//   --soup            <out_prefix>.soup: the triangle soup Scene::loadObj
+//                     built (scene.cpp:51-250, buildTriVector :394-416),
+//                     u64 n, float bbox[6], then n float[9] triangles; with
+//                     --soup-only nothing else is run
+//   --flood           <out_prefix>.outside: GeomOctree::hiddenGeometryFloodfill
+//                     (geom_octree_extension.cpp:1651-1891) on a copy of the
+//                     SVO whose outside masks are zeroed first (the
+//                     reference never initialises them), per level u64 count
+//                     + one outsideMask byte per node.  Runs last: the
+//                     reference exits when the start corner cell is set,
+//                     after every other output is written
+//   --traverse <pts>  <out_prefix>.trav: EncodedSSVDAG::traverse
+//                     (encoded_ssvdag.cpp:527-574) of the .ssvdag encoding
+//                     for every point of <pts> (u64 n, then n float[3]); one
+//                     int32 per point
 //
 // Writes <out_prefix>.{svo,dag,sdag,csv}.pool, the four encoded files
 // <out_prefix>.{svdag,esvdag,ussvdag,ssvdag,csv.svdag} and a one-line JSON
@@ -63,27 +80,90 @@ static void dump_pool(const GeomOctree& oct, const std::string& path) {
   std::fclose(fp);
 }
 
+static void dump_soup(Scene& scene, const std::string& path) {
+  FILE* fp = std::fopen(path.c_str(), "wb");
+  if (!fp) { std::perror(path.c_str()); std::exit(2); }
+  const uint64_t n = scene.getNRawTriangles();
+  auto lo = scene.getAABB()[0], hi = scene.getAABB()[1];
+  const float bb[6] = {lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
+  std::fwrite(&n, 8, 1, fp);
+  std::fwrite(bb, 4, 6, fp);
+  for (uint64_t t = 0; t < n; ++t) {
+    const sl::point3f* v = scene.getTrianglePtr(t);
+    for (int i = 0; i < 3; ++i) {
+      const float xyz[3] = {v[i][0], v[i][1], v[i][2]};
+      std::fwrite(xyz, 4, 3, fp);
+    }
+  }
+  std::fclose(fp);
+}
+
+static void dump_outside(const GeomOctree& oct, const std::string& path) {
+  FILE* fp = std::fopen(path.c_str(), "wb");
+  if (!fp) { std::perror(path.c_str()); std::exit(2); }
+  const GeomOctree::NodeData& d = oct.getNodeData();
+  for (size_t l = 0; l < d.size(); ++l) {
+    const uint64_t n = d[l].size();
+    std::fwrite(&n, 8, 1, fp);
+    std::vector<unsigned char> m(n);
+    for (uint64_t i = 0; i < n; ++i) m[i] = d[l][i].getOutsideMask();
+    if (n) std::fwrite(m.data(), 1, n, fp);
+  }
+  std::fclose(fp);
+}
+
+static void dump_traverse(const EncodedSSVDAG& enc, const std::string& pts_path, const std::string& path) {
+  FILE* fi = std::fopen(pts_path.c_str(), "rb");
+  if (!fi) { std::perror(pts_path.c_str()); std::exit(2); }
+  uint64_t n = 0;
+  if (std::fread(&n, 8, 1, fi) != 1) std::exit(2);
+  std::vector<float> p(3 * n);
+  if (n && std::fread(p.data(), 4, 3 * n, fi) != 3 * n) std::exit(2);
+  std::fclose(fi);
+  std::vector<int32_t> out(n);
+  for (uint64_t i = 0; i < n; ++i) out[i] = enc.traverse(sl::point3f(p[3 * i], p[3 * i + 1], p[3 * i + 2]));
+  FILE* fp = std::fopen(path.c_str(), "wb");
+  if (!fp) { std::perror(path.c_str()); std::exit(2); }
+  if (n) std::fwrite(out.data(), 4, n, fp);
+  std::fclose(fp);
+}
+
 int main(int argc, char** argv) {
   if (argc < 4) {
-    std::fprintf(stderr, "usage: ref_dump scene.obj levels out_prefix [step_levels]\n");
+    std::fprintf(stderr, "usage: ref_dump scene.obj levels out_prefix [step_levels] [--soup|--soup-only] [--flood] "
+                         "[--traverse points]\n");
     return 1;
   }
   std::string obj = argv[1];
   unsigned levels = (unsigned)std::atoi(argv[2]);
   std::string pre = argv[3];
-  int step = argc > 4 ? std::atoi(argv[4]) : 0;
+  int step = 0;
+  bool soup = false, soup_only = false, flood = false;
+  std::string trav_pts;
+  for (int a = 4; a < argc; ++a) {
+    const std::string o = argv[a];
+    if (o == "--soup") soup = true;
+    else if (o == "--soup-only") soup = soup_only = true;
+    else if (o == "--flood") flood = true;
+    else if (o == "--traverse" && a + 1 < argc) trav_pts = argv[++a];
+    else step = std::atoi(argv[a]);
+  }
 
   Scene scene;
   scene.loadObj(obj, false, false, false, false, true);
+  if (soup) dump_soup(scene, pre + ".soup");
+  if (soup_only) return 0;
   auto minF = scene.getAABB()[0], maxF = scene.getAABB()[1];
   sl::aabox3d bb(sl::point3d(minF[0], minF[1], minF[2]), sl::point3d(maxF[0], maxF[1], maxF[2]));
 
   GeomOctree oct(&scene);
   sl::real_time_clock ck;
   ck.restart();
+  GeomOctree* svo_copy = nullptr;
   if (step == 0) {
     oct.buildSVO(levels, bb, false, NULL, false);
     dump_pool(oct, pre + ".svo.pool");
+    if (flood) svo_copy = new GeomOctree(oct);
     oct.toDAG();
   } else {
     oct.buildDAG(levels, (unsigned)step, bb, false);
@@ -111,6 +191,7 @@ int main(int argc, char** argv) {
   EncodedSSVDAG ssvdag;
   ssvdag.encode(sd);
   ssvdag.save(pre + ".ssvdag");
+  if (!trav_pts.empty()) dump_traverse(ssvdag, trav_pts, pre + ".trav");
 
   GeomOctree cs(oct);
   ck.restart();
@@ -127,5 +208,18 @@ int main(int argc, char** argv) {
       "\"t_build_dag_s\": %.6f, \"t_sdag_s\": %.6f, \"t_csv_s\": %.6f}\n",
       levels, st_svo.nTotalVoxels, st_svo.nNodesSVO, st_svo.nNodesLastLevSVO, oct.getStats().nNodesDAG,
       sd.getStats().nNodesSDAG, cs.getNNodes(), merged, t_dag, t_sdag, t_csv);
+  std::fflush(stdout);
+  if (svo_copy) {
+    // GeomOctree::Node's constructor (octree_node.cpp:22-37) leaves
+    // outsideMask uninitialised (geom_octree.hpp:64) while the fill only ever
+    // sets bits, so the masks start from indeterminate values; zero them
+    // first, the state the fill assumes (it zeroes the root's itself, :1821)
+    GeomOctree::NodeData& nd = const_cast<GeomOctree::NodeData&>(svo_copy->getNodeData());
+    for (auto& lev : nd)
+      for (auto& n : lev) n.outsideMask = 0;
+    svo_copy->hiddenGeometryFloodfill();
+    dump_outside(*svo_copy, pre + ".outside");
+    delete svo_copy;
+  }
   return 0;
 }

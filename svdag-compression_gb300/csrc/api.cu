@@ -246,6 +246,13 @@ int svdag_reduce_dag(svdag_ctx* h) {
   });
 }
 
+int svdag_tri_box_children(svdag_ctx* h, const float* tris, const double* centers, const double* half_sides,
+                           uint64_t n, uint8_t* masks, uint64_t* fallbacks) {
+  if (n && (!tris || !centers || !half_sides || !masks))
+    return fail(h, SVDAG_ERR_INVALID_ARG, "tri_box_children: null buffer");
+  return guarded(h, [&](Ctx& c) { svdag::tri_box_children(c, tris, centers, half_sides, n, masks, fallbacks); });
+}
+
 int svdag_init_child_levels(svdag_ctx* h) {
   return guarded(h, [&](Ctx& c) {
     if (c.state == SVDAG_S_EMPTY) throw Error(SVDAG_ERR_INVALID_STATE, "initChildLevels: empty octree");

@@ -80,6 +80,10 @@ void phase_flood_fill(Ctx& c, uint64_t* n_empty, uint64_t* n_surface);
 // Reference-count order of a level, exactly as the reference's std::sort of
 // (index, count) pairs leaves it (refsort.cu): order[k] = k-th node.
 void refcount_order(const Exec& ex, const uint32_t* counts, uint64_t n, uint32_t* order);
+// testTriBox of the 8 children of n (triangle, node) pairs, host buffers in
+// and out (voxelize.cu).
+void tri_box_children(Ctx& c, const float* tris, const double* centers, const double* half_sides, uint64_t n,
+                      uint8_t* masks, uint64_t* fallbacks);
 // toDAG with every temporary in caller-provided device scratch (no allocation).
 void phase_reduce_dag_scratch(Ctx& c, uint8_t* scratch, uint64_t capacity);
 

@@ -391,7 +391,71 @@ __global__ void k_count_voxels(const uint32_t* __restrict__ hdr, uint64_t n, uns
   if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, (unsigned long long)s);
 }
 
+// testTriBox for the 8 children of arbitrary (triangle, node) pairs, with the
+// decision sequence k_expand applies to a frontier pair: the slab
+// classification first, the certified full test for the children it leaves
+// open.  One pair per thread; bit ci of masks[i] = child ci overlaps.
+__global__ void k_tri_box_children(const float* __restrict__ tris, const double* __restrict__ centers,
+                                   const double* __restrict__ half_sides, uint64_t n, uint8_t* __restrict__ masks,
+                                   unsigned long long* __restrict__ n_fallback) {
+  unsigned fb = 0;
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const float* tp = tris + 9 * i;
+    float t[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) t[j] = tp[j];
+    const double* c = centers + 3 * i;
+    const double k = half_sides[i];
+    const double cc[3] = {c[0], c[1], c[2]};
+    sat::NodeBoxes nb;
+    sat::node_boxes(cc, k, nb);
+    sat::Pair32 P;
+    sat::pair_core(t, tp, c, nb, k, P);
+    sat::pair_slabs(P);
+    uint32_t m = 0, full = 0;
+    for (int ci = 7; ci >= 0; --ci) {
+      const int f = sat::child_fast(P, ci);
+      if (f == 1) m |= 1u << ci;
+      else if (f == 2) full |= 1u << ci;
+    }
+    if (full) {
+      sat::pair_edges(P);
+      for (uint32_t r = full; r; r &= r - 1) {
+        const int ci = __ffs(int(r)) - 1;
+        if (sat::child_full(P, ci, &fb)) m |= 1u << ci;
+      }
+    }
+    masks[i] = uint8_t(m);
+  }
+  unsigned long long sum = fb;
+  for (int o = 16; o; o >>= 1) sum += __shfl_down_sync(0xFFFFFFFFu, sum, o);
+  if ((threadIdx.x & 31) == 0 && sum) atomicAdd(n_fallback, sum);
+}
+
 }  // namespace
+
+void tri_box_children(Ctx& c, const float* h_tris, const double* h_centers, const double* h_half, uint64_t n,
+                      uint8_t* h_masks, uint64_t* fallbacks) {
+  const cudaStream_t st = c.stream;
+  const uint64_t m = n ? n : 1;
+  DBuf<float> d_t(9 * m, st);
+  DBuf<double> d_c(3 * m, st), d_k(m, st);
+  DBuf<uint8_t> d_m(m, st);
+  DBuf<unsigned long long> d_fb(1, st);
+  SVDAG_CUDA(cudaMemsetAsync(d_fb.get(), 0, 8, st));
+  if (n) {
+    SVDAG_CUDA(cudaMemcpyAsync(d_t.get(), h_tris, 36 * n, cudaMemcpyHostToDevice, st));
+    SVDAG_CUDA(cudaMemcpyAsync(d_c.get(), h_centers, 24 * n, cudaMemcpyHostToDevice, st));
+    SVDAG_CUDA(cudaMemcpyAsync(d_k.get(), h_half, 8 * n, cudaMemcpyHostToDevice, st));
+    SVDAG_LAUNCH(c.ex, k_tri_box_children, grid_for(c.ex, n, 256), 256, 0, d_t.get(), d_c.get(), d_k.get(), n,
+                 d_m.get(), d_fb.get());
+    SVDAG_CUDA(cudaMemcpyAsync(h_masks, d_m.get(), n, cudaMemcpyDeviceToHost, st));
+  }
+  unsigned long long fbh = 0;
+  SVDAG_CUDA(cudaMemcpyAsync(&fbh, d_fb.get(), 8, cudaMemcpyDeviceToHost, st));
+  SVDAG_CUDA(cudaStreamSynchronize(st));
+  if (fallbacks) *fallbacks = fbh;
+}
 
 void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6], const uint32_t* tri_list, uint64_t n_list) {
   const Exec& ex = c.ex;

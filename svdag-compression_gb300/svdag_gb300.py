@@ -66,6 +66,7 @@ GPU_SYMBOLS = {
     "svdag_voxelize": (_I, [_VP, _U32, _VP]),
     "svdag_build_dag": (_I, [_VP, _U32, _U32, _VP]),
     "svdag_reduce_dag": (_I, [_VP]),
+    "svdag_tri_box_children": (_I, [_VP, _VP, _VP, _VP, _U64, _VP, ctypes.POINTER(_U64)]),
     "svdag_init_child_levels": (_I, [_VP]),
     "svdag_reduce_sdag": (_I, [_VP]),
     "svdag_cross_level_merge": (_I, [_VP]),
@@ -361,6 +362,20 @@ class Octree:
 
     def toDAG(self):
         self._check(self._lib.svdag_reduce_dag(self._h))
+
+    def triBoxChildren(self, tris, centers, half_sides):
+        """testTriBox of the 8 children of each (triangle, node) pair on the
+        GPU (svdag_tri_box_children): (u8 masks, fp64 fallback count)."""
+        tris = np.ascontiguousarray(tris, np.float32)
+        centers = np.ascontiguousarray(centers, np.float64)
+        half_sides = np.ascontiguousarray(half_sides, np.float64)
+        n = tris.shape[0]
+        assert centers.shape == (n, 3) and half_sides.shape == (n,)
+        out = np.zeros(n, np.uint8)
+        fb = _U64()
+        self._check(self._lib.svdag_tri_box_children(self._h, tris.ctypes.data, centers.ctypes.data,
+                                                     half_sides.ctypes.data, n, out.ctypes.data, ctypes.byref(fb)))
+        return out, fb.value
 
     def encode(self, fmt="svdag"):
         """The EncodedSVDAG ("svdag") or EncodedUSSVDAG ("ussvdag") word

@@ -19,6 +19,25 @@ def box_scene(n, levels, seed):
     return sv.boxes((lo + 0.25) / res, (hi - 0.25) / res)
 
 
+def cavity_scene():
+    """A closed box shell with a sealed box cavity inside it."""
+    outer = sv.boxes(np.array([[0.2, 0.2, 0.2]]), np.array([[0.8, 0.8, 0.8]]))
+    inner = sv.boxes(np.array([[0.4, 0.4, 0.4]]), np.array([[0.6, 0.6, 0.6]]))
+    return np.concatenate([outer, inner])
+
+
+def levels_digest(levels):
+    """SHA-256 over per-level byte arrays (u64 count, then the bytes), the
+    form of the golden outside-mask digests."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for lev in levels:
+        h.update(np.uint64(len(lev)).tobytes())
+        h.update(np.ascontiguousarray(lev).tobytes())
+    return h.hexdigest()
+
+
 SCENES = {
     "ico5_L9": lambda: sv.icosphere(5, 0.4, 0.08, 1234),
     "ico5_L7": lambda: sv.icosphere(5, 0.4, 0.08, 1234),
@@ -29,6 +48,7 @@ SCENES = {
     "terrain129_L9_step1": lambda: sv.terrain(129, 8, 0.3, 11),
     "terrain257_L10": lambda: sv.terrain(257, 8, 0.3, 3),
     "boxes_L8": lambda: box_scene(300, 8, 21),
+    "cavity_L7": lambda: cavity_scene(),
     # the benchmark's headline workload (8,396,796 triangles, depth 12)
     "terrain2048_L12": lambda: sv.terrain(2048, 8, 0.3, 7),
 }

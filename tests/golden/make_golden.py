@@ -6,8 +6,11 @@ by oracle/Makefile) on seeded synthetic scenes.
 
 Each case records the reference's counts and SHA-256 digests of its SVO,
 DAG, SDAG and CSVDAG node pools (48-byte records, oracle/ref_dump.cpp) and of
-the encoded .svdag/.esvdag/.ussvdag/.ssvdag/.csv.svdag files.  Small cases
-also keep their full DAG/SDAG/CSVDAG pools as .npz.
+the encoded .svdag/.esvdag/.ussvdag/.ssvdag/.csv.svdag files; the FLOOD cases
+also the outside masks of the reference's hiddenGeometryFloodfill.  Small
+cases also keep their full DAG/SDAG/CSVDAG pools as .npz.  `--obj` writes
+obj_ingest.json: the triangle soups the reference's Scene::loadObj builds
+from seeded OBJ files full of parsing edge cases.
 """
 import hashlib
 import json
@@ -42,7 +45,16 @@ CASES = {
     # triangles), depth 12, seed 7; the reference's single-threaded build
     # takes minutes here, so it is generated on request (--only)
     "terrain2048_L12": (lambda: sv.terrain(2048, 8, 0.3, 7), 12, 0, False),
+    "cavity_L7": (lambda: cavity_scene(), 7, 0, False),
 }
+# cases whose SVO also goes through the reference's hiddenGeometryFloodfill
+# (their start corner cell is empty)
+FLOOD = {"ico3_L6", "ico5_L7", "terrain65_L8", "terrain129_L9", "cavity_L7", "ico4_L8_seed5"}
+# seeded OBJ files of tests/_objgen.py (without the face records the
+# reference's loader crashes on) run through the reference's Scene::loadObj:
+# name -> (seed, lines, final newline)
+OBJ_CASES = {"obj_s1": (1, 3000, True), "obj_s2": (2, 60000, True), "obj_s3": (3, 60000, False),
+             "obj_s5_short": (5, 20000, True)}
 # cases a plain run skips (regenerate with --only NAME)
 ON_REQUEST = {"terrain2048_L12"}
 
@@ -57,6 +69,33 @@ def box_scene(n, levels, seed):
     return sv.boxes((lo + 0.25) / res, (hi - 0.25) / res)
 
 
+def cavity_scene():
+    """A closed box shell with a sealed box cavity inside it."""
+    outer = sv.boxes(np.array([[0.2, 0.2, 0.2]]), np.array([[0.8, 0.8, 0.8]]))
+    inner = sv.boxes(np.array([[0.4, 0.4, 0.4]]), np.array([[0.6, 0.6, 0.6]]))
+    return np.concatenate([outer, inner])
+
+
+def read_levels_u8(path):
+    """Per-level byte arrays (u64 count, then count bytes, per level)."""
+    raw = open(path, "rb").read()
+    out, o = [], 0
+    while o < len(raw):
+        n = int(np.frombuffer(raw[o:o + 8], np.uint64)[0])
+        o += 8
+        out.append(np.frombuffer(raw[o:o + n], np.uint8))
+        o += n
+    return out
+
+
+def levels_digest(levels):
+    h = hashlib.sha256()
+    for lev in levels:
+        h.update(np.uint64(len(lev)).tobytes())
+        h.update(np.ascontiguousarray(lev).tobytes())
+    return h.hexdigest()
+
+
 def sha(path):
     with open(path, "rb") as f:
         return hashlib.sha256(f.read()).hexdigest()
@@ -68,7 +107,8 @@ def run_case(name, make, levels, step, keep):
         obj = os.path.join(td, "scene.obj")
         sv.write_obj(obj, tris, True)
         pre = os.path.join(td, "out")
-        r = subprocess.run([REF_DUMP, obj, str(levels), pre] + ([str(step)] if step else []),
+        r = subprocess.run([REF_DUMP, obj, str(levels), pre] + ([str(step)] if step else []) +
+                           (["--flood"] if name in FLOOD else []),
                            stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, check=True)
         line = [l for l in r.stdout.splitlines() if l.startswith("REFJSON ")][-1]
         info = json.loads(line[len("REFJSON "):])
@@ -86,6 +126,10 @@ def run_case(name, make, levels, step, keep):
                           "nnodes": int(pool["nnodes"]), "nvoxels": int(pool["nvoxels"])}
             pools[kind] = pool["pool"]
         info["files"] = {ext: sha(pre + "." + ext) for ext in ("svdag", "esvdag", "ussvdag", "ssvdag", "csv.svdag")}
+        if name in FLOOD:
+            masks = read_levels_u8(pre + ".outside")
+            info["outside"] = {"counts": [int(len(m)) for m in masks], "digest": levels_digest(masks),
+                               "marked": [int(np.count_nonzero(m)) for m in masks]}
         if keep:
             arrs = {}
             for kind in ("dag", "sdag", "csv"):
@@ -95,10 +139,43 @@ def run_case(name, make, levels, step, keep):
     return info
 
 
+def run_obj_cases():
+    """The reference loader's triangle soup and bounding box for each seeded
+    OBJ file (obj_ingest.json): SHA-256 of the float[9] triangles and the
+    bbox as float32 bit patterns."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    from _objgen import make_obj
+
+    out = {}
+    for name, (seed, lines, final_nl) in OBJ_CASES.items():
+        with tempfile.TemporaryDirectory() as td:
+            obj = os.path.join(td, "s.obj")
+            with open(obj, "wb") as f:
+                f.write(make_obj(seed, lines, final_newline=final_nl, reference_safe=True))
+            pre = os.path.join(td, "out")
+            subprocess.run([REF_DUMP, obj, "1", pre, "--soup-only"], stdout=subprocess.DEVNULL,
+                           stderr=subprocess.DEVNULL, check=True)
+            raw = open(pre + ".soup", "rb").read()
+            n = int(np.frombuffer(raw[:8], np.uint64)[0])
+            bb = np.frombuffer(raw[8:32], np.float32)
+            tris = raw[32:]
+            assert len(tris) == 36 * n
+            out[name] = {"seed": seed, "lines": lines, "final_newline": final_nl, "n_tris": n,
+                         "tris_sha256": hashlib.sha256(tris).hexdigest(),
+                         "bbox_bits": [int(x) for x in bb.view(np.uint32)]}
+        print(name, n, flush=True)
+    with open(os.path.join(HERE, "obj_ingest.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+
+
 def main(argv):
     """`make_golden.py` regenerates every default case; `make_golden.py
     --only NAME [NAME ...]` regenerates the named cases and keeps the others
-    already in golden.json."""
+    already in golden.json; `make_golden.py --obj` regenerates the OBJ
+    loader fixtures."""
+    if argv[:1] == ["--obj"]:
+        run_obj_cases()
+        return
     path = os.path.join(HERE, "golden.json")
     if argv[:1] == ["--only"]:
         names = argv[1:]

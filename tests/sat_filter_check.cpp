@@ -3,6 +3,12 @@
 // (oracle/svdag_oracle.cpp, ora_tri_box).  Prints one summary line:
 //   cases=<n> mismatches=<m> fallbacks=<f> hits=<h>
 // Built and run by tests/test_sat_filter.py with -ffp-contract=off.
+//
+//   satcheck <n> [dump_path]
+// With dump_path, every (triangle, node) case is also written there as a
+// 69-byte record -- triangle float[9], node centre double[3], child half
+// side double, the oracle's 8-child overlap mask u8 -- for the device-side
+// check of the same filter (tests/test_sat_device.py).
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -16,15 +22,18 @@ using namespace svdag::sat;
 
 static uint64_t g_cases = 0, g_mis = 0, g_hits = 0;
 static unsigned g_fb = 0;
+static FILE* g_dump = nullptr;
 
 static void check(const float t[9], const double pc[3], double k) {
   NodeBoxes nb;
   node_boxes(pc, k, nb);
   Pair32 P;
   pair_setup(t, t, pc, nb, k, P);
+  uint8_t mask = 0;
   for (int ci = 0; ci < 8; ++ci) {
     const double c[3] = {pc[0] + ((ci & 4) ? k : -k), pc[1] + ((ci & 2) ? k : -k), pc[2] + ((ci & 1) ? k : -k)};
     const bool want = ora_tri_box(c, k, t) != 0;
+    mask |= uint8_t(want) << ci;
     const bool got = child_overlap(P, ci, &g_fb);
     ++g_cases;
     g_hits += want;
@@ -35,10 +44,20 @@ static void check(const float t[9], const double pc[3], double k) {
       ++g_mis;
     }
   }
+  if (g_dump) {
+    std::fwrite(t, 4, 9, g_dump);
+    std::fwrite(pc, 8, 3, g_dump);
+    std::fwrite(&k, 8, 1, g_dump);
+    std::fwrite(&mask, 1, 1, g_dump);
+  }
 }
 
 int main(int argc, char** argv) {
   const long n = argc > 1 ? std::atol(argv[1]) : 200000;
+  if (argc > 2) {
+    g_dump = std::fopen(argv[2], "wb");
+    if (!g_dump) { std::perror(argv[2]); return 2; }
+  }
   std::mt19937_64 rng(12345);
   std::uniform_real_distribution<double> U(0.0, 1.0);
   for (long it = 0; it < n; ++it) {
@@ -113,6 +132,7 @@ int main(int argc, char** argv) {
     float u[9] = {0.4f, 0.4f, 0.4f, 0.6f, 0.5f, 0.5f, 3e30f, 0.5f, 0.6f};
     check(u, pc, 0.25);
   }
+  if (g_dump) std::fclose(g_dump);
   std::printf("cases=%llu mismatches=%llu fallbacks=%u hits=%llu\n", (unsigned long long)g_cases,
               (unsigned long long)g_mis, g_fb, (unsigned long long)g_hits);
   return g_mis ? 1 : 0;

@@ -10,7 +10,7 @@ import oracle_py
 import svdag_gb300 as sv
 from _floodcheck import dense_outside, marked_voxels
 from _occupancy import occupancy
-from _scenes import SCENES
+from _scenes import SCENES, golden, levels_digest
 
 pytestmark = pytest.mark.gpu
 
@@ -50,6 +50,24 @@ def test_flood_fill_matches_oracle(name, L):
     g.toDAG()
     with pytest.raises(sv.SvdagError):
         g.hiddenGeometryFloodfill()
+
+
+G = golden()
+
+
+@pytest.mark.parametrize("name", sorted(k for k in G if "outside" in G[k]))
+def test_flood_fill_matches_reference_masks(name):
+    """The outside masks of every level equal those of the reference's own
+    hiddenGeometryFloodfill (compiled from its sources, masks zeroed first;
+    golden digests) on the reference's node numbering."""
+    g = G[name]
+    o = sv.Octree()
+    o.upload_triangles(SCENES[name]())
+    o.buildSVO(g["levels"])
+    assert oracle_py.pool_digest(o.pool()) == g["svo"]["digest"]
+    masks, _, _ = o.hiddenGeometryFloodfill()
+    assert [len(m) for m in masks] == g["outside"]["counts"]
+    assert levels_digest(masks) == g["outside"]["digest"]
 
 
 def test_flood_fill_start_cell_set():

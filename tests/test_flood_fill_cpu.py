@@ -1,7 +1,10 @@
 """The restated hidden-geometry flood fill (oracle, geom_octree_extension.cpp:
-1651-1891) against a dense 6-connected labelling of the voxel grid: the empty
-cells it marks cover exactly the empty voxels connected to the corner, and
-the set voxels it marks are exactly those touching them.  No GPU."""
+1651-1891) against the reference's own hiddenGeometryFloodfill (golden
+outside masks, compiled reference, masks zeroed first because the reference
+never initialises them) and against a dense 6-connected labelling of the
+voxel grid: the empty cells it marks cover exactly the empty voxels
+connected to the corner, and the set voxels it marks are exactly those
+touching them.  No GPU."""
 import numpy as np
 import pytest
 
@@ -9,7 +12,20 @@ import oracle_py
 import svdag_gb300 as sv
 from _floodcheck import dense_outside, marked_voxels
 from _occupancy import occupancy
-from _scenes import SCENES
+from _scenes import SCENES, golden, levels_digest
+
+G = golden()
+FLOOD = sorted(k for k in G if "outside" in G[k])
+
+
+@pytest.mark.parametrize("name", FLOOD)
+def test_oracle_flood_fill_matches_reference_masks(name):
+    g = G[name]
+    o = oracle_py.OracleOctree()
+    o.buildSVO(SCENES[name](), g["levels"])
+    masks, n_empty, n_surface = o.hiddenGeometryFloodfill()
+    assert [len(m) for m in masks] == g["outside"]["counts"]
+    assert levels_digest(masks) == g["outside"]["digest"]
 
 
 def _shell_with_cavity():
