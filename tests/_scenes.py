@@ -57,6 +57,18 @@ SCENES = {
 HEAVY = {"terrain2048_L12"}
 
 
+def traverse_points(levels, seed=2024, n_random=300000):
+    """Query points of the traversal fixtures: every voxel centre (levels
+    <= 7), then seeded uniform points in [-0.05, 1.05)^3 (some outside the
+    box)."""
+    pts = []
+    if levels <= 7:
+        r = 1 << levels
+        pts.append((np.indices((r, r, r)).reshape(3, -1).T.astype(np.float64) + 0.5) / r)
+    pts.append(np.random.default_rng(seed).uniform(-0.05, 1.05, (n_random, 3)))
+    return np.concatenate(pts).astype(np.float32)
+
+
 def golden():
     with open(os.path.join(GOLDEN, "golden.json")) as f:
         return json.load(f)

@@ -28,6 +28,9 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import svdag_gb300 as sv  # noqa: E402
 import oracle_py  # noqa: E402
 
+sys.path.insert(0, os.path.dirname(HERE))
+from _scenes import traverse_points  # noqa: E402
+
 REF_DUMP = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
 
 # name -> (scene builder, levels, step_levels, keep_full_pools)
@@ -50,6 +53,13 @@ CASES = {
 # cases whose SVO also goes through the reference's hiddenGeometryFloodfill
 # (their start corner cell is empty)
 FLOOD = {"ico3_L6", "ico5_L7", "terrain65_L8", "terrain129_L9", "cavity_L7", "ico4_L8_seed5"}
+# cases whose .ssvdag encoding goes through the reference's
+# EncodedSSVDAG::traverse on traverse_points(levels) (all their child
+# pointers are one word, where the reference's decoder reads its own
+# encoding; tests/test_traverse.py says what the comparison covers)
+TRAVERSE = {"ico3_L6", "ico5_L7"}
+
+
 # seeded OBJ files of tests/_objgen.py (without the face records the
 # reference's loader crashes on) run through the reference's Scene::loadObj:
 # name -> (seed, lines, final newline)
@@ -107,8 +117,14 @@ def run_case(name, make, levels, step, keep):
         obj = os.path.join(td, "scene.obj")
         sv.write_obj(obj, tris, True)
         pre = os.path.join(td, "out")
-        r = subprocess.run([REF_DUMP, obj, str(levels), pre] + ([str(step)] if step else []) +
-                           (["--flood"] if name in FLOOD else []),
+        extra = ["--flood"] if name in FLOOD else []
+        if name in TRAVERSE:
+            pts = traverse_points(levels)
+            with open(os.path.join(td, "pts.bin"), "wb") as f:
+                f.write(np.uint64(pts.shape[0]).tobytes())
+                f.write(pts.tobytes())
+            extra += ["--traverse", os.path.join(td, "pts.bin")]
+        r = subprocess.run([REF_DUMP, obj, str(levels), pre] + ([str(step)] if step else []) + extra,
                            stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, check=True)
         line = [l for l in r.stdout.splitlines() if l.startswith("REFJSON ")][-1]
         info = json.loads(line[len("REFJSON "):])
@@ -126,6 +142,10 @@ def run_case(name, make, levels, step, keep):
                           "nnodes": int(pool["nnodes"]), "nvoxels": int(pool["nvoxels"])}
             pools[kind] = pool["pool"]
         info["files"] = {ext: sha(pre + "." + ext) for ext in ("svdag", "esvdag", "ussvdag", "ssvdag", "csv.svdag")}
+        if name in TRAVERSE:
+            res = np.fromfile(pre + ".trav", np.int32)
+            np.savez_compressed(os.path.join(HERE, name + "_traverse.npz"), depth=res.astype(np.int8))
+            info["traverse"] = {"points": int(res.size), "file": name + "_traverse.npz"}
         if name in FLOOD:
             masks = read_levels_u8(pre + ".outside")
             info["outside"] = {"counts": [int(len(m)) for m in masks], "digest": levels_digest(masks),
