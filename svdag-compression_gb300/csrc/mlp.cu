@@ -13,15 +13,19 @@
 // each proposal with the exact distance, so the network only decides which
 // pairs get checked, never which merges are accepted.
 //
-// Kernels: a tiled fp32 GEMM (128x128 block tile, 8x8 per thread, optional
-// transposes, fused bias + ReLU, split-K for the weight gradients), the
-// siamese loss and its gradient, bias gradients, Adam, and a banded top-k
-// selection.  The layers are small (512x256 at most); they run on the FP32
-// pipes.
+// Kernels: a tensor-core GEMM (mma.sync m16n8k16 on fp16 operands, fp32
+// accumulation, tiles moved by cp.async in a 3-stage pipeline) with fused
+// row gather, bias, ReLU, ReLU mask and column sums (bias gradients), split-K
+// for the weight gradients; the siamese loss and its gradient, Adam, the
+// training-pair sampler, and a banded top-k selection.  One training step is
+// captured as a CUDA graph and replayed for every batch.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <random>
+#include <type_traits>
+
+#include <cuda_fp16.h>
 
 #include "ctx.cuh"
 #include "lossy.cuh"
@@ -30,99 +34,297 @@ namespace svdag {
 namespace {
 
 constexpr int kIn = 512, kH = 256, kOut = 64;
-constexpr int kBM = 128, kBN = 128, kBK = 8;
+// training: pairs per batch (rows = 2x), Adam learning rate
+#ifndef SVDAG_MLP_BATCH
+#define SVDAG_MLP_BATCH 4096
+#endif
+#ifndef SVDAG_MLP_LR
+#define SVDAG_MLP_LR 1e-3f
+#endif
+constexpr int kTrainBatch = SVDAG_MLP_BATCH;
+constexpr float kTrainLr = SVDAG_MLP_LR;
 
-// C[M x N] = op(A)[M x K] * op(B)[K x N] (+ bias[N]) (ReLU); row-major.
-// TA: A is stored K x M; TB: B is stored N x K.  128x128 block tile, 8x8
-// outputs per thread (rows ty*4+{0..3} and 64+ty*4+{0..3}, columns likewise),
-// operands staged k-major in shared memory and read as float4.  With
-// gridDim.z > 1 the K range is split and partial sums are added into C
-// (zeroed by the caller; no bias or ReLU then).
-template <bool TA, bool TB>
-__global__ void __launch_bounds__(256) k_gemm(const float* __restrict__ A, const float* __restrict__ B,
-                                              float* __restrict__ C, int M, int N, int K, int k_per,
-                                              const float* __restrict__ bias, int relu, int accumulate) {
-  __shared__ __align__(16) float sA[kBK][kBM];
-  __shared__ __align__(16) float sB[kBK][kBN];
-  const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
-  const int row0 = blockIdx.y * kBM, col0 = blockIdx.x * kBN;
+// ---------------------------------------------------------------------------
+// Tensor-core GEMM on fp16 operands.  C[M x N] = op(A)[M x K] * op(B)[K x N]
+// with fp32 accumulation (mma.sync m16n8k16).  A is stored M x K (K
+// contiguous) or, with A_KM, K x M; B is stored K x N or, with B_NK, N x K;
+// both are fp16 in global memory.  A's stored rows may be gathered through
+// `rowmap` (stored row r is row rowmap[r] of the array).  C is fp32 or fp16,
+// row-major.  Epilogue, in order: x alpha, + bias[n] (fp32), ReLU, a ReLU
+// mask (C[m][n] = 0 where mask[m][n] <= 0: the backward of a ReLU layer),
+// column sums x colsum_scale added into colsum[N] (bias gradients); with
+// gridDim.z > 1, atomic partial sums over a split K range (fp32 C zeroed by
+// the caller).
+//
+// Block tile BM x BN x 64, 8 warps of (BM/WGM) x (BN/WGN) warp tiles built
+// from m16n8 fragments loaded by ldmatrix (.trans for the K-major / K x N
+// layouts).  Tiles move global -> shared memory with 16-byte cp.async in a
+// 3-stage pipeline (two tiles in flight while one is multiplied); rows past
+// the matrix are zero-filled by the copy itself.  Dimensions along which a
+// tile is read in 8-element chunks (K for M x K / N x K storage, M and N
+// otherwise) must be whole tiles (multiples of 64 along K, of the tile width
+// along M and N) -- true of every layer width here.
+constexpr int kBK = 64, kPad = 8, kGemmThreads = 256, kStages = 3;
+
+__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], const uint32_t b[2]) {
+  asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+               "{%0,%1,%2,%3};\n"
+               : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <bool TRANS>
+__device__ __forceinline__ void ldsm_x4(uint32_t r[4], const void* smem) {
+  const uint32_t a = uint32_t(__cvta_generic_to_shared(smem));
+  if (TRANS)
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+  else
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+}
+
+// 16-byte global -> shared copy; src_bytes = 0 writes zeros.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, uint32_t src_bytes) {
+  const uint32_t a = uint32_t(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(a), "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// Copies a ROWS x COLS tile (COLS contiguous in global memory, 8-element
+// chunks) of a row-major fp16 matrix with leading dimension ld: global rows
+// [r0, r0 + ROWS) below rlim (through rowmap when given), columns
+// [c0, c0 + COLS); rows at or past rlim are zero.
+template <int ROWS, int COLS>
+__device__ __forceinline__ void tile_copy(__half* s, const __half* g, int ld, int r0, int rlim, int c0,
+                                          const uint32_t* rowmap) {
+  constexpr int kChunks = ROWS * COLS / 8;
+  static_assert(kChunks % kGemmThreads == 0, "tile shape");
+#pragma unroll
+  for (int i = 0; i < kChunks / kGemmThreads; ++i) {
+    const int ch = threadIdx.x + i * kGemmThreads;
+    const int r = ch / (COLS / 8), c = (ch % (COLS / 8)) * 8;
+    const int gr = r0 + r;
+    const bool ok = gr < rlim;
+    const __half* src = ok ? g + size_t(rowmap ? rowmap[gr] : uint32_t(gr)) * ld + c0 + c : g;
+    cp_async16(s + r * (COLS + kPad) + c, src, ok ? 16u : 0u);
+  }
+}
+
+template <class OutT>
+__device__ __forceinline__ void store2(OutT* o, float a, float b);
+template <>
+__device__ __forceinline__ void store2<float>(float* o, float a, float b) {
+  *reinterpret_cast<float2*>(o) = make_float2(a, b);
+}
+template <>
+__device__ __forceinline__ void store2<__half>(__half* o, float a, float b) {
+  *reinterpret_cast<__half2*>(o) = __floats2half2_rn(a, b);
+}
+
+template <bool A_KM, bool B_NK, int BM, int BN, int WGM>
+struct GemmShape {
+  static constexpr int WGN = 8 / WGM;
+  static constexpr int WM = BM / WGM, WN = BN / WGN;
+  static constexpr int MI = WM / 16, NI = WN / 8;
+  static constexpr int AR = A_KM ? kBK : BM, AC = A_KM ? BM : kBK;
+  static constexpr int BR = B_NK ? BN : kBK, BC = B_NK ? kBK : BN;
+  static constexpr int kA = AR * (AC + kPad), kB = BR * (BC + kPad);
+  static constexpr int kSmemBytes = kStages * (kA + kB) * 2;
+};
+
+template <bool A_KM, bool B_NK, int BM, int BN, int WGM, class OutT>
+__global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(const __half* __restrict__ A, const __half* __restrict__ B,
+                                                          OutT* __restrict__ C, int M, int N, int K, int k_per,
+                                                          const uint32_t* __restrict__ rowmap, float alpha,
+                                                          const float* __restrict__ bias, int relu,
+                                                          const __half* __restrict__ mask, float* __restrict__ colsum,
+                                                          float colsum_scale) {
+  using S = GemmShape<A_KM, B_NK, BM, BN, WGM>;
+  constexpr int WM = S::WM, WN = S::WN, MI = S::MI, NI = S::NI, AC = S::AC, BC = S::BC;
+  static_assert(MI >= 1 && NI >= 2 && NI % 2 == 0, "warp tile");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __half* sA = reinterpret_cast<__half*>(smem_raw);
+  __half* sB = sA + kStages * S::kA;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wm = warp % WGM, wn = warp / WGM;
+  const int row0 = blockIdx.y * BM, col0 = blockIdx.x * BN;
   const int kb = blockIdx.z * k_per, ke = min(K, kb + k_per);
-  float acc[8][8] = {};
-  for (int k0 = kb; k0 < ke; k0 += kBK) {
+  const int nk = ke > kb ? (ke - kb + kBK - 1) / kBK : 0;
+
+  auto load = [&](int t, int stage) {
+    const int k0 = kb + t * kBK;
+    __half* a = sA + stage * S::kA;
+    __half* b = sB + stage * S::kB;
+    if (A_KM) tile_copy<S::AR, AC>(a, A, M, k0, ke, row0, rowmap);
+    else tile_copy<S::AR, AC>(a, A, K, row0, M, k0, rowmap);
+    if (B_NK) tile_copy<S::BR, BC>(b, B, K, col0, N, k0, nullptr);
+    else tile_copy<S::BR, BC>(b, B, N, k0, ke, col0, nullptr);
+  };
+  float acc[MI][NI][4];
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const int idx = t * 4 + e;  // 0..1023 over the 128 x 8 tile
-      int r, k;
-      if (TA) { k = idx / kBM; r = idx % kBM; } else { r = idx / kBK; k = idx % kBK; }
-      const int gr = row0 + r, gk = k0 + k;
-      float a = 0.f;
-      if (gr < M && gk < ke) a = TA ? A[size_t(gk) * M + gr] : A[size_t(gr) * K + gk];
-      sA[k][r] = a;
-      int c, kk;
-      if (TB) { c = idx / kBK; kk = idx % kBK; } else { kk = idx / kBN; c = idx % kBN; }
-      const int gc = col0 + c, gk2 = k0 + kk;
-      float b = 0.f;
-      if (gc < N && gk2 < ke) b = TB ? B[size_t(gc) * K + gk2] : B[size_t(gk2) * N + gc];
-      sB[kk][c] = b;
-    }
-    __syncthreads();
+  for (int i = 0; i < MI; ++i)
 #pragma unroll
-    for (int k = 0; k < kBK; ++k) {
-      const float4 a0 = *reinterpret_cast<const float4*>(&sA[k][ty * 4]);
-      const float4 a1 = *reinterpret_cast<const float4*>(&sA[k][64 + ty * 4]);
-      const float4 b0 = *reinterpret_cast<const float4*>(&sB[k][tx * 4]);
-      const float4 b1 = *reinterpret_cast<const float4*>(&sB[k][64 + tx * 4]);
-      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+    for (int j = 0; j < NI; ++j)
 #pragma unroll
-      for (int i = 0; i < 8; ++i)
+      for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
+
 #pragma unroll
-        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-    }
-    __syncthreads();
+  for (int t = 0; t < kStages - 1; ++t) {
+    if (t < nk) load(t, t);
+    cp_async_commit();
   }
-  const bool split = gridDim.z > 1;
+  for (int it = 0; it < nk; ++it) {
+    cp_async_wait<kStages - 2>();
+    __syncthreads();  // tile `it` visible to all warps; stage (it - 1) % kStages free
+    if (it + kStages - 1 < nk) load(it + kStages - 1, (it + kStages - 1) % kStages);
+    cp_async_commit();
+    const __half* a_s = sA + (it % kStages) * S::kA;
+    const __half* b_s = sB + (it % kStages) * S::kB;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const int r = row0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + i - 4);
-    if (r >= M) continue;
+    for (int kk = 0; kk < kBK; kk += 16) {
+      uint32_t af[MI][4], bf[NI][2];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int cidx = col0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + j - 4);
-      if (cidx >= N) continue;
-      float* o = C + size_t(r) * N + cidx;
-      if (split) {
-        atomicAdd(o, acc[i][j]);
-        continue;
+      for (int mi = 0; mi < MI; ++mi) {
+        const int mb = wm * WM + mi * 16;
+        if (A_KM) {
+          const int j = lane >> 3, r = lane & 7;
+          ldsm_x4<true>(af[mi], a_s + (kk + r + (j >= 2 ? 8 : 0)) * (AC + kPad) + mb + ((j & 1) ? 8 : 0));
+        } else {
+          ldsm_x4<false>(af[mi], a_s + (mb + (lane & 15)) * (AC + kPad) + kk + (lane >> 4) * 8);
+        }
       }
-      float v = acc[i][j];
-      if (bias) v += bias[cidx];
-      if (relu) v = fmaxf(v, 0.f);
-      *o = accumulate ? *o + v : v;
+#pragma unroll
+      for (int ni = 0; ni < NI; ni += 2) {
+        const int nb = wn * WN + ni * 8;
+        const int j = lane >> 3, r = lane & 7;
+        uint32_t t[4];
+        if (B_NK) ldsm_x4<false>(t, b_s + (nb + r + (j >= 2 ? 8 : 0)) * (BC + kPad) + kk + ((j & 1) ? 8 : 0));
+        else ldsm_x4<true>(t, b_s + (kk + r + ((j & 1) ? 8 : 0)) * (BC + kPad) + nb + (j >= 2 ? 8 : 0));
+        bf[ni][0] = t[0];
+        bf[ni][1] = t[1];
+        bf[ni + 1][0] = t[2];
+        bf[ni + 1][1] = t[3];
+      }
+#pragma unroll
+      for (int mi = 0; mi < MI; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < NI; ++ni) mma16816(acc[mi][ni], af[mi], bf[ni]);
     }
   }
+  cp_async_wait<0>();
+
+  const bool split = gridDim.z > 1;
+  const int g = lane >> 2, t4 = lane & 3;
+  float cs[NI][2];
+#pragma unroll
+  for (int ni = 0; ni < NI; ++ni) cs[ni][0] = cs[ni][1] = 0.f;
+#pragma unroll
+  for (int mi = 0; mi < MI; ++mi)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int r = row0 + wm * WM + mi * 16 + g + h * 8;
+      if (r >= M) continue;
+#pragma unroll
+      for (int ni = 0; ni < NI; ++ni) {
+        const int c = col0 + wn * WN + ni * 8 + t4 * 2;  // N is a multiple of the tile width
+        float v0 = alpha * acc[mi][ni][2 * h], v1 = alpha * acc[mi][ni][2 * h + 1];
+        OutT* o = C + size_t(r) * N + c;
+        if (split) {
+          atomicAdd(reinterpret_cast<float*>(o), v0);
+          atomicAdd(reinterpret_cast<float*>(o) + 1, v1);
+          continue;
+        }
+        if (bias) { v0 += bias[c]; v1 += bias[c + 1]; }
+        if (relu) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+        if (mask) {
+          const __half2 mk = *reinterpret_cast<const __half2*>(mask + size_t(r) * N + c);
+          if (!(__low2float(mk) > 0.f)) v0 = 0.f;
+          if (!(__high2float(mk) > 0.f)) v1 = 0.f;
+        }
+        cs[ni][0] += v0;
+        cs[ni][1] += v1;
+        store2<OutT>(o, v0, v1);
+      }
+    }
+  if (colsum && !split) {
+    // lanes with the same t4 hold the same columns: reduce over g, then one
+    // atomic per column and warp row
+#pragma unroll
+    for (int ni = 0; ni < NI; ++ni)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        float v = cs[ni][e];
+        v += __shfl_xor_sync(0xFFFFFFFFu, v, 4);
+        v += __shfl_xor_sync(0xFFFFFFFFu, v, 8);
+        v += __shfl_xor_sync(0xFFFFFFFFu, v, 16);
+        if (g == 0) atomicAdd(&colsum[col0 + wn * WN + ni * 8 + t4 * 2 + e], v * colsum_scale);
+      }
+  }
+}
+
+struct GemmOpts {
+  const uint32_t* rowmap = nullptr;  // gather of A's stored rows
+  float alpha = 1.f;
+  const float* bias = nullptr;
+  bool relu = false;
+  const __half* mask = nullptr;      // ReLU backward mask (same shape as C)
+  float* colsum = nullptr;           // column sums of the result (x colsum_scale), zeroed by the caller
+  float colsum_scale = 1.f;
+  bool zeroed = false;               // fp32 C already zero (split-K accumulates into it)
+};
+
+template <bool A_KM, bool B_NK, int BM, int BN, int WGM, class OutT>
+void launch_gemm(const Exec& ex, dim3 grid, const __half* A, const __half* B, OutT* C, int M, int N, int K, int k_per,
+                 const GemmOpts& o) {
+  using S = GemmShape<A_KM, B_NK, BM, BN, WGM>;
+  auto* kern = k_gemm_tc<A_KM, B_NK, BM, BN, WGM, OutT>;
+  static bool attr = false;  // per instantiation; the attribute is a process-wide property of the function
+  if (!attr) {
+    SVDAG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kSmemBytes));
+    attr = true;
+  }
+  SVDAG_LAUNCH(ex, (k_gemm_tc<A_KM, B_NK, BM, BN, WGM, OutT>), grid, kGemmThreads, S::kSmemBytes, A, B, C, M, N, K,
+               k_per, o.rowmap, o.alpha, o.bias, o.relu ? 1 : 0, o.mask, o.colsum, o.colsum_scale);
 }
 
 // Splits K when the output has too few tiles to fill the GPU (the weight
-// gradients: 512x256 outputs over K = 2 x batch rows).
-template <bool TA, bool TB>
-void gemm(const Exec& ex, const float* A, const float* B, float* C, int M, int N, int K, const float* bias = nullptr,
-          bool relu = false, bool acc = false) {
-  const int tiles = ((N + kBN - 1) / kBN) * ((M + kBM - 1) / kBM);
+// gradients: at most 512 x 256 outputs over K = 2 x batch rows); split
+// results are atomic partial sums into C (fp32), which is zeroed here unless
+// the caller already did.
+template <bool A_KM, bool B_NK, class OutT>
+void gemm_tc(const Exec& ex, const __half* A, const __half* B, OutT* C, int M, int N, int K,
+             const GemmOpts& o = GemmOpts()) {
+  constexpr int BM = 128;
+  const bool narrow = N <= 64;
+  const int BN = narrow ? 64 : 128;
+  // chunked dimensions (see k_gemm_tc) must be whole tiles
+  if (N % BN || (A_KM && M % BM) || (!A_KM && K % kBK) || (B_NK && K % kBK))
+    throw Error(SVDAG_ERR_INVALID_ARG, "gemm: unsupported shape");
+  const int tiles = (N / BN) * ((M + BM - 1) / BM);
   int splits = 1;
-  if (!bias && !relu && !acc && tiles < 2 * ex.sm_count) {
-    splits = std::max(1, std::min(2 * ex.sm_count / tiles, K / 256));
-  }
+  const bool can_split = std::is_same<OutT, float>::value && !o.bias && !o.relu && !o.mask && !o.colsum;
+  if (can_split && tiles < ex.sm_count) splits = std::max(1, std::min(2 * ex.sm_count / tiles, K / 256));
   const int k_per = ((K + splits - 1) / splits + kBK - 1) / kBK * kBK;
   splits = (K + k_per - 1) / k_per;
-  if (splits > 1) SVDAG_CUDA(cudaMemsetAsync(C, 0, sizeof(float) * size_t(M) * N, ex.stream));
-  dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM, splits);
-  SVDAG_LAUNCH(ex, (k_gemm<TA, TB>), grid, 256, 0, A, B, C, M, N, K, k_per, bias, relu ? 1 : 0, acc ? 1 : 0);
+  if (splits > 1 && !o.zeroed) SVDAG_CUDA(cudaMemsetAsync(C, 0, sizeof(OutT) * size_t(M) * N, ex.stream));
+  const dim3 grid(N / BN, (M + BM - 1) / BM, splits);
+  if (narrow) launch_gemm<A_KM, B_NK, 128, 64, 4, OutT>(ex, grid, A, B, C, M, N, K, k_per, o);
+  else launch_gemm<A_KM, B_NK, 128, 128, 2, OutT>(ex, grid, A, B, C, M, N, K, k_per, o);
 }
 
+// Static loss scale of the fp16 backward: the loss gradient is multiplied by
+// it before it is rounded to fp16 (gradients of order 1e-6 stay normal fp16
+// values), and the epilogues that produce the fp32 parameter gradients divide
+// by it again.
+constexpr float kLossScale = 1024.f;
+
 // Siamese loss: rows [0, n) are side a, [n, 2n) side b of the embeddings.
-// pred = |e_a - e_b|^2, loss = mean (pred - t)^2; dE written for both sides.
-__global__ void k_pair_loss(const float* __restrict__ E, const float* __restrict__ t, int n, float* __restrict__ dE,
+// pred = |e_a - e_b|^2, loss = mean (pred - t)^2; dE (x kLossScale, fp16)
+// written for both sides.
+__global__ void k_pair_loss(const float* __restrict__ E, const float* __restrict__ t, int n, __half* __restrict__ dE,
                             float* __restrict__ loss) {
   for (int p = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); p < n; p += gridDim.x * (blockDim.x / 32)) {
     const int lane = threadIdx.x & 31;
@@ -131,51 +333,97 @@ __global__ void k_pair_loss(const float* __restrict__ E, const float* __restrict
     float s = d0 * d0 + d1 * d1;
     for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
     const float r = s - t[p];
-    const float g = 2.f * r / float(n);  // d loss / d pred
-    dE[size_t(p) * kOut + lane] = g * 2.f * d0;
-    dE[size_t(p) * kOut + lane + 32] = g * 2.f * d1;
-    dE[size_t(p + n) * kOut + lane] = -g * 2.f * d0;
-    dE[size_t(p + n) * kOut + lane + 32] = -g * 2.f * d1;
+    const float g = kLossScale * 2.f * r / float(n);  // d loss / d pred, scaled
+    dE[size_t(p) * kOut + lane] = __float2half_rn(g * 2.f * d0);
+    dE[size_t(p) * kOut + lane + 32] = __float2half_rn(g * 2.f * d1);
+    dE[size_t(p + n) * kOut + lane] = __float2half_rn(-g * 2.f * d0);
+    dE[size_t(p + n) * kOut + lane + 32] = __float2half_rn(-g * 2.f * d1);
     if (lane == 0) atomicAdd(loss, r * r / float(n));
   }
 }
 
-// dX *= (H > 0)
-__global__ void k_relu_back(float* __restrict__ dH, const float* __restrict__ H, size_t n) {
-  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
-    if (H[i] <= 0.f) dH[i] = 0.f;
-}
-
-// db[j] += sum over this block's rows of dY[i][j] (db zeroed by the caller)
-constexpr int kBiasRows = 128;
-__global__ void k_bias_grad(const float* __restrict__ dY, int M, int N, float* __restrict__ db) {
-  const int r0 = blockIdx.y * kBiasRows, r1 = min(M, r0 + kBiasRows);
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x) {
-    float s = 0.f;
-    for (int i = r0; i < r1; ++i) s += dY[size_t(i) * N + j];
-    atomicAdd(&db[j], s);
-  }
-}
-void bias_grad(const Exec& ex, const float* dY, int M, int N, float* db) {
-  SVDAG_CUDA(cudaMemsetAsync(db, 0, sizeof(float) * N, ex.stream));
-  SVDAG_LAUNCH(ex, k_bias_grad, dim3((N + 255) / 256, (M + kBiasRows - 1) / kBiasRows), 256, 0, dY, M, N, db);
-}
-
-__global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
-                       size_t n, float lr, float b1, float b2, float c1, float c2) {
+// Adam; also refreshes the fp16 copy of the parameters the GEMMs read.
+__global__ void k_adam(float* __restrict__ w, __half* __restrict__ wh, const float* __restrict__ g,
+                       float* __restrict__ m, float* __restrict__ v, size_t n, float lr, float b1, float b2, float c1,
+                       float c2) {
   for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
     const float gi = g[i];
     const float mi = b1 * m[i] + (1.f - b1) * gi;
     const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
     m[i] = mi;
     v[i] = vi;
-    w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + 1e-8f);
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + 1e-8f);
+    w[i] = wi;
+    wh[i] = __float2half_rn(wi);
   }
 }
 
+// Adam with the step number read from the device (training replays one
+// captured step graph): step = *counter + 1.
+__global__ void k_adam_dev(float* __restrict__ w, __half* __restrict__ wh, const float* __restrict__ g,
+                           float* __restrict__ m, float* __restrict__ v, size_t n, float lr, float b1, float b2,
+                           const unsigned long long* __restrict__ counter) {
+  const float t = float(*counter + 1);
+  const float c1 = 1.f - powf(b1, t), c2 = 1.f - powf(b2, t);
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + 1e-8f);
+    w[i] = wi;
+    wh[i] = __float2half_rn(wi);
+  }
+}
+
+// Training pairs drawn on the device from a counter-based generator
+// (splitmix64 of seed and pair index): pair i takes a candidate p at a
+// uniform sorted position and, for odd i when p's band has partners, a
+// partner inside the band (near pairs), otherwise a uniform one.  Written as
+// the pair (for the exact targets) and as input-row indices laid out per
+// batch of B pairs (the a sides, then the b sides).
+__device__ __forceinline__ uint64_t splitmix(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__global__ void k_sample_pairs(const uint32_t* __restrict__ order, const uint32_t* __restrict__ band_end, uint32_t n,
+                               uint64_t np, int B, uint64_t seed, uint2* __restrict__ pairs,
+                               uint32_t* __restrict__ rows) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < np; i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t r0 = splitmix(seed ^ (2 * i)), r1 = splitmix(seed ^ (2 * i + 1));
+    const uint32_t p = uint32_t(r0 % n);
+    const uint32_t e = band_end[p];
+    const uint32_t q = ((i & 1) && e > p + 1) ? p + 1 + uint32_t(r1 % (e - p - 1)) : uint32_t(r1 % n);
+    const uint2 pr = make_uint2(order[p], order[q]);
+    pairs[i] = pr;
+    const uint64_t b0 = i / B * B, j = i - b0;
+    rows[2 * b0 + j] = pr.x;
+    rows[2 * b0 + B + j] = pr.y;
+  }
+}
+
+// Start of a replayed training step: batch (*counter mod batches) of the
+// epoch's rows and targets into the step's fixed buffers.
+__global__ void k_batch_setup(const unsigned long long* __restrict__ counter, uint32_t batches, int B,
+                              const uint32_t* __restrict__ rows_all, const float* __restrict__ t_all,
+                              uint32_t* __restrict__ rows, float* __restrict__ t) {
+  const uint64_t b = *counter % batches;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * B; i += gridDim.x * blockDim.x) {
+    rows[i] = rows_all[2 * b * B + i];
+    if (i < B) t[i] = t_all[b * B + i];
+  }
+}
+
+__global__ void k_step_advance(unsigned long long* counter) { *counter += 1; }
+
 // Candidate features: 512 cells, the fraction of set voxels in each cell's
 // Morton-aligned block (8 voxels per cell three levels above the leaves).
-__global__ void k_features(const uint8_t* __restrict__ bytes, uint64_t per, uint32_t n, float* __restrict__ X) {
+// (The fractions k / (8 g) are exact in fp16 for the 1, 8 and 64 bytes per
+// cell of candidates 3-5 levels above the leaves.)
+__global__ void k_features(const uint8_t* __restrict__ bytes, uint64_t per, uint32_t n, __half* __restrict__ X) {
   const uint64_t g = per / kIn;  // bytes per cell
   const float inv = 1.f / float(8 * g);
   for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < uint64_t(n) * kIn;
@@ -184,20 +432,15 @@ __global__ void k_features(const uint8_t* __restrict__ bytes, uint64_t per, uint
     const uint8_t* p = bytes + c * per + f * g;
     uint32_t cnt = 0;
     for (uint64_t k = 0; k < g; ++k) cnt += __popc(uint32_t(p[k]));
-    X[i] = float(cnt) * inv;
+    X[i] = __float2half_rn(float(cnt) * inv);
   }
 }
 
-// Rows of X for a batch of pairs: side a then side b.
-__global__ void k_gather_pairs(const float* __restrict__ X, const uint2* __restrict__ pairs, int n,
-                               float* __restrict__ out) {
-  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < size_t(2 * n) * kIn;
-       i += size_t(gridDim.x) * blockDim.x) {
-    const size_t r = i / kIn, f = i % kIn;
-    const uint2 p = pairs[r < size_t(n) ? r : r - n];
-    const uint32_t c = r < size_t(n) ? p.x : p.y;
-    out[i] = X[size_t(c) * kIn + f];
-  }
+// fp32 rows -> fp16 (network input of the C ABI's test entry points, and the
+// fp16 copy of the parameters)
+__global__ void k_to_half(const float* __restrict__ x, size_t n, __half* __restrict__ out) {
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+    out[i] = __float2half_rn(x[i]);
 }
 
 // Exact normalised distance of training pairs: |a xor b| / (|a| + |b|).
@@ -283,12 +526,15 @@ struct Mlp {
     return s;
   }
   DBuf<float> w, g, m, v;
+  DBuf<__half> wh;  // fp16 copy of w, the GEMMs' operand (refreshed by Adam and set_params)
   float* p[6] = {};
   float* gp[6] = {};
+  __half* h[6] = {};
   int step = 0;
   void init(uint64_t seed, cudaStream_t st) {
     const size_t n = total();
     w.alloc(n, st);
+    wh.alloc(n, st);
     g.alloc(n, st);
     m.alloc(n, st);
     v.alloc(n, st);
@@ -307,18 +553,26 @@ struct Mlp {
     SVDAG_CUDA(cudaMemsetAsync(m.get(), 0, 4 * n, st));
     SVDAG_CUDA(cudaMemsetAsync(v.get(), 0, 4 * n, st));
     bind();
+    refresh_half(st);
     step = 0;
   }
   void bind() {
     size_t o = 0;
-    for (int t = 0; t < 6; ++t) { p[t] = w.get() + o; gp[t] = g.get() + o; o += kSizes[t]; }
+    for (int t = 0; t < 6; ++t) { p[t] = w.get() + o; gp[t] = g.get() + o; h[t] = wh.get() + o; o += kSizes[t]; }
   }
+  void refresh_half(cudaStream_t st);
 };
 constexpr size_t Mlp::kSizes[6];
+void Mlp::refresh_half(cudaStream_t st) {
+  k_to_half<<<unsigned(std::min<size_t>((total() + 255) / 256, 4096)), 256, 0, st>>>(w.get(), total(), wh.get());
+  SVDAG_CUDA(cudaGetLastError());
+}
 
+// Activations and gradients of one batch (rows = 2 x pairs: side a, then
+// side b); inputs, hidden activations and hidden gradients are fp16.
 struct MlpWork {
-  DBuf<float> X, H1, H2, E, dE, dH2, dH1, t;
-  DBuf<float> loss;
+  DBuf<__half> X, H1, H2, dE, dH2, dH1;
+  DBuf<float> E, t, loss, xin;
   int cap = 0;
   void ensure(int rows, cudaStream_t st) {
     if (rows <= cap) return;
@@ -335,31 +589,91 @@ struct MlpWork {
   }
 };
 
-void mlp_forward(const Exec& ex, Mlp& net, MlpWork& W, int rows) {
-  gemm<false, false>(ex, W.X.get(), net.p[0], W.H1.get(), rows, kH, kIn, net.p[1], true);
-  gemm<false, false>(ex, W.H1.get(), net.p[2], W.H2.get(), rows, kH, kH, net.p[3], true);
-  gemm<false, false>(ex, W.H2.get(), net.p[4], W.E.get(), rows, kOut, kH, net.p[5], false);
+// Forward of `rows` input rows (row r = X row rowmap[r] when given): fp16
+// operands (the inputs are exact in fp16) and hidden activations, fp32
+// accumulation, fp32 embeddings.
+void mlp_forward(const Exec& ex, Mlp& net, MlpWork& W, const __half* X, const uint32_t* rowmap, int rows) {
+  GemmOpts o1;
+  o1.rowmap = rowmap;
+  o1.bias = net.p[1];
+  o1.relu = true;
+  gemm_tc<false, false, __half>(ex, X, net.h[0], W.H1.get(), rows, kH, kIn, o1);
+  GemmOpts o2;
+  o2.bias = net.p[3];
+  o2.relu = true;
+  gemm_tc<false, false, __half>(ex, W.H1.get(), net.h[2], W.H2.get(), rows, kH, kH, o2);
+  GemmOpts o3;
+  o3.bias = net.p[5];
+  gemm_tc<false, false, float>(ex, W.H2.get(), net.h[4], W.E.get(), rows, kOut, kH, o3);
 }
 
-// Loss and gradients of one batch of n pairs (X rows: side a, then side b; t: targets).
-void mlp_loss_grad(const Exec& ex, Mlp& net, MlpWork& W, int n) {
+// A second stream and fork / join events for the weight-gradient GEMMs,
+// which run beside the hidden-gradient GEMMs of the same layer inside a
+// captured training step (graph branches).
+struct SideStream {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork[2] = {nullptr, nullptr}, join = nullptr;
+  void create() {
+    SVDAG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    for (auto& e : fork) SVDAG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    SVDAG_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+  }
+  ~SideStream() {
+    for (auto e : fork)
+      if (e) cudaEventDestroy(e);
+    if (join) cudaEventDestroy(join);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+// Loss and gradients of one batch of n pairs (X rows through rowmap: side a,
+// then side b; W.t: targets).  The backward runs on fp16 operands scaled by
+// kLossScale (dE, dH2, dH1), fp32 accumulation; the ReLU backward and the
+// bias gradients are fused into the GEMMs that produce dH2 and dH1 (the
+// output bias's gradient is an exact zero: the two sides of every pair
+// contribute opposite terms), and the weight-gradient epilogues undo the
+// scale.  Every gradient is zeroed by one memset.  With `side`, the weight
+// gradients of layers 3 and 2 run on the side stream, beside dH2 and dH1.
+void mlp_loss_grad(const Exec& ex, Mlp& net, MlpWork& W, const __half* X, const uint32_t* rowmap, int n,
+                   SideStream* side = nullptr) {
   const int rows = 2 * n;
-  mlp_forward(ex, net, W, rows);
+  const float inv = 1.f / kLossScale;
+  mlp_forward(ex, net, W, X, rowmap, rows);
   SVDAG_CUDA(cudaMemsetAsync(W.loss.get(), 0, 4, ex.stream));
+  SVDAG_CUDA(cudaMemsetAsync(net.g.get(), 0, 4 * Mlp::total(), ex.stream));
   SVDAG_LAUNCH(ex, k_pair_loss, grid_for(ex, n, 8), 256, 0, W.E.get(), W.t.get(), n, W.dE.get(), W.loss.get());
-  // layer 3
-  gemm<true, false>(ex, W.H2.get(), W.dE.get(), net.gp[4], kH, kOut, rows);
-  bias_grad(ex, W.dE.get(), rows, kOut, net.gp[5]);
-  gemm<false, true>(ex, W.dE.get(), net.p[4], W.dH2.get(), rows, kH, kOut);
-  SVDAG_LAUNCH(ex, k_relu_back, grid_for(ex, size_t(rows) * kH, 256), 256, 0, W.dH2.get(), W.H2.get(), size_t(rows) * kH);
-  // layer 2
-  gemm<true, false>(ex, W.H1.get(), W.dH2.get(), net.gp[2], kH, kH, rows);
-  bias_grad(ex, W.dH2.get(), rows, kH, net.gp[3]);
-  gemm<false, true>(ex, W.dH2.get(), net.p[2], W.dH1.get(), rows, kH, kH);
-  SVDAG_LAUNCH(ex, k_relu_back, grid_for(ex, size_t(rows) * kH, 256), 256, 0, W.dH1.get(), W.H1.get(), size_t(rows) * kH);
+  Exec sx = ex;
+  if (side) sx.stream = side->stream;
+  GemmOpts wg;  // weight gradients: split-K partial sums into the zeroed gradients, unscaled
+  wg.alpha = inv;
+  wg.zeroed = true;
+  GemmOpts hg;  // hidden gradients: ReLU mask, bias gradient as column sums
+  hg.colsum_scale = inv;
+  // layer 3: dW3 (side) beside dH2
+  if (side) {
+    SVDAG_CUDA(cudaEventRecord(side->fork[0], ex.stream));
+    SVDAG_CUDA(cudaStreamWaitEvent(side->stream, side->fork[0], 0));
+  }
+  gemm_tc<true, false, float>(sx, W.H2.get(), W.dE.get(), net.gp[4], kH, kOut, rows, wg);
+  hg.mask = W.H2.get();
+  hg.colsum = net.gp[3];
+  gemm_tc<false, true, __half>(ex, W.dE.get(), net.h[4], W.dH2.get(), rows, kH, kOut, hg);
+  // layer 2: dW2 (side) beside dH1
+  if (side) {
+    SVDAG_CUDA(cudaEventRecord(side->fork[1], ex.stream));
+    SVDAG_CUDA(cudaStreamWaitEvent(side->stream, side->fork[1], 0));
+  }
+  gemm_tc<true, false, float>(sx, W.H1.get(), W.dH2.get(), net.gp[2], kH, kH, rows, wg);
+  hg.mask = W.H1.get();
+  hg.colsum = net.gp[1];
+  gemm_tc<false, true, __half>(ex, W.dH2.get(), net.h[2], W.dH1.get(), rows, kH, kH, hg);
   // layer 1
-  gemm<true, false>(ex, W.X.get(), W.dH1.get(), net.gp[0], kIn, kH, rows);
-  bias_grad(ex, W.dH1.get(), rows, kH, net.gp[1]);
+  wg.rowmap = rowmap;
+  gemm_tc<true, false, float>(ex, X, W.dH1.get(), net.gp[0], kIn, kH, rows, wg);
+  if (side) {
+    SVDAG_CUDA(cudaEventRecord(side->join, side->stream));
+    SVDAG_CUDA(cudaStreamWaitEvent(ex.stream, side->join, 0));
+  }
 }
 
 void mlp_adam(const Exec& ex, Mlp& net, float lr) {
@@ -367,8 +681,8 @@ void mlp_adam(const Exec& ex, Mlp& net, float lr) {
   ++net.step;
   const float c1 = 1.f - std::pow(b1, float(net.step)), c2 = 1.f - std::pow(b2, float(net.step));
   const size_t n = Mlp::total();
-  SVDAG_LAUNCH(ex, k_adam, grid_for(ex, n, 256), 256, 0, net.w.get(), net.g.get(), net.m.get(), net.v.get(), n, lr, b1,
-               b2, c1, c2);
+  SVDAG_LAUNCH(ex, k_adam, grid_for(ex, n, 256), 256, 0, net.w.get(), net.wh.get(), net.g.get(), net.m.get(),
+               net.v.get(), n, lr, b1, b2, c1, c2);
 }
 
 // ---------------------------------------------------------------------------
@@ -387,8 +701,8 @@ struct LearnedProposer : LossyProposer {
     const cudaStream_t st = c.stream;
     const uint32_t n = S.n;
     if (S.k < 3) throw Error(SVDAG_ERR_INVALID_ARG, "lossy: learned proposals need candidates 3+ levels above the leaves");
-    // features of all candidates
-    DBuf<float> X(size_t(n) * kIn, st);
+    // features of all candidates (fp16)
+    DBuf<__half> X(size_t(n) * kIn, st);
     SVDAG_LAUNCH(ex, k_features, grid_for(ex, uint64_t(n) * kIn, 256), 256, 0,
                  reinterpret_cast<const uint8_t*>(S.bytes.get()), S.words * 8, n, X.get());
     // band of each sorted position (same bound as the exact enumeration)
@@ -406,10 +720,13 @@ struct LearnedProposer : LossyProposer {
         band_end[p] = e;
       }
     }
+    DBuf<uint32_t> d_order(n, st), d_end(n, st);
+    SVDAG_CUDA(cudaMemcpyAsync(d_order.get(), order.data(), 4ull * n, cudaMemcpyHostToDevice, st));
+    SVDAG_CUDA(cudaMemcpyAsync(d_end.get(), band_end.data(), 4ull * n, cudaMemcpyHostToDevice, st));
     if (!trained) {
       if (train) {
         const auto t0 = std::chrono::steady_clock::now();
-        fit(c, S, X, order, band_end, cfg);
+        fit(c, S, X, d_order, d_end, cfg);
         train_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
       }
       trained = true;
@@ -420,17 +737,13 @@ struct LearnedProposer : LossyProposer {
     work.ensure(chunk, st);
     for (uint32_t r0 = 0; r0 < n; r0 += chunk) {
       const int rows = int(std::min<uint32_t>(chunk, n - r0));
-      SVDAG_CUDA(cudaMemcpyAsync(work.X.get(), X.get() + size_t(r0) * kIn, 4ull * rows * kIn, cudaMemcpyDeviceToDevice, st));
-      mlp_forward(ex, net, work, rows);
+      mlp_forward(ex, net, work, X.get() + size_t(r0) * kIn, nullptr, rows);
       SVDAG_CUDA(cudaMemcpyAsync(E.get() + size_t(r0) * kOut, work.E.get(), 4ull * rows * kOut, cudaMemcpyDeviceToDevice, st));
     }
     // top-k per candidate within its band
     std::vector<uint64_t> off(n + 1, 0);
     for (uint32_t p = 0; p < n; ++p) off[p + 1] = off[p] + std::min<uint32_t>(cfg.top_k, band_end[p] - p - 1);
-    DBuf<uint32_t> d_order(n, st), d_end(n, st);
     DBuf<uint64_t> d_off(n + 1, st);
-    SVDAG_CUDA(cudaMemcpyAsync(d_order.get(), order.data(), 4ull * n, cudaMemcpyHostToDevice, st));
-    SVDAG_CUDA(cudaMemcpyAsync(d_end.get(), band_end.data(), 4ull * n, cudaMemcpyHostToDevice, st));
     SVDAG_CUDA(cudaMemcpyAsync(d_off.get(), off.data(), 8ull * (n + 1), cudaMemcpyHostToDevice, st));
     pairs.alloc(off[n] ? off[n] : 1, st);
     if (off[n])
@@ -440,43 +753,66 @@ struct LearnedProposer : LossyProposer {
     return off[n];
   }
 
-  // Training pairs: half within the bands (near pairs), half uniform.
-  void fit(Ctx& c, const LevelSubtrees& S, const DBuf<float>& X, const std::vector<uint32_t>& order,
-           const std::vector<uint32_t>& band_end, const LossyConfig& cfg) {
+  // Training pairs: half within the bands (near pairs), half uniform, drawn
+  // on the device (k_sample_pairs), rounded up to whole batches of
+  // kTrainBatch pairs; their exact targets (k_pair_target).  One training
+  // step -- batch setup, forward, loss, backward with the fused bias and
+  // ReLU gradients (the weight gradients on a parallel branch), Adam, step
+  // counter -- is captured once as a CUDA graph and replayed for every batch
+  // of every epoch (the batch and the Adam step come from a device counter),
+  // without host synchronisation.
+  void fit(Ctx& c, const LevelSubtrees& S, const DBuf<__half>& X, const DBuf<uint32_t>& d_order,
+           const DBuf<uint32_t>& d_end, const LossyConfig& cfg) {
     const Exec& ex = c.ex;
     const cudaStream_t st = c.stream;
     const uint32_t n = S.n;
-    const uint64_t np = std::max<uint64_t>(1024, cfg.train_pairs);
-    std::vector<uint2> hp(np);
-    std::mt19937_64 rng(cfg.seed * 0x9E3779B97F4A7C15ull + 7);
-    for (uint64_t i = 0; i < np; ++i) {
-      const uint32_t p = uint32_t(rng() % n);
-      uint32_t q;
-      if ((i & 1) && band_end[p] > p + 1) q = p + 1 + uint32_t(rng() % (band_end[p] - p - 1));
-      else q = uint32_t(rng() % n);
-      hp[i] = make_uint2(order[p], order[q]);
-    }
+    const int B = kTrainBatch;
+    const uint64_t batches = std::max<uint64_t>(1, (std::max<uint64_t>(1024, cfg.train_pairs) + B - 1) / B);
+    const uint64_t np = batches * B;
     DBuf<uint2> pairs(np, st);
+    DBuf<uint32_t> rows_all(2 * np, st), rows(2 * B, st);
     DBuf<float> target(np, st);
-    SVDAG_CUDA(cudaMemcpyAsync(pairs.get(), hp.data(), 8 * np, cudaMemcpyHostToDevice, st));
+    DBuf<unsigned long long> counter(1, st);
+    SVDAG_LAUNCH(ex, k_sample_pairs, grid_for(ex, np, 256), 256, 0, d_order.get(), d_end.get(), n, np, B,
+                 cfg.seed * 0x9E3779B97F4A7C15ull + 7, pairs.get(), rows_all.get());
     SVDAG_LAUNCH(ex, k_pair_target, grid_for(ex, np, 8, 16), 256, 0, S.bytes.get(), S.words, S.pop.get(), pairs.get(),
                  np, target.get());
-    const int B = 4096;
+    SVDAG_CUDA(cudaMemsetAsync(counter.get(), 0, 8, st));
     work.ensure(2 * B, st);
-    float loss = 0;
-    for (uint32_t ep = 0; ep < std::max(1u, cfg.epochs); ++ep) {
-      for (uint64_t b0 = 0; b0 < np; b0 += B) {
-        const int nb = int(std::min<uint64_t>(B, np - b0));
-        SVDAG_LAUNCH(ex, k_gather_pairs, grid_for(ex, size_t(2 * nb) * kIn, 256), 256, 0, X.get(), pairs.get() + b0, nb,
-                     work.X.get());
-        SVDAG_CUDA(cudaMemcpyAsync(work.t.get(), target.get() + b0, 4ull * nb, cudaMemcpyDeviceToDevice, st));
-        mlp_loss_grad(ex, net, work, nb);
-        mlp_adam(ex, net, 1e-3f);
-      }
-      loss = read_scalar(ex, work.loss.get());
+    Exec gx = ex;
+    gx.prof = nullptr;  // no per-launch timing events inside a captured graph
+    SideStream side;
+    side.create();
+    const uint64_t l0 = gx.launches ? *gx.launches : 0;
+    cudaGraph_t graph = nullptr;
+    SVDAG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+      SVDAG_LAUNCH(gx, k_batch_setup, 32, 256, 0, counter.get(), uint32_t(batches), B, rows_all.get(), target.get(),
+                   rows.get(), work.t.get());
+      mlp_loss_grad(gx, net, work, X.get(), rows.get(), B, &side);
+      SVDAG_LAUNCH(gx, k_adam_dev, grid_for(gx, Mlp::total(), 256), 256, 0, net.w.get(), net.wh.get(), net.g.get(),
+                   net.m.get(), net.v.get(), Mlp::total(), kTrainLr, 0.9f, 0.999f, counter.get());
+      SVDAG_LAUNCH(gx, k_step_advance, 1, 1, 0, counter.get());
+    } catch (...) {
+      cudaStreamEndCapture(st, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
     }
+    SVDAG_CUDA(cudaStreamEndCapture(st, &graph));
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ri = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    SVDAG_CUDA(ri);
+    const uint64_t steps = batches * std::max(1u, cfg.epochs);
+    cudaError_t rl = cudaSuccess;
+    for (uint64_t i = 0; i < steps && rl == cudaSuccess; ++i) rl = cudaGraphLaunch(exec, st);
+    // the replays run the step's kernels again (counted once at capture)
+    if (gx.launches) *gx.launches += (steps - 1) * (*gx.launches - l0);
+    const float loss = rl == cudaSuccess ? read_scalar(ex, work.loss.get()) : 0.f;
+    cudaGraphExecDestroy(exec);
+    SVDAG_CUDA(rl);
     last_loss = loss;
-    (void)n;
+    net.step += int(steps);
   }
 };
 
@@ -556,9 +892,14 @@ int svdag_mlp_get_params(svdag_mlp* m, float* host) {
 int svdag_mlp_set_params(svdag_mlp* m, const float* host) {
   if (!m || !host) return SVDAG_ERR_INVALID_ARG;
   cudaSetDevice(m->h.device);
-  if (cudaMemcpyAsync(m->h.net.w.get(), host, 4 * svdag::Mlp::total(), cudaMemcpyHostToDevice, m->h.stream) != cudaSuccess ||
-      cudaStreamSynchronize(m->h.stream) != cudaSuccess)
+  if (cudaMemcpyAsync(m->h.net.w.get(), host, 4 * svdag::Mlp::total(), cudaMemcpyHostToDevice, m->h.stream) != cudaSuccess)
     return SVDAG_ERR_CUDA;
+  try {
+    m->h.net.refresh_half(m->h.stream);
+  } catch (const svdag::Error& e) {
+    return e.code;
+  }
+  if (cudaStreamSynchronize(m->h.stream) != cudaSuccess) return SVDAG_ERR_CUDA;
   return SVDAG_OK;
 }
 
@@ -572,11 +913,14 @@ int svdag_mlp_loss_grad(svdag_mlp* m, const float* x_a, const float* x_b, const 
     auto& H = m->h;
     SVDAG_CUDA(cudaSetDevice(H.device));
     H.work.ensure(int(2 * n), H.stream);
-    SVDAG_CUDA(cudaMemcpyAsync(H.work.X.get(), x_a, 4ull * n * svdag::kIn, cudaMemcpyHostToDevice, H.stream));
-    SVDAG_CUDA(cudaMemcpyAsync(H.work.X.get() + size_t(n) * svdag::kIn, x_b, 4ull * n * svdag::kIn,
-                               cudaMemcpyHostToDevice, H.stream));
+    const size_t cnt = size_t(n) * svdag::kIn;
+    H.work.xin.alloc(2 * cnt, H.stream);
+    SVDAG_CUDA(cudaMemcpyAsync(H.work.xin.get(), x_a, 4 * cnt, cudaMemcpyHostToDevice, H.stream));
+    SVDAG_CUDA(cudaMemcpyAsync(H.work.xin.get() + cnt, x_b, 4 * cnt, cudaMemcpyHostToDevice, H.stream));
+    SVDAG_LAUNCH(H.ex, svdag::k_to_half, svdag::grid_for(H.ex, 2 * cnt, 256), 256, 0, H.work.xin.get(), 2 * cnt,
+                 H.work.X.get());
     SVDAG_CUDA(cudaMemcpyAsync(H.work.t.get(), t, 4ull * n, cudaMemcpyHostToDevice, H.stream));
-    svdag::mlp_loss_grad(H.ex, H.net, H.work, int(n));
+    svdag::mlp_loss_grad(H.ex, H.net, H.work, H.work.X.get(), nullptr, int(n));
     SVDAG_CUDA(cudaMemcpyAsync(loss, H.work.loss.get(), 4, cudaMemcpyDeviceToHost, H.stream));
     SVDAG_CUDA(cudaMemcpyAsync(grads, H.net.g.get(), 4 * svdag::Mlp::total(), cudaMemcpyDeviceToHost, H.stream));
     SVDAG_CUDA(cudaStreamSynchronize(H.stream));
@@ -593,8 +937,12 @@ int svdag_mlp_embed(svdag_mlp* m, const float* x, uint32_t n, float* out) {
     auto& H = m->h;
     SVDAG_CUDA(cudaSetDevice(H.device));
     H.work.ensure(int(n), H.stream);
-    SVDAG_CUDA(cudaMemcpyAsync(H.work.X.get(), x, 4ull * n * svdag::kIn, cudaMemcpyHostToDevice, H.stream));
-    svdag::mlp_forward(H.ex, H.net, H.work, int(n));
+    const size_t cnt = size_t(n) * svdag::kIn;
+    H.work.xin.alloc(cnt, H.stream);
+    SVDAG_CUDA(cudaMemcpyAsync(H.work.xin.get(), x, 4 * cnt, cudaMemcpyHostToDevice, H.stream));
+    SVDAG_LAUNCH(H.ex, svdag::k_to_half, svdag::grid_for(H.ex, cnt, 256), 256, 0, H.work.xin.get(), cnt,
+                 H.work.X.get());
+    svdag::mlp_forward(H.ex, H.net, H.work, H.work.X.get(), nullptr, int(n));
     SVDAG_CUDA(cudaMemcpyAsync(out, H.work.E.get(), 4ull * n * svdag::kOut, cudaMemcpyDeviceToHost, H.stream));
     SVDAG_CUDA(cudaStreamSynchronize(H.stream));
     return SVDAG_OK;

@@ -49,10 +49,26 @@ def test_network_gradients_match_cpu_model():
     t = rng.random(40).astype(np.float32)
     loss, g = m.loss_grad(xa, xb, t)
     rl, rg = mlp_ref.loss_grad(w, xa, xb, t)
-    assert abs(loss - rl) <= 1e-4 * max(1.0, abs(rl))
-    assert np.max(np.abs(g - rg)) <= 1e-3 * max(1e-6, np.max(np.abs(rg)))
+    # tensor-core operands: fp16 (11-bit significands; the backward scaled
+    # by a static loss scale), fp32 accumulation.  Tolerances: the loss within
+    # 1 % of the float64 model's; per parameter block (W1 b1 W2 b2 W3 b3) the
+    # gradient within 2 % in L2 norm and every element within 5 % of the
+    # block's largest (the output bias's gradient is an exact zero in the
+    # model -- the two sides' terms cancel -- so it is held to an absolute
+    # bound instead); embeddings within 1 % of the largest
+    assert abs(loss - rl) <= 1e-2 * max(1.0, abs(rl))
+    bounds = np.cumsum([0] + [int(np.prod(s)) for s in mlp_ref.SHAPES])
+    for blk, (lo, hi) in enumerate(zip(bounds[:-1], bounds[1:])):
+        ref, got = rg[lo:hi], g[lo:hi]
+        if blk == 5:
+            assert np.max(np.abs(got)) <= 1e-3 * np.max(np.abs(rg)), blk
+            continue
+        err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        assert err <= 2e-2, (blk, err)
+        assert np.max(np.abs(got - ref)) <= 5e-2 * np.max(np.abs(ref)), blk
     e = m.embed(xa)
-    assert np.allclose(e, mlp_ref.forward(w, xa.astype(np.float64))[2], rtol=1e-4, atol=1e-4)
+    er = mlp_ref.forward(w, xa.astype(np.float64))[2]
+    assert np.max(np.abs(e - er)) <= 1e-2 * np.max(np.abs(er))
 
 
 def test_training_beats_the_untrained_network():
