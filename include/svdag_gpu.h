@@ -113,6 +113,29 @@ int svdag_tri_box_children(svdag_ctx* ctx, const float* tris, const double* cent
                            uint64_t n, uint8_t* masks, uint64_t* fallbacks);
 /* GeomOctree::toDAG (src/symvox/geom_octree.cpp:462-548) */
 int svdag_reduce_dag(svdag_ctx* ctx);
+/* GeomOctree::sortByEffectiveRefCount (src/symvox/geom_octree_extension.cpp:
+ * 521-620): every level of a DAG reordered by effective reference count
+ * (root paths to the node, 32-bit unsigned sums), descending, in exactly the
+ * order the reference's unstable std::sort gives, children renamed.  The
+ * first step of toLossyDag (:887). */
+int svdag_sort_by_effective_refcount(svdag_ctx* ctx);
+/* The candidate edges toLossyDag (src/symvox/geom_octree_extension.cpp:
+ * 904-1049) builds at `level` of a DAG in effective-reference-count order
+ * (svdag_sort_by_effective_refcount), before its MCL clustering: for every
+ * node A whose effective count is at most included_ref_count and that is not
+ * a parent of a cluster representative of the level below (reps_below: one
+ * byte per node of level + 1, non-zero = representative; NULL = none), each
+ * earlier node B with such a count and the same node hash (computeNodeHash
+ * at depth max(levels - level - 2, 1)) -- at levels - 2, a hash one bit away,
+ * weight 1 -- whose subtree difference (diffSubtrees, with its abort rules)
+ * is within round((levels - level)^2 * diff_factor) and below 4 per compared
+ * leaf, weight 1 - diff / (max + 1).  Edges (src = A, tgt = B, weight) are
+ * written sorted by (src, tgt); *count receives their number.  With
+ * capacity 0 and NULL arrays the call only counts; a capacity below the
+ * count is SVDAG_ERR_OVERFLOW.  1 <= level <= levels - 2. */
+int svdag_lossy_candidates(svdag_ctx* ctx, uint32_t level, float diff_factor, int included_ref_count,
+                           const uint8_t* reps_below, uint32_t* src, uint32_t* tgt, float* weight, uint64_t capacity,
+                           uint64_t* count);
 /* GeomOctree::initChildLevels (src/symvox/geom_octree_extension.cpp:21-30) */
 int svdag_init_child_levels(svdag_ctx* ctx);
 /* GeomOctree::toSDAG(false, false) (src/symvox/geom_octree.cpp:551-697) */

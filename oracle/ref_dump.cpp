@@ -17,6 +17,13 @@
 //                     + one outsideMask byte per node.  Runs last: the
 //                     reference exits when the start corner cell is set,
 //                     after every other output is written
+//   --lossy <infl> <diff> <refs>
+//                     GeomOctree::toLossyDag (geom_octree_extension.cpp:
+//                     797-1179) on a copy of the DAG, in the working
+//                     directory: its candidate edges go to edges<lev>.txt
+//                     before it runs the external MCL program as
+//                     $HOME/local/bin/mcl (cluster.hpp:134-192), which the
+//                     caller provides
 //   --traverse <pts>  <out_prefix>.trav: EncodedSSVDAG::traverse
 //                     (encoded_ssvdag.cpp:527-574) of the .ssvdag encoding
 //                     for every point of <pts> (u64 n, then n float[3]); one
@@ -131,14 +138,16 @@ static void dump_traverse(const EncodedSSVDAG& enc, const std::string& pts_path,
 int main(int argc, char** argv) {
   if (argc < 4) {
     std::fprintf(stderr, "usage: ref_dump scene.obj levels out_prefix [step_levels] [--soup|--soup-only] [--flood] "
-                         "[--traverse points]\n");
+                         "[--traverse points] [--lossy infl diff refs]\n");
     return 1;
   }
   std::string obj = argv[1];
   unsigned levels = (unsigned)std::atoi(argv[2]);
   std::string pre = argv[3];
   int step = 0;
-  bool soup = false, soup_only = false, flood = false;
+  bool soup = false, soup_only = false, flood = false, lossy = false;
+  float infl = 2.f, diff_factor = 1.f;
+  int refs = 1;
   std::string trav_pts;
   for (int a = 4; a < argc; ++a) {
     const std::string o = argv[a];
@@ -146,6 +155,12 @@ int main(int argc, char** argv) {
     else if (o == "--soup-only") soup = soup_only = true;
     else if (o == "--flood") flood = true;
     else if (o == "--traverse" && a + 1 < argc) trav_pts = argv[++a];
+    else if (o == "--lossy" && a + 3 < argc) {
+      lossy = true;
+      infl = std::strtof(argv[++a], nullptr);
+      diff_factor = std::strtof(argv[++a], nullptr);
+      refs = std::atoi(argv[++a]);
+    }
     else step = std::atoi(argv[a]);
   }
 
@@ -209,6 +224,12 @@ int main(int argc, char** argv) {
       levels, st_svo.nTotalVoxels, st_svo.nNodesSVO, st_svo.nNodesLastLevSVO, oct.getStats().nNodesDAG,
       sd.getStats().nNodesSDAG, cs.getNNodes(), merged, t_dag, t_sdag, t_csv);
   std::fflush(stdout);
+  if (lossy) {
+    GeomOctree lo(oct);
+    lo.toLossyDag(infl, diff_factor, refs);
+    std::printf("REFLOSSY {\"nodes_after\": %zu}\n", lo.getNNodes());
+    std::fflush(stdout);
+  }
   if (svo_copy) {
     // GeomOctree::Node's constructor (octree_node.cpp:22-37) leaves
     // outsideMask uninitialised (geom_octree.hpp:64) while the fill only ever

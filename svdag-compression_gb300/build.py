@@ -28,7 +28,7 @@ CXX = os.environ.get("CXX", "g++")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # extra nvcc flags (e.g. tuning macros), whitespace separated
 EXTRA_NVCC = os.environ.get("SVDAG_NVCC_FLAGS", "").split()
-CU_SOURCES = ["api.cu", "voxelize.cu", "reduce.cu", "csvdag.cu", "chunked.cu", "batch.cu", "lossy.cu", "mlp.cu", "encode.cu", "traverse.cu", "raycast.cu", "floodfill.cu", "noalloc.cu", "refsort.cu"]
+CU_SOURCES = ["api.cu", "voxelize.cu", "reduce.cu", "csvdag.cu", "chunked.cu", "batch.cu", "lossy.cu", "mlp.cu", "encode.cu", "traverse.cu", "raycast.cu", "floodfill.cu", "noalloc.cu", "refsort.cu", "lossy_ref.cu"]
 HOST_SOURCES = ["synth.cpp", "encoders.cpp", "scene.cpp", "geom_octree.cpp"]
 
 

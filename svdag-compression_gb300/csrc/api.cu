@@ -1,6 +1,8 @@
 // C ABI of the SVDAG construction path (include/svdag_gpu.h).
 #include <algorithm>
 #include <cstring>
+#include <string>
+#include <vector>
 #include <new>
 
 #include "ctx.cuh"
@@ -251,6 +253,33 @@ int svdag_tri_box_children(svdag_ctx* h, const float* tris, const double* center
   if (n && (!tris || !centers || !half_sides || !masks))
     return fail(h, SVDAG_ERR_INVALID_ARG, "tri_box_children: null buffer");
   return guarded(h, [&](Ctx& c) { svdag::tri_box_children(c, tris, centers, half_sides, n, masks, fallbacks); });
+}
+
+int svdag_sort_by_effective_refcount(svdag_ctx* h) {
+  return guarded(h, [&](Ctx& c) { svdag::phase_sort_by_effective_refcount(c); });
+}
+
+int svdag_lossy_candidates(svdag_ctx* h, uint32_t level, float diff_factor, int included_ref_count,
+                           const uint8_t* reps_below, uint32_t* src, uint32_t* tgt, float* weight, uint64_t capacity,
+                           uint64_t* count) {
+  if (!count) return fail(h, SVDAG_ERR_INVALID_ARG, "lossy candidates: null count");
+  return guarded(h, [&](Ctx& c) {
+    std::vector<uint32_t> s, t;
+    std::vector<float> w;
+    svdag::lossy_candidate_edges(c, level, diff_factor, included_ref_count, reps_below, s, t, w);
+    *count = s.size();
+    if (s.size() > capacity || (!s.empty() && (!src || !tgt || !weight))) {
+      if (capacity || src || tgt || weight)
+        throw Error(SVDAG_ERR_OVERFLOW, "lossy candidates: " + std::to_string(s.size()) + " edges, capacity " +
+                                            std::to_string(capacity));
+      return;  // size query
+    }
+    if (!s.empty()) {
+      std::memcpy(src, s.data(), 4 * s.size());
+      std::memcpy(tgt, t.data(), 4 * t.size());
+      std::memcpy(weight, w.data(), 4 * w.size());
+    }
+  });
 }
 
 int svdag_init_child_levels(svdag_ctx* h) {

@@ -84,6 +84,10 @@ void refcount_order(const Exec& ex, const uint32_t* counts, uint64_t n, uint32_t
 // and out (voxelize.cu).
 void tri_box_children(Ctx& c, const float* tris, const double* centers, const double* half_sides, uint64_t n,
                       uint8_t* masks, uint64_t* fallbacks);
+// The reference's lossy candidate stage (lossy_ref.cu).
+void phase_sort_by_effective_refcount(Ctx& c);
+void lossy_candidate_edges(Ctx& c, uint32_t level, float diff_factor, int included, const uint8_t* reps_below,
+                           std::vector<uint32_t>& src, std::vector<uint32_t>& tgt, std::vector<float>& weight);
 // toDAG with every temporary in caller-provided device scratch (no allocation).
 void phase_reduce_dag_scratch(Ctx& c, uint8_t* scratch, uint64_t capacity);
 

@@ -66,6 +66,8 @@ GPU_SYMBOLS = {
     "svdag_voxelize": (_I, [_VP, _U32, _VP]),
     "svdag_build_dag": (_I, [_VP, _U32, _U32, _VP]),
     "svdag_reduce_dag": (_I, [_VP]),
+    "svdag_sort_by_effective_refcount": (_I, [_VP]),
+    "svdag_lossy_candidates": (_I, [_VP, _U32, ctypes.c_float, _I, _VP, _VP, _VP, _VP, _U64, ctypes.POINTER(_U64)]),
     "svdag_tri_box_children": (_I, [_VP, _VP, _VP, _VP, _U64, _VP, ctypes.POINTER(_U64)]),
     "svdag_init_child_levels": (_I, [_VP]),
     "svdag_reduce_sdag": (_I, [_VP]),
@@ -428,6 +430,26 @@ class Octree:
         s = _LossyStats()
         self._check(self._lib.svdag_lossy_dag(self._h, ctypes.byref(p), ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in _LossyStats._fields_}
+
+    def sortByEffectiveRefCount(self):
+        """GeomOctree::sortByEffectiveRefCount on the GPU."""
+        self._check(self._lib.svdag_sort_by_effective_refcount(self._h))
+
+    def lossyCandidates(self, level, diff_factor=1.0, included_ref_count=1, reps_below=None):
+        """The reference toLossyDag's candidate edges at `level` (see
+        svdag_lossy_candidates): (src, tgt, weight) arrays sorted by (src, tgt)."""
+        reps = None if reps_below is None else np.ascontiguousarray(reps_below, np.uint8)
+        rp = reps.ctypes.data if reps is not None else None
+        cnt = _U64()
+        self._check(self._lib.svdag_lossy_candidates(self._h, level, diff_factor, included_ref_count, rp, None, None,
+                                                     None, 0, ctypes.byref(cnt)))
+        n = cnt.value
+        src, tgt, w = np.zeros(n, np.uint32), np.zeros(n, np.uint32), np.zeros(n, np.float32)
+        if n:
+            self._check(self._lib.svdag_lossy_candidates(self._h, level, diff_factor, included_ref_count, rp,
+                                                         src.ctypes.data, tgt.ctypes.data, w.ctypes.data, n,
+                                                         ctypes.byref(cnt)))
+        return src, tgt, w
 
     def toDAG_noalloc(self):
         """toDAG with the library's static device scratch (no allocation);

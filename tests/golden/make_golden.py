@@ -60,6 +60,50 @@ FLOOD = {"ico3_L6", "ico5_L7", "terrain65_L8", "terrain129_L9", "cavity_L7", "ic
 TRAVERSE = {"ico3_L6", "ico5_L7"}
 
 
+# cases whose DAG goes through the reference's toLossyDag up to its MCL
+# clustering: name -> (inflation, allowed diff factor, included ref count).
+# A stand-in `mcl` records every batch of candidate edges the reference
+# writes (edges<lev>.txt, cluster.hpp:145-152) and answers with singleton
+# clusters; the edges of the two lowest processed levels (levels - 2, one-bit
+# hash probe; levels - 3, hash + diffSubtrees) are kept.
+LOSSY = {"terrain65_L8": (2.0, 1.0, 1), "ico5_L7": (2.0, 1.0, 1), "boxes_L8": (2.0, 2.0, 2),
+         "terrain129_L9": (2.0, 1.5, 3)}
+FAKE_MCL = """#!/bin/sh
+# stand-in for the MCL program: keeps the edges file, answers singletons
+in="$1"; out=""
+while [ $# -gt 0 ]; do if [ "$1" = "-o" ]; then out="$2"; fi; shift; done
+cat "$in" >> "$in.all"
+awk '{print $1; print $2}' "$in" | sort -n -u > "$out"
+"""
+
+
+def run_lossy(name, obj, levels, params):
+    """Runs the reference's toLossyDag on the scene's DAG with the stand-in
+    MCL; returns the candidate edges of levels - 2 and levels - 3."""
+    with tempfile.TemporaryDirectory() as td:
+        home = os.path.join(td, "home")
+        os.makedirs(os.path.join(home, "local", "bin"))
+        mcl = os.path.join(home, "local", "bin", "mcl")
+        with open(mcl, "w") as f:
+            f.write(FAKE_MCL)
+        os.chmod(mcl, 0o755)
+        env = dict(os.environ, HOME=home)
+        r = subprocess.run([REF_DUMP, obj, str(levels), os.path.join(td, "out"), "--lossy"] + [str(x) for x in params],
+                           cwd=td, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        # the reference's progress logger divides by zero on levels of fewer
+        # than 5 nodes (round(size / 10) == 0) and takes the process down
+        # there; the levels below it are complete once the next one started
+        started = {int(x.split(":")[0]) for x in r.stdout.split("\nLevel ")[1:]}
+        out = {}
+        for lev in (levels - 2, levels - 3):
+            assert r.returncode == 0 or (lev - 1) in started, (name, lev, r.returncode)
+            path = os.path.join(td, "edges%d.txt.all" % lev)
+            rows = [l.split() for l in open(path)] if os.path.exists(path) else []
+            rows.sort(key=lambda t: (int(t[0]), int(t[1])))
+            out[lev] = rows
+        return out
+
+
 # seeded OBJ files of tests/_objgen.py (without the face records the
 # reference's loader crashes on) run through the reference's Scene::loadObj:
 # name -> (seed, lines, final newline)
@@ -146,6 +190,16 @@ def run_case(name, make, levels, step, keep):
             res = np.fromfile(pre + ".trav", np.int32)
             np.savez_compressed(os.path.join(HERE, name + "_traverse.npz"), depth=res.astype(np.int8))
             info["traverse"] = {"points": int(res.size), "file": name + "_traverse.npz"}
+        if name in LOSSY:
+            edges = run_lossy(name, obj, levels, LOSSY[name])
+            arrs, info_l = {}, {}
+            for lev, rows in edges.items():
+                arrs["l%d_src" % lev] = np.array([int(t[0]) for t in rows], np.uint32)
+                arrs["l%d_tgt" % lev] = np.array([int(t[1]) for t in rows], np.uint32)
+                arrs["l%d_w" % lev] = np.array([t[2] for t in rows], "<U16")
+                info_l[str(lev)] = len(rows)
+            np.savez_compressed(os.path.join(HERE, name + "_lossy.npz"), **arrs)
+            info["lossy"] = {"params": list(LOSSY[name]), "edges": info_l, "file": name + "_lossy.npz"}
         if name in FLOOD:
             masks = read_levels_u8(pre + ".outside")
             info["outside"] = {"counts": [int(len(m)) for m in masks], "digest": levels_digest(masks),
