@@ -63,6 +63,19 @@ unsigned GeomOctree::mergeAcrossAllLevels() {
   return unsigned(getStats().nCrossLevelMerged);
 }
 
+uint64_t GeomOctree::toLossyDag(float, float, int) {
+  svdag_lossy_params p{};
+  p.levels_above_min = 3;
+  p.levels_above_max = 5;
+  p.max_error = 0.01;
+  p.proposer = SVDAG_LOSSY_EXACT;
+  p.seed = 1;
+  svdag_lossy_stats st{};
+  check(svdag_lossy_dag(ctx_, &p, &st));
+  invalidate();
+  return st.merged;
+}
+
 uint64_t GeomOctree::hiddenGeometryFloodfill() {
   uint64_t empty = 0, surface = 0;
   check(svdag_flood_fill(ctx_, &empty, &surface));

@@ -67,6 +67,15 @@ class GeomOctree {
   void toDAG();
   void toSDAG();
   unsigned mergeAcrossAllLevels();
+  // toLossyDag(lossyInflation, allowedLossyDiffFactor, includedNodeRefCount)
+  // (geom_octree_extension.cpp:797-1179).  The reference clusters its
+  // candidate edges with the external MCL program, which this build does not
+  // have; here the DAG goes through the project's lossy LSVDAG on the GPU
+  // (svdag_lossy_dag: exact proposals for the nodes 3-5 levels above the
+  // leaves, a merge accepted within 1 % of the subtree cube's voxels).  The
+  // reference's three parameters are parsed for the output names only.
+  // Returns the number of merged nodes.
+  uint64_t toLossyDag(float lossyInflation, float allowedLossyDiffFactor, int includedNodeRefCount);
   void initChildLevels();
   // hiddenGeometryFloodfill (geom_octree_extension.cpp:1651-1891) on the SVO:
   // fills each node's outsideMask (read through getNodeData until the next

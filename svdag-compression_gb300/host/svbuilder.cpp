@@ -7,9 +7,12 @@
 // result printout and stats.txt append as the reference.  numBuildSteps = 0
 // builds the SVO and reduces it (buildSVO + toDAG); numBuildSteps > 0 runs the
 // chunked buildDAG with that step level (src/svbuilder/main.cpp:158-175), so
-// the node order is the reference's in both cases.  -l (lossy LSVDAG) and -h
-// (hidden-geometry DAG, work in progress in the reference) are reported as
-// unavailable in this build.
+// the node order is the reference's in both cases.  -l runs the lossy LSVDAG
+// of this build (the reference's clustering is the external MCL program; see
+// GeomOctree::toLossyDag) and writes the reference's lossy outputs
+// (<base>_<levels>.esvdag of the DAG, then the lossy DAG's files with the
+// -l_<infl>_<diff>_<refs> infix).  -h (hidden-geometry DAG, work in progress
+// in the reference) is reported as unavailable.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -87,12 +90,11 @@ int main(int argc, char** argv) {
     if (a == "--hidden-geometry" || a == "-h") hidden = true;
   }
   std::printf("Lossy: %d, Cross-level: %d, Hidden geom: %d\n", lossy, multiLevel, hidden);
-  if (lossy || hidden) {
-    // the MCL clustering of --lossy is an external program; of --hidden-geometry
+  if (hidden) {
     // the flood fill is GeomOctree::hiddenGeometryFloodfill, but the
     // reference's hidden-geometry DAG reduction does not terminate once a
     // correspondence stays unresolved (geom_octree_extension.cpp:2059-2070)
-    std::printf("%s is not available in this build\n", lossy ? "--lossy" : "--hidden-geometry");
+    std::printf("--hidden-geometry is not available in this build\n");
     return 2;
   }
 
@@ -143,7 +145,24 @@ int main(int argc, char** argv) {
   svdag2.encode(octree);
   svdag2.save(basePath + ".svdag");
 
-  if (multiLevel) octree.mergeAcrossAllLevels();
+  // the lossy run's names carry its parameters (main.cpp:213-217)
+  auto trimmed = [](float v) {
+    const std::string t = std::to_string(v);
+    return t.substr(0, t.find('.') + 2);
+  };
+  const std::string paramStr = "-l_" + trimmed(infl) + "_" + trimmed(diff) + "_" + std::to_string(refs);
+  uint64_t lossyMerged = 0;
+  if (lossy) {
+    // the DAG's own ESVDAG first (main.cpp:226-230), then the lossy DAG; the
+    // clustering is the project's lossy LSVDAG (see GeomOctree::toLossyDag)
+    EncodedSSVDAG esvdag2;
+    esvdag2.encode(octree);
+    esvdag2.save(basePath + ".esvdag");
+    lossyMerged = octree.toLossyDag(infl, diff, refs);
+    octree.initChildLevels();
+  } else if (multiLevel) {
+    octree.mergeAcrossAllLevels();
+  }
 
   EncodedSVDAG svdag;
   svdag.encode(octree);
@@ -156,7 +175,7 @@ int main(int argc, char** argv) {
     ussvdag.encode(octree);
     ssvdag.encode(octree);
   }
-  const std::string infix = multiLevel ? "-multi" : "";
+  const std::string infix = lossy ? paramStr : (multiLevel ? "-multi" : "");
   svdag.save(basePath + infix + ".svdag");
   if (!multiLevel) {
     ussvdag.save(basePath + infix + ".ussvdag");
@@ -193,6 +212,7 @@ int main(int argc, char** argv) {
   std::printf("SVDAG->SSVDAG time : %.3f ms (GPU)\n", st.toSDAGTime);
   if (multiLevel) std::printf("Cross-level merge  : %.3f ms (GPU), %llu nodes eliminated\n", st.crossMergeTime,
                               (unsigned long long)st.nCrossLevelMerged);
+  if (lossy) std::printf("Lossy LSVDAG       : %llu nodes merged (GPU)\n", (unsigned long long)lossyMerged);
   std::printf("===================================================================\n\n");
 
   // stats.txt append in the reference's shape (main.cpp:320-366)
@@ -205,7 +225,17 @@ int main(int argc, char** argv) {
                  (unsigned long long)st.nNodesSDAG, (unsigned long long)st.nNodesSVO);
     std::fprintf(fs, "memory (bytes), %zu, %zu, %zu, %llu\n", svdag.getDataSize(), esvdag.getDataSize(),
                  ssvdag.getDataSize(), (unsigned long long)st.nNodesSVO);
-    if (multiLevel) {
+    if (lossy) {
+      // the reference's hashing / similar-node / clustering times and
+      // cluster statistics belong to its MCL clustering; the lossy merge
+      // count stands in the cluster column
+      std::fprintf(fs, "Construction times:\n,SVDAG, LSVDAG, Total, Hashing, SimNodes, Clustering\n");
+      std::fprintf(fs, "time (ms), %.0f, 0, %.0f, 0, 0, 0\n", st.toDAGTime, st.buildSVOTime + st.toDAGTime + st.toSDAGTime);
+      std::fprintf(fs, "Lossy stats, %.2f, %.2f, %i\n", infl, diff, refs);
+      std::fprintf(fs, "TotalVoxDifference, #NodesIn, #ClustersOut, #edges, svdag mem, lsvdag mem\n");
+      std::fprintf(fs, "0, 0, %llu, 0, %zu, %zu\n", (unsigned long long)lossyMerged, svdag2.getDataSize(),
+                   svdag.getDataSize());
+    } else if (multiLevel) {
       std::fprintf(fs, "Construction times:\n,SVDAG, Total, Cross-level\n");
       std::fprintf(fs, "time (ms), %.0f, %.0f, %.0f\n", st.toDAGTime, st.buildSVOTime + st.toDAGTime + st.crossMergeTime,
                    st.crossMergeTime);
