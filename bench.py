@@ -418,7 +418,10 @@ def run_ours(args, rank, local, world):
         launches_per_step = n / args.steps
         ab = B.get(name)  # algorithmic bytes of one step's launches
         achieved = (ab / launches_per_step) / (per_launch_ms / 1e3) / 1e9 if ab else None
-        roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+        # k_expand is bound by instruction issue (SAT arithmetic), not HBM;
+        # its algorithmic bytes over HBM bandwidth are reported all the same
+        roof = {"kernel": name, "bound": "issue" if name == "k_expand" else "hbm", "achieved": achieved,
+                "peak": hbm_peak, "unit": "GB/s",
                 "frac": (achieved / hbm_peak) if achieved else None,
                 "traffic": (KERNEL_DRAM_BYTES_PER_LAUNCH.get(name)
                             if args.workload == "terrain" and args.grid == 2048 and args.levels == 12 else None),
