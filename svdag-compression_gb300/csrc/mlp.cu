@@ -294,10 +294,15 @@ void launch_gemm(const Exec& ex, dim3 grid, const __half* A, const __half* B, Ou
 // gradients: at most 512 x 256 outputs over K = 2 x batch rows); split
 // results are atomic partial sums into C (fp32), which is zeroed here unless
 // the caller already did.
+// Row-major A (M = batch rows, many tiles) uses 64-row tiles: twice the
+// blocks of 128-row ones, two of them resident per SM (the GEMMs are small
+// and latency-bound; ncu: one 8-warp block per SM left the tensor pipe busy
+// a quarter of the time).  K-major A (M = a layer width) keeps 128 rows and
+// splits K instead.
 template <bool A_KM, bool B_NK, class OutT>
 void gemm_tc(const Exec& ex, const __half* A, const __half* B, OutT* C, int M, int N, int K,
              const GemmOpts& o = GemmOpts()) {
-  constexpr int BM = 128;
+  constexpr int BM = A_KM ? 128 : 64;
   const bool narrow = N <= 64;
   const int BN = narrow ? 64 : 128;
   // chunked dimensions (see k_gemm_tc) must be whole tiles
@@ -311,8 +316,13 @@ void gemm_tc(const Exec& ex, const __half* A, const __half* B, OutT* C, int M, i
   splits = (K + k_per - 1) / k_per;
   if (splits > 1 && !o.zeroed) SVDAG_CUDA(cudaMemsetAsync(C, 0, sizeof(OutT) * size_t(M) * N, ex.stream));
   const dim3 grid(N / BN, (M + BM - 1) / BM, splits);
-  if (narrow) launch_gemm<A_KM, B_NK, 128, 64, 4, OutT>(ex, grid, A, B, C, M, N, K, k_per, o);
-  else launch_gemm<A_KM, B_NK, 128, 128, 2, OutT>(ex, grid, A, B, C, M, N, K, k_per, o);
+  if constexpr (A_KM) {
+    if (narrow) launch_gemm<A_KM, B_NK, 128, 64, 4, OutT>(ex, grid, A, B, C, M, N, K, k_per, o);
+    else launch_gemm<A_KM, B_NK, 128, 128, 2, OutT>(ex, grid, A, B, C, M, N, K, k_per, o);
+  } else {
+    if (narrow) launch_gemm<A_KM, B_NK, 64, 64, 2, OutT>(ex, grid, A, B, C, M, N, K, k_per, o);
+    else launch_gemm<A_KM, B_NK, 64, 128, 2, OutT>(ex, grid, A, B, C, M, N, K, k_per, o);
+  }
 }
 
 // Static loss scale of the fp16 backward: the loss gradient is multiplied by
