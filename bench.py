@@ -69,6 +69,9 @@ def parse():
     ap.add_argument("--boxes", type=int, default=200000)
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--reduction-sms", type=int, default=None,
+                    help="SMs the SSVDAG and CSVDAG reductions may take while the next step builds (pipelined "
+                         "steps; default a quarter of the GPU; 0 = all)")
     ap.add_argument("--no-pipeline", action="store_true",
                     help="terrain/city: run the timed steps one after another instead of overlapping a step's "
                          "SSVDAG / CSVDAG reductions with the next step's voxelization")
@@ -285,13 +288,17 @@ def run_ours(args, rank, local, world):
         if profile:
             collect("dag", octree)
 
-    def start_reductions(octree, profile=False):
+    def start_reductions(octree, profile=False, cap=0):
         # the SSVDAG and CSVDAG reductions of the same DAG are independent:
         # two clones on their own streams, driven from two host threads (a
         # clone is complete when clone() returns, so the octree may be
-        # rebuilt while they run)
+        # rebuilt while they run); `cap` SMs each when they share the GPU
+        # with the next build
         s = octree.clone(stream=red_streams[0].cuda_stream)
         c = octree.clone(stream=red_streams[1].cuda_stream) if have_csv else None
+        for o in (s, c):
+            if o is not None:
+                o.set_persistent_blocks(cap)
         for o in (s, c):
             if profile and o is not None:
                 o.profile(True)
@@ -359,7 +366,7 @@ def run_ours(args, rank, local, world):
                 build(base)
                 if pending is not None:
                     outs.append(finish(pending))
-                pending = start_reductions(base)
+                pending = start_reductions(base, cap=red_sms)
             else:
                 outs.append(step(base, profile=events))
         if pending is not None:
@@ -383,6 +390,8 @@ def run_ours(args, rank, local, world):
                 a[0] += n
                 a[1] += ms
         return ms_total, prof, base.stats()["gpu_launches"] - launches0 + extra, outs
+
+    red_sms = reduction_sms(args, torch, dev)
 
     # timed region: K steps, clocks sampled meanwhile
     clocks = ClockSampler(local)
@@ -484,6 +493,7 @@ def run_ours(args, rank, local, world):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clk, "gpu_launches": int(launches), "roofline": roof, "reduction_roofline": red, "e2e": e2e,
         "pipelined": not args.no_pipeline,
+        "reduction_sms": red_sms if not args.no_pipeline else 0,
         "sequential_ms_per_step": ms_seq,
         "kernel_events_region_ms_per_step": ms_events / args.steps,
         "kernel_ms_per_step": sum(v[1] for v in prof.values()) / args.steps,
@@ -516,6 +526,15 @@ def level_info(sv, base, s_last, args):
     return {"svo": svo, "svo_total": st["n_nodes_svo"], "dag": dag, "frontier": [st["frontier_pairs"]],
             "sdag": [s_last.level_count(l) for l in range(levels)], "sat_fallbacks": st["sat_fallbacks"],
             "svo_digest": None if args.step_level else svo_digest}
+
+
+def reduction_sms(args, torch, dev):
+    """SMs each of the SSVDAG and CSVDAG reductions may take while the next
+    step voxelizes (their persistent kernels start only when their whole grid
+    fits, so a full-GPU grid would wait for, then exclude, the build)."""
+    if args.reduction_sms is not None:
+        return max(0, args.reduction_sms)
+    return max(1, torch.cuda.get_device_properties(dev).multi_processor_count // 4)
 
 
 def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
@@ -573,9 +592,14 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
             o.toDAG()
         o.initChildLevels()
 
+    red_sms = 0 if args.no_pipeline else reduction_sms(args, torch, torch.device("cuda", local))
+
     def start_one():
         s = o.clone(stream=red_streams[0].cuda_stream)
         c = o.clone(stream=red_streams[1].cuda_stream) if have_csv else None
+        for x in (s, c):
+            if x is not None:
+                x.set_persistent_blocks(red_sms)
 
         def sdag():
             s.toSDAG()
@@ -625,7 +649,7 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
     ms = e0.elapsed_time(e1) / args.steps
     return {"value": voxels / (ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms, "wall_ms_per_step": wall,
             "h2d_bytes_per_step": int(36 * T), "d2h_bytes_per_step": int(d2h),
-            "pipelined": not args.no_pipeline,
+            "pipelined": not args.no_pipeline, "reduction_sms": red_sms,
             "path": "C ABI: svdag_upload_triangles from pinned host memory, build, svdag_download_level of every "
                     "level of the SSVDAG and the CSVDAG into pinned host buffers; a step's upload and "
                     "voxelization overlap the previous step's reductions and read-back"}

@@ -84,6 +84,16 @@ const char* svdag_last_error(const svdag_ctx* ctx);
 const char* svdag_status_string(int status);
 int svdag_synchronize(svdag_ctx* ctx);
 
+/* The reductions (toDAG, toSDAG, mergeAcrossAllLevels) each run as one
+ * persistent cooperative kernel of at most one block per SM; a cooperative
+ * launch starts only when its whole grid fits, so a full-GPU reduction waits
+ * for (and then excludes) other work on the GPU.  This caps the context's
+ * reduction grids at `blocks` SMs (0 = no cap, the default), leaving the
+ * other SMs to work on other streams -- e.g. the next scene's voxelization
+ * while this one's SSVDAG and CSVDAG reductions run.  Clones inherit it.
+ * (No reference counterpart: a GPU scheduling knob.) */
+int svdag_set_persistent_blocks(svdag_ctx* ctx, unsigned blocks);
+
 /* Scene input: triangles as float[9] each (v0 v1 v2, xyz), the layout of
  * Scene::getTrianglePtr (src/symvox/scene.hpp:90).  upload copies from host
  * memory; set_device borrows a device buffer that must outlive the build. */

@@ -197,11 +197,16 @@ int svdag_clone_on(const svdag_ctx* src, void* stream, svdag_ctx** out) {
     c.child_levels_init = s.child_levels_init;
     std::memcpy(c.bbox, s.bbox, sizeof(c.bbox));
     c.root_side = s.root_side;
+    c.ex.persistent_blocks = s.ex.persistent_blocks;
     c.st = s.st;
     c.lev.resize(s.lev.size());
     for (size_t l = 0; l < s.lev.size(); ++l) copy_level(s, c.lev[l], s.lev[l], c.stream);
     SVDAG_CUDA(cudaStreamSynchronize(c.stream));
   });
+}
+
+int svdag_set_persistent_blocks(svdag_ctx* h, unsigned blocks) {
+  return guarded(h, [&](Ctx& c) { c.ex.persistent_blocks = blocks; });
 }
 
 int svdag_synchronize(svdag_ctx* h) {

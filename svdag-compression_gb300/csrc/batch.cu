@@ -695,6 +695,9 @@ void batch_reduce(Batch& B, bool sdag, bool csv) {
           X.ex.stream = streams[w];
           X.ex.launches = &B.worker_launches[w];
           X.ex.prof = nullptr;
+          // W streams run persistent toSDAG / merge kernels side by side:
+          // each grid takes at most its share of the SMs (one block per SM)
+          X.ex.persistent_blocks = std::max(1u, unsigned(B.ex.sm_count / W));
           X.levels = S.levels;
           X.state = S.state;
           X.st = S.st;

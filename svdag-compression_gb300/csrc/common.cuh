@@ -59,6 +59,7 @@ struct Exec {
   int sm_count = 152;
   uint64_t* launches = nullptr;  // incremented once per kernel launch
   Profiler* prof = nullptr;      // non-null while kernel timing is enabled
+  unsigned persistent_blocks = 0;  // cap on a persistent kernel's grid (0 = one block per SM)
 };
 
 // Grid for a grid-stride loop over n items.
@@ -150,6 +151,13 @@ __device__ __forceinline__ uint64_t hash_key9(uint32_t hdr, const uint32_t ch[8]
 __device__ __forceinline__ void load_children(const uint32_t* ch, uint64_t i, uint32_t out[8]) {
   const uint4* p = reinterpret_cast<const uint4*>(ch + 8 * i);
   uint4 a = p[0], b = p[1];
+  out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
+  out[4] = b.x; out[5] = b.y; out[6] = b.z; out[7] = b.w;
+}
+// The same through L2 only (data written by other blocks of the running kernel).
+__device__ __forceinline__ void load_children_cg(const uint32_t* ch, uint64_t i, uint32_t out[8]) {
+  const uint4* p = reinterpret_cast<const uint4*>(ch + 8 * i);
+  const uint4 a = __ldcg(p), b = __ldcg(p + 1);
   out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
   out[4] = b.x; out[5] = b.y; out[6] = b.z; out[7] = b.w;
 }

@@ -1,5 +1,8 @@
 // Open-addressing hash table of node keys shared by the DAG, SDAG and
-// CSVDAG reductions.  A key is (hdr word, 8 child words) read from
+// CSVDAG reductions.  Keys never change while a table is built or read, so
+// they are plain (L1-cached) loads; inserts read slots through L2 (__ldcg),
+// as other threads fill them concurrently; lookups run after all inserts and
+// read them plainly.  A key is (hdr word, 8 child words) read from
 // structure-of-arrays level buffers; a slot packs (hash tag << 32 | index).
 // Equal keys converge on their minimum index (atomicMin), so after all
 // inserts every slot holds its key's first occurrence.
@@ -40,6 +43,17 @@ struct Table {
   uint64_t mask;  // size - 1 (power of two)
 };
 
+// Slots are probed linearly, an aligned pair per 16-byte load (tables have
+// at least 32 slots, a power of two, so pairs never wrap).
+constexpr int kGroup = 2;
+template <bool kL2>
+__device__ __forceinline__ void load_group(const unsigned long long* slots, uint64_t g, unsigned long long w[kGroup]) {
+  const ulonglong2* p = reinterpret_cast<const ulonglong2*>(slots + g);
+  const ulonglong2 x = kL2 ? __ldcg(p) : *p;
+  w[0] = x.x;
+  w[1] = x.y;
+}
+
 // Insert node i's key; equal keys keep the minimum index.  Returns the slot.
 __device__ uint64_t table_insert(Table T, const uint32_t* hdr, const uint32_t* ch, uint32_t i, uint32_t h,
                                  const uint32_t c[8], int* err) {
@@ -47,21 +61,32 @@ __device__ uint64_t table_insert(Table T, const uint32_t* hdr, const uint32_t* c
   const uint64_t tag = hk >> 32;
   const unsigned long long mine = (tag << 32) | i;
   uint64_t pos = hk & T.mask;
-  for (uint64_t probe = 0; probe <= T.mask; ++probe) {
-    unsigned long long cur = ld_cg64(&T.slots[pos]);
-    if (cur == kEmpty64) {
-      const unsigned long long prev = atomicCAS(&T.slots[pos], kEmpty64, mine);
-      if (prev == kEmpty64) return pos;
-      cur = prev;
-    }
-    if ((cur >> 32) == tag) {
-      const uint32_t j = uint32_t(cur);
-      if (key_equal_at(hdr, ch, j, h, c)) {
-        if (i < j) atomicMin(&T.slots[pos], mine);
-        return pos;
+  uint64_t probe = 0;
+  while (probe <= T.mask) {
+    const uint64_t g = pos & ~uint64_t(kGroup - 1);
+    unsigned long long w[kGroup];
+    load_group<true>(T.slots, g, w);
+    const int k0 = int(pos - g);
+#pragma unroll
+    for (int k = 0; k < kGroup; ++k) {  // unrolled: w stays in registers
+      if (k < k0) continue;
+      ++probe;
+      const uint64_t sp = g + uint64_t(k);
+      unsigned long long cur = w[k];
+      if (cur == kEmpty64) {
+        const unsigned long long prev = atomicCAS(&T.slots[sp], kEmpty64, mine);
+        if (prev == kEmpty64) return sp;
+        cur = prev;
+      }
+      if ((cur >> 32) == tag) {
+        const uint32_t j = uint32_t(cur);
+        if (key_equal_at(hdr, ch, j, h, c)) {
+          if (i < j) atomicMin(&T.slots[sp], mine);
+          return sp;
+        }
       }
     }
-    pos = (pos + 1) & T.mask;
+    pos = (g + kGroup) & T.mask;
   }
   atomicExch(err, 1);
   return kEmpty64;
@@ -72,14 +97,24 @@ __device__ uint32_t table_find(Table T, const uint32_t* hdr, const uint32_t* ch,
   const uint64_t hk = hash_key9(h, c);
   const uint64_t tag = hk >> 32;
   uint64_t pos = hk & T.mask;
-  for (uint64_t probe = 0; probe <= T.mask; ++probe) {
-    const unsigned long long cur = T.slots[pos];
-    if (cur == kEmpty64) return kNone;
-    if ((cur >> 32) == tag) {
-      const uint32_t j = uint32_t(cur);
-      if (key_equal_at(hdr, ch, j, h, c)) return j;
+  uint64_t probe = 0;
+  while (probe <= T.mask) {
+    const uint64_t g = pos & ~uint64_t(kGroup - 1);
+    unsigned long long w[kGroup];
+    load_group<false>(T.slots, g, w);
+    const int k0 = int(pos - g);
+#pragma unroll
+    for (int k = 0; k < kGroup; ++k) {
+      if (k < k0) continue;
+      ++probe;
+      const unsigned long long cur = w[k];
+      if (cur == kEmpty64) return kNone;
+      if ((cur >> 32) == tag) {
+        const uint32_t j = uint32_t(cur);
+        if (key_equal_at(hdr, ch, j, h, c)) return j;
+      }
     }
-    pos = (pos + 1) & T.mask;
+    pos = (g + kGroup) & T.mask;
   }
   return kNone;
 }

@@ -17,14 +17,20 @@
 // unique nodes before it, else becomes unique.  Only the first occurrence of
 // a raw key can be unique, so the candidate for variant k of node i is the
 // first occurrence of the raw key equal to that variant.  Node i is then
-// decided once every earlier-ordered candidate is decided; rounds over the
-// undecided nodes resolve the dependency chains (the lowest undecided index
-// always resolves, so rounds terminate) and give exactly the sequential
+// decided once every earlier-ordered candidate is decided: one pass in index
+// order per thread, waiting on undecided candidates (the lowest undecided
+// index never waits, so the pass advances), gives exactly the sequential
 // result.
+//
+// Each phase runs as one persistent cooperative kernel over all levels
+// (k_dag_persistent, k_sdag_persistent; barrier and launch in persist.cuh)
+// with a single read of the reduced counts at the end.  The per-level
+// toDAG kernels serve the entry point that works in caller-provided scratch.
 #include <algorithm>
 
 #include "ctx.cuh"
 #include "dedup.cuh"
+#include "persist.cuh"
 
 namespace svdag {
 namespace {
@@ -176,142 +182,377 @@ __constant__ int kVarFlip[8] = {0, 4, 2, 1, 6, 5, 3, 7};
 // correspondence mirror flags for each variant: bit0 X, bit1 Y, bit2 Z
 __constant__ uint8_t kVarAxes[8] = {0, 1, 2, 4, 3, 5, 6, 7};
 
-// Invariance bits, the 7 normalised variants and their candidates.
-__global__ void k_sdag_candidates(Table T, const uint32_t* __restrict__ hdr, const uint32_t* __restrict__ ch, uint64_t n,
-                                  const uint32_t* __restrict__ slot_of, const uint8_t* __restrict__ child_inv,
-                                  uint8_t* __restrict__ inv, uint32_t* __restrict__ cand) {
-  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
-    uint32_t h, c[8];
-    load_key(hdr, ch, i, h, c);
-    const uint32_t s = slot_of[i];
-    cand[i] = (s == kNone) ? kNone : uint32_t(T.slots[s]);
-    // invariance on X, Y, Z (geom_octree.cpp:604-606): n == n.mirror(axis)
-    uint32_t iv = 0;
-    {
-      uint32_t mh, mc[8];
-      mirror_node(h, c, 4, mh, mc); if (same_key(h, c, mh, mc)) iv |= 1u;
-      mirror_node(h, c, 2, mh, mc); if (same_key(h, c, mh, mc)) iv |= 2u;
-      mirror_node(h, c, 1, mh, mc); if (same_key(h, c, mh, mc)) iv |= 4u;
-    }
-    inv[i] = uint8_t(iv);
-    uint32_t cinv[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) cinv[k] = (child_inv && c[k] != kNull) ? child_inv[c[k]] : 0u;
-    for (int v = 1; v < 8; ++v) {
-      const int flip = kVarFlip[v];
-      uint32_t vh, vc[8];
-      mirror_node(h, c, flip, vh, vc);
-      if (child_inv) {
-        // invertInvs (geom_octree.cpp:822-831): drop the mirror bit of an axis
-        // of this variant when the child is invariant on it
-        uint32_t clrx = 0, clry = 0, clrz = 0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          if (vc[k] == kNull) continue;
-          const uint32_t ci = cinv[k ^ flip];
-          if ((flip & 4) && (ci & 1u)) clrx |= 1u << k;
-          if ((flip & 2) && (ci & 2u)) clry |= 1u << k;
-          if ((flip & 1) && (ci & 4u)) clrz |= 1u << k;
-        }
-        vh &= ~((clrx << 8) | (clry << 16) | (clrz << 24));
-      }
-      cand[uint64_t(v) * n + i] = table_find(T, hdr, ch, vh, vc);
-    }
-  }
-}
+// --- persistent forms of toDAG and toSDAG ------------------------------------
+// One cooperative launch per phase runs every level (bottom-up), the
+// sub-steps of a level separated by grid barriers; per-level scratch is
+// sized from the largest level, outputs from each level's input count
+// (a level only shrinks), and the reduced counts are read once at the end.
 
-// One resolution round over undecided nodes (see file comment).
-__global__ void k_sdag_round(const uint32_t* __restrict__ cand, uint64_t n, uint32_t* state, uint8_t* __restrict__ var,
-                             unsigned long long* undecided) {
-  unsigned long long left = 0;
-  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
-    if (ld_cg32(&state[i]) != kUndecided) continue;
-    bool stuck = false, done = false;
-    for (int k = 0; k < 8; ++k) {
-      const uint32_t cnd = cand[uint64_t(k) * n + i];
-      if (cnd == kNone || cnd >= uint32_t(i)) continue;
-      const uint32_t s = ld_cg32(&state[cnd]);
-      if (s == kUndecided) { stuck = true; break; }
-      if (s == kUnique) {
-        var[i] = uint8_t(k);
-        __stcg(&state[i], cnd);
-        done = true;
-        break;
-      }
-    }
-    if (!stuck && !done) __stcg(&state[i], kUnique);
-    if (stuck) ++left;
-  }
-  for (int o = 16; o; o >>= 1) left += __shfl_down_sync(0xFFFFFFFFu, left, o);
-  if ((threadIdx.x & 31) == 0 && left) atomicAdd(undecided, left);
-}
+constexpr unsigned kResolveSpinLimit = 1u << 16;  // polls of one wait in the resolution pass
 
-// Sequential fallback for long dependency chains: one thread, index order.
-__global__ void k_sdag_serial(const uint32_t* __restrict__ cand, uint64_t n, uint32_t* state, uint8_t* var) {
-  if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  for (uint64_t i = 0; i < n; ++i) {
-    if (state[i] != kUndecided) continue;
-    bool done = false;
-    for (int k = 0; k < 8 && !done; ++k) {
-      const uint32_t cnd = cand[uint64_t(k) * n + i];
-      if (cnd == kNone || cnd >= uint32_t(i)) continue;
-      if (state[cnd] == kUnique) { var[i] = uint8_t(k); state[i] = cnd; done = true; }
-    }
-    if (!done) state[i] = kUnique;
-  }
-}
-
-struct UniqueFlagIn {
-  const uint32_t* state;
-  __device__ __forceinline__ uint32_t operator()(uint64_t i) const { return state[i] == kUnique ? 1u : 0u; }
+struct RedLevel {
+  uint32_t* hdr;   // input level (children remapped in place by the level below)
+  uint32_t* ch;    // null on the leaf level of toSDAG
+  uint32_t* ohdr;  // reduced level, capacity n (toDAG leaf: 256)
+  uint32_t* och;
+  uint8_t* oinv;   // toSDAG: invariance bits of the reduced level
+  uint64_t n;
+  uint64_t slots;  // hash table size for this level (power of two)
 };
 
-__global__ void k_compact_sdag(const uint32_t* __restrict__ hdr, const uint32_t* __restrict__ ch, const uint8_t* __restrict__ inv,
-                               uint64_t n, const uint32_t* __restrict__ state, const uint8_t* __restrict__ var,
-                               const uint32_t* __restrict__ newid, uint32_t* __restrict__ out_hdr, uint32_t* __restrict__ out_ch,
-                               uint8_t* __restrict__ out_inv, uint32_t* __restrict__ corr_id, uint8_t* __restrict__ corr_m) {
-  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
-    const uint32_t s = state[i];
-    if (s == kUnique) {
-      const uint32_t id = newid[i];
-      corr_id[i] = id;
-      corr_m[i] = 0;
-      out_hdr[id] = hdr[i];
-      out_inv[id] = inv[i];
-      if (ch) {
-        uint32_t c[8];
-        load_children(ch, i, c);
-        store_children(out_ch, id, c);
-      }
-    } else {
-      corr_id[i] = newid[s];
-      corr_m[i] = kVarAxes[var[i]];
-    }
+struct RedArgs {
+  RedLevel lev[kMaxRedLevels];
+  uint32_t levels;
+  unsigned long long* slots;  // hash table, sized for the largest level
+  uint32_t* slot_of;          // per node of the current level
+  uint32_t* rep;              // toDAG: first occurrence of the node's key
+  uint32_t* newid;
+  uint32_t* bsum;             // per block
+  uint32_t* first;            // toDAG leaf: first occurrence per mask [256]
+  uint32_t* cand;             // toSDAG: 8 candidates per node
+  uint32_t* state;            // toSDAG: kUndecided, kUnique or the matched node
+  uint8_t* inv;               // toSDAG: invariance bits per node
+  uint8_t* var;               // toSDAG: variant of the match
+  unsigned long long* left;   // toSDAG: nodes whose resolution wait ran out
+  uint32_t* cnt;              // [levels] reduced counts
+  int* err;
+  GridBar* bar;
+  unsigned long long* trace;  // step trace or null
+};
+
+// Level-ordered ids of the flagged nodes of this block's share:
+// newid[i] = number of flagged nodes before i.  bsum holds every block's
+// count (written before the last barrier); the total goes to *cnt.
+template <class Flag>
+__device__ __forceinline__ void emit_ids(const RedArgs& a, uint64_t b0, uint64_t b1, Flag flag, uint32_t* cnt) {
+  uint32_t total;
+  uint32_t base = block_offset(a.bsum, &total);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *cnt = total;
+  for (uint64_t t0 = b0; t0 < b1; t0 += blockDim.x) {
+    const uint64_t i = t0 + threadIdx.x;
+    const uint32_t f = (i < b1 && flag(i)) ? 1u : 0u;
+    uint32_t tile;
+    const uint32_t pre = block_excl_scan<uint32_t>(f, &tile);
+    if (f) a.newid[i] = base + pre;
+    base += tile;
   }
 }
 
-// Parents at level lev-1: children with a pointer -> (id, mirror bits).
-__global__ void k_remap_parents_sdag(uint32_t* __restrict__ phdr, uint32_t* __restrict__ pch, uint64_t np,
-                                     const uint32_t* __restrict__ corr_id, const uint8_t* __restrict__ corr_m) {
-  for (uint64_t p = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; p < np; p += uint64_t(gridDim.x) * blockDim.x) {
-    uint32_t c[8];
-    load_children(pch, p, c);
-    uint32_t mx = 0, my = 0, mz = 0;
-    bool any = false;
+template <class Flag>
+__device__ __forceinline__ void count_share(const RedArgs& a, uint64_t b0, uint64_t b1, Flag flag) {
+  uint32_t c = 0;
+  SVDAG_BLOCK_STRIDE(i, b0, b1) c += flag(i) ? 1u : 0u;
+  c = block_sum(c);
+  if (threadIdx.x == 0) a.bsum[blockIdx.x] = c;
+}
+
+// toDAG (geom_octree.cpp:462-548): the leaf level by its 256 masks, inner
+// levels through the hash table; each level's parents are remapped before
+// the parent level is deduplicated.
+__global__ void __launch_bounds__(kDagThreads, 1) k_dag_persistent(const RedArgs a) {
+  __shared__ uint32_t sf[256], sr[256];
+  unsigned trace_pos = 0;
+  trace_mark(a.trace, trace_pos, kStEntry);
+  const uint32_t L = a.levels;  // >= 2
+  const RedLevel& leaf = a.lev[L - 1];
+  if (blockIdx.x == 0)
+    for (int m = threadIdx.x; m < 256; m += blockDim.x) a.first[m] = kNone;
+  if (L >= 3) clear_slots(a.slots, a.lev[L - 2].slots);
+  for (int m = threadIdx.x; m < 256; m += blockDim.x) sf[m] = kNone;
+  SVDAG_STEP(a, L - 1, kStPrologue);
+
+  // leaf level: first occurrence of every mask (four headers per 16-byte load)
+  {
+    const uint64_t n4 = leaf.n / 4;
+    const uint4* h4 = reinterpret_cast<const uint4*>(leaf.hdr);
+    SVDAG_GRID_STRIDE(q, n4) {
+      const uint4 w = h4[q];
+      const uint32_t hv[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      if (c[j] == kNull) continue;
-      any = true;
-      const uint32_t old = c[j];
-      const uint32_t m = corr_m[old];
-      c[j] = corr_id[old];
-      if (m & 1u) mx |= 1u << j;
-      if (m & 2u) my |= 1u << j;
-      if (m & 4u) mz |= 1u << j;
+      for (int j = 0; j < 4; ++j) {
+        const uint32_t m = hv[j] & 0xFFu, i = uint32_t(4 * q + j);
+        if (m && sf[m] > i) atomicMin(&sf[m], i);  // read first: common masks repeat
+      }
     }
-    if (!any) continue;
-    store_children(pch, p, c);
-    if (mx | my | mz) phdr[p] |= (mx << 8) | (my << 16) | (mz << 24);
+    SVDAG_GRID_STRIDE(i, leaf.n - 4 * n4) {
+      const uint32_t k = uint32_t(4 * n4 + i), m = leaf.hdr[k] & 0xFFu;
+      if (m && sf[m] > k) atomicMin(&sf[m], k);
+    }
+  }
+  __syncthreads();
+  for (int m = threadIdx.x; m < 256; m += blockDim.x)
+    if (sf[m] != kNone) atomicMin(&a.first[m], sf[m]);
+  SVDAG_STEP(a, L - 1, kStLeafFirst);
+
+  // rank of each mask by first occurrence (every block), the reduced leaf
+  // level (block 0) and the leaves' parents
+  for (int m = threadIdx.x; m < 256; m += blockDim.x) sf[m] = a.first[m];
+  __syncthreads();
+  uint32_t present = 0;
+  for (int m = threadIdx.x; m < 256; m += blockDim.x) {
+    uint32_t r;
+    if (sf[m] != kNone) {
+      r = 0;
+      for (int k = 0; k < 256; ++k) r += (sf[k] < sf[m]) ? 1u : 0u;
+      if (blockIdx.x == 0) leaf.ohdr[r] = uint32_t(m);
+      ++present;
+    } else {
+      // a pointer to an empty node (only a joined chunk root can be one) maps
+      // to 0, the reference's default correspondence (geom_octree.cpp:493-496)
+      r = (m == 0) ? 0u : kNone;
+    }
+    sr[m] = r;
+  }
+  present = block_sum(present);
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.cnt[L - 1] = present;
+  {
+    const RedLevel& P = a.lev[L - 2];
+    SVDAG_GRID_STRIDE(p, P.n) {
+      const uint32_t m = P.hdr[p] & 0xFFu;
+      if (!m) continue;
+      uint32_t c[8];
+      load_children(P.ch, p, c);
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if ((m >> j) & 1u) {
+          // an empty leaf never has a set parent bit after cleanEmptyNodes;
+          // the reference's zero-initialised correspondence is kept for it
+          const uint32_t lm = leaf.hdr[c[j]] & 0xFFu;
+          c[j] = lm ? sr[lm] : 0u;
+        }
+      store_children(P.ch, p, c);
+    }
+  }
+  SVDAG_STEP(a, L - 1, kStLeafRank);
+
+  for (uint32_t lev = L - 2; lev >= 1; --lev) {
+    const RedLevel& V = a.lev[lev];
+    const Table T{a.slots, V.slots - 1};
+    SVDAG_GRID_STRIDE(i, V.n) {
+      uint32_t h, c[8];
+      load_key(V.hdr, V.ch, i, h, c);
+      if ((h & 0xFFu) == 0) { a.slot_of[i] = kNone; continue; }  // empty nodes are skipped (geom_octree.cpp:495)
+      a.slot_of[i] = uint32_t(table_insert(T, V.hdr, V.ch, uint32_t(i), h, c, a.err));
+    }
+    SVDAG_STEP(a, lev, kStInsert);
+
+    uint64_t b0, b1;
+    block_share(V.n, b0, b1);
+    SVDAG_BLOCK_STRIDE(i, b0, b1) {
+      const uint32_t s = a.slot_of[i];
+      a.rep[i] = (s == kNone) ? kNone : uint32_t(a.slots[s]);
+    }
+    __syncthreads();
+    auto is_rep = [&](uint64_t i) { return a.rep[i] == uint32_t(i); };
+    count_share(a, b0, b1, is_rep);
+    SVDAG_STEP(a, lev, kStCount);
+
+    emit_ids(a, b0, b1, is_rep, &a.cnt[lev]);
+    if (lev >= 2) clear_slots(a.slots, a.lev[lev - 1].slots);
+    SVDAG_STEP(a, lev, kStEmit);
+
+    SVDAG_GRID_STRIDE(i, V.n) {
+      if (a.rep[i] != uint32_t(i)) continue;
+      const uint32_t id = a.newid[i];
+      V.ohdr[id] = V.hdr[i];
+      uint32_t c[8];
+      load_children(V.ch, i, c);
+      store_children(V.och, id, c);
+    }
+    const RedLevel& P = a.lev[lev - 1];
+    SVDAG_GRID_STRIDE(p, P.n) {
+      const uint32_t m = P.hdr[p] & 0xFFu;
+      if (!m) continue;
+      uint32_t c[8];
+      load_children(P.ch, p, c);
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if ((m >> j) & 1u) {
+          const uint32_t r = a.rep[c[j]];
+          c[j] = (r == kNone) ? 0u : a.newid[r];
+        }
+      store_children(P.ch, p, c);
+    }
+    SVDAG_STEP(a, lev, kStCompact);
+  }
+}
+
+// toSDAG (geom_octree.cpp:551-697): per level, candidates of the 8 mirror
+// variants, the resolution pass (see the file comment), then the unique nodes
+// in order and the parents' pointers with their mirror bits.
+__global__ void __launch_bounds__(kRedThreads, 1) k_sdag_persistent(const RedArgs a) {
+  const uint32_t L = a.levels;  // >= 2
+  unsigned trace_pos = 0;
+  trace_mark(a.trace, trace_pos, kStEntry);
+  clear_slots(a.slots, a.lev[L - 1].slots);
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.left[0] = 0;
+  SVDAG_STEP(a, L - 1, kStPrologue);
+  const uint8_t* child_inv = nullptr;
+  for (uint32_t lev = L - 1; lev >= 1; --lev) {
+    const RedLevel& V = a.lev[lev];
+    const uint64_t n = V.n;
+    const Table T{a.slots, V.slots - 1};
+    SVDAG_GRID_STRIDE(i, n) {
+      uint32_t h, c[8];
+      load_key(V.hdr, V.ch, i, h, c);
+      if ((h & 0xFFu) == 0) { a.slot_of[i] = kNone; continue; }
+      a.slot_of[i] = uint32_t(table_insert(T, V.hdr, V.ch, uint32_t(i), h, c, a.err));
+    }
+    SVDAG_STEP(a, lev, kStInsert);
+
+    // invariance bits and the candidates of the 7 normalised variants: eight
+    // lanes per node, lane v looks variant v up (v = 0: the raw key's first
+    // occurrence from the insert), so a node costs one lookup's latency;
+    // lane k loads child k's invariance bits once and the group shares them
+    {
+      const int v = threadIdx.x & 7;
+      const int g0 = int(threadIdx.x & 24);  // first lane of the group in the warp
+      const unsigned gmask = 0xFFu << g0;
+      const int flip = kVarFlip[v];
+      const uint64_t stride = (uint64_t(gridDim.x) * blockDim.x) >> 3;
+      for (uint64_t i = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 3; i < n; i += stride) {
+        uint32_t h, c[8];
+        load_key(V.hdr, V.ch, i, h, c);
+        const uint32_t mine = (child_inv && c[v] != kNull) ? uint32_t(child_inv[c[v]]) : 0u;
+        uint32_t cinv[8];  // invariance bits of the child at mirrored position k
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cinv[k] = __shfl_sync(gmask, mine, g0 | (k ^ flip));
+        if (v == 0) {
+          const uint32_t s = a.slot_of[i];
+          a.cand[i] = (s == kNone) ? kNone : uint32_t(a.slots[s]);
+          // invariance on X, Y, Z (geom_octree.cpp:604-606): n == n.mirror(axis)
+          uint32_t iv = 0;
+          uint32_t mh, mc[8];
+          mirror_node(h, c, 4, mh, mc); if (same_key(h, c, mh, mc)) iv |= 1u;
+          mirror_node(h, c, 2, mh, mc); if (same_key(h, c, mh, mc)) iv |= 2u;
+          mirror_node(h, c, 1, mh, mc); if (same_key(h, c, mh, mc)) iv |= 4u;
+          a.inv[i] = uint8_t(iv);
+          a.state[i] = kUndecided;
+          continue;
+        }
+        uint32_t vh, vc[8];
+        mirror_node(h, c, flip, vh, vc);
+        if (child_inv) {
+          // invertInvs (geom_octree.cpp:822-831): drop the mirror bit of an
+          // axis of this variant when the child is invariant on it
+          uint32_t clrx = 0, clry = 0, clrz = 0;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            if (vc[k] == kNull) continue;
+            const uint32_t ci = cinv[k];
+            if ((flip & 4) && (ci & 1u)) clrx |= 1u << k;
+            if ((flip & 2) && (ci & 2u)) clry |= 1u << k;
+            if ((flip & 1) && (ci & 4u)) clrz |= 1u << k;
+          }
+          vh &= ~((clrx << 8) | (clry << 16) | (clrz << 24));
+        }
+        a.cand[uint64_t(v) * n + i] = table_find(T, V.hdr, V.ch, vh, vc);
+      }
+    }
+    SVDAG_STEP(a, lev, kStCandidates);
+
+    // resolution in one pass: each thread takes its nodes in index order; a
+    // candidate before the node that is still undecided is waited for.  The
+    // lowest undecided node waits for nothing, so the pass always advances
+    // (all blocks are resident).  A wait that exceeds its limit leaves the
+    // node undecided and flags the level for the serial finish.
+    {
+      unsigned long long gave_up = 0;
+      SVDAG_GRID_STRIDE(i, n) {
+        bool done = false, stalled = false;
+        for (int k = 0; k < 8; ++k) {
+          const uint32_t cnd = a.cand[uint64_t(k) * n + i];
+          if (cnd == kNone || cnd >= uint32_t(i)) continue;
+          uint32_t s = ld_cg32(&a.state[cnd]);
+          for (unsigned spins = 0; s == kUndecided && spins < kResolveSpinLimit; ++spins) {
+            __nanosleep(64);
+            s = ld_cg32(&a.state[cnd]);
+          }
+          if (s == kUndecided) { stalled = true; break; }
+          if (s == kUnique) {
+            a.var[i] = uint8_t(k);
+            __stcg(&a.state[i], cnd);
+            done = true;
+            break;
+          }
+        }
+        if (stalled) { ++gave_up; continue; }
+        if (!done) __stcg(&a.state[i], kUnique);
+      }
+      gave_up = block_sum(gave_up);
+      if (threadIdx.x == 0 && gave_up) atomicAdd(&a.left[0], gave_up);
+    }
+    SVDAG_STEP(a, lev, kStRound);
+    if (a.left[0] != 0) {
+      // long dependency chains: one thread finishes in index order
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        for (uint64_t i = 0; i < n; ++i) {
+          if (a.state[i] != kUndecided) continue;
+          bool done = false;
+          for (int k = 0; k < 8 && !done; ++k) {
+            const uint32_t cnd = a.cand[uint64_t(k) * n + i];
+            if (cnd == kNone || cnd >= uint32_t(i)) continue;
+            if (ld_cg32(&a.state[cnd]) == kUnique) { a.var[i] = uint8_t(k); __stcg(&a.state[i], cnd); done = true; }
+          }
+          if (!done) __stcg(&a.state[i], kUnique);
+        }
+      }
+      SVDAG_STEP(a, lev, kStSerial);
+    }
+
+    uint64_t b0, b1;
+    block_share(n, b0, b1);
+    auto is_unique = [&](uint64_t i) { return a.state[i] == kUnique; };
+    count_share(a, b0, b1, is_unique);
+    SVDAG_STEP(a, lev, kStCount);
+
+    // every block has read the stall counter: reset it for the next level
+    emit_ids(a, b0, b1, is_unique, &a.cnt[lev]);
+    if (lev >= 2) clear_slots(a.slots, a.lev[lev - 1].slots);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.left[0] = 0;
+    SVDAG_STEP(a, lev, kStEmit);
+
+    SVDAG_GRID_STRIDE(i, n) {
+      if (a.state[i] != kUnique) continue;
+      const uint32_t id = a.newid[i];
+      V.ohdr[id] = V.hdr[i];
+      V.oinv[id] = a.inv[i];
+      if (V.ch) {
+        uint32_t c[8];
+        load_children(V.ch, i, c);
+        store_children(V.och, id, c);
+      }
+    }
+    // parents: children with a pointer -> (id, mirror bits)
+    const RedLevel& P = a.lev[lev - 1];
+    SVDAG_GRID_STRIDE(p, P.n) {
+      uint32_t c[8];
+      load_children(P.ch, p, c);
+      uint32_t mx = 0, my = 0, mz = 0;
+      bool any = false;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if (c[j] == kNull) continue;
+        any = true;
+        const uint32_t old = c[j];
+        const uint32_t s = a.state[old];
+        uint32_t m = 0;
+        if (s == kUnique) {
+          c[j] = a.newid[old];
+        } else {
+          c[j] = a.newid[s];
+          m = kVarAxes[a.var[old]];
+        }
+        if (m & 1u) mx |= 1u << j;
+        if (m & 2u) my |= 1u << j;
+        if (m & 4u) mz |= 1u << j;
+      }
+      if (!any) continue;
+      store_children(P.ch, p, c);
+      if (mx | my | mz) P.hdr[p] = P.hdr[p] | (mx << 8) | (my << 16) | (mz << 24);
+    }
+    child_inv = V.oinv;
+    SVDAG_STEP(a, lev, kStCompact);
   }
 }
 
@@ -320,53 +561,67 @@ __global__ void k_remap_parents_sdag(uint32_t* __restrict__ phdr, uint32_t* __re
 void phase_reduce_dag(Ctx& c) {
   if (c.state != SVDAG_S_SVO && c.state != SVDAG_S_DAG)
     throw Error(SVDAG_ERR_INVALID_STATE, "toDAG: the octree is not an SVO or DAG");
+  const uint32_t L = c.levels;
+  if (L > kMaxRedLevels) throw Error(SVDAG_ERR_INVALID_ARG, "toDAG: too many levels");
   const Exec& ex = c.ex;
   const cudaStream_t st = c.stream;
-  DBuf<int> d_err(1, st);
-  SVDAG_CUDA(cudaMemsetAsync(d_err.get(), 0, 4, st));
-  DBuf<uint32_t> d_cnt(1, st);
   uint64_t nnodes = 1;
-  for (uint32_t lev = c.levels - 1; lev > 0; --lev) {
-    Level& L = c.lev[lev];
-    Level& P = c.lev[lev - 1];
-    const uint64_t n = L.n;
-    if (lev == c.levels - 1) {
-      DBuf<uint32_t> first(256, st), rank(256, st);
-      fill<uint32_t>(ex, first.get(), 256, kNone);
-      DBuf<uint32_t> out_hdr(256, st);
-      if (n) SVDAG_LAUNCH(ex, k_leaf_first, grid_for(ex, n, 256, 4), 256, 0, L.hdr.get(), n, first.get());
-      SVDAG_LAUNCH(ex, k_leaf_rank, 1, 256, 0, first.get(), rank.get(), out_hdr.get(), d_cnt.get());
-      if (P.n)
-        SVDAG_LAUNCH(ex, k_remap_parents_leafrank, grid_for(ex, P.n, 256), 256, 0, P.hdr.get(), P.ch.get(), P.n,
-                     L.hdr.get(), rank.get());
-      const uint64_t d = read_scalar(ex, d_cnt.get());
-      L.hdr = std::move(out_hdr);
-      L.n = d;
-    } else {
-      DBuf<unsigned long long> tb;
-      Table T = make_table(ex, n, tb);
-      DBuf<uint32_t> slot_of(n ? n : 1, st), rep(n ? n : 1, st), newid(n ? n : 1, st), corr(n ? n : 1, st);
-      if (n) {
-        SVDAG_LAUNCH(ex, k_insert, grid_for(ex, n, 256), 256, 0, T, L.hdr.get(), L.ch.get(), n, slot_of.get(), d_err.get());
-        SVDAG_LAUNCH(ex, k_rep, grid_for(ex, n, 256), 256, 0, T, slot_of.get(), n, rep.get());
+  if (L >= 2) {
+    RedArgs a{};
+    a.levels = L;
+    uint64_t max_n = 1, max_slots = 32;
+    std::vector<DBuf<uint32_t>> ohdr(L), och(L);
+    for (uint32_t l = 0; l < L; ++l) {
+      Level& V = c.lev[l];
+      RedLevel& R = a.lev[l];
+      R.hdr = V.hdr.get();
+      R.ch = V.ch.get();
+      R.n = V.n;
+      if (l == 0) continue;
+      if (l == L - 1) {
+        ohdr[l].alloc(256, st);
+      } else {
+        if (V.n >= 0xFFFFFFF0ull) throw Error(SVDAG_ERR_OVERFLOW, "toDAG: more than 2^32 nodes in a level");
+        R.slots = table_slots(V.n);
+        max_n = std::max<uint64_t>(max_n, V.n);
+        max_slots = std::max<uint64_t>(max_slots, R.slots);
+        ohdr[l].alloc(V.n ? V.n : 1, st);
+        och[l].alloc(8 * (V.n ? V.n : 1), st);
+        R.och = och[l].get();
       }
-      tb.release();
-      slot_of.release();
-      device_exclusive_scan<uint32_t>(ex, RepFlagIn{rep.get()}, n, U32Out{newid.get()}, d_cnt.get());
-      const uint64_t d = read_scalar(ex, d_cnt.get());
-      DBuf<uint32_t> out_hdr(d ? d : 1, st), out_ch(8 * (d ? d : 1), st);
-      if (n)
-        SVDAG_LAUNCH(ex, k_compact_dag, grid_for(ex, n, 256), 256, 0, L.hdr.get(), L.ch.get(), n, rep.get(),
-                     newid.get(), out_hdr.get(), out_ch.get(), corr.get());
-      if (P.n)
-        SVDAG_LAUNCH(ex, k_remap_parents, grid_for(ex, P.n, 256), 256, 0, P.hdr.get(), P.ch.get(), P.n, corr.get());
-      L.hdr = std::move(out_hdr);
-      L.ch = std::move(out_ch);
-      L.n = d;
+      R.ohdr = ohdr[l].get();
     }
-    nnodes += L.n;
+    const unsigned grid = persistent_grid(ex, k_dag_persistent, kDagThreads, std::max<uint64_t>(max_n, c.lev[L - 1].n));
+    DBuf<unsigned long long> slots(L >= 3 ? max_slots : 1, st);
+    DBuf<uint32_t> slot_of(max_n, st), rep(max_n, st), newid(max_n, st), bsum(grid, st), first(256, st);
+    DBuf<RedCtl> ctl(1, st);
+    SVDAG_CUDA(cudaMemsetAsync(ctl.get(), 0, sizeof(RedCtl), st));
+    a.slots = slots.get();
+    a.slot_of = slot_of.get();
+    a.rep = rep.get();
+    a.newid = newid.get();
+    a.bsum = bsum.get();
+    a.first = first.get();
+    a.cnt = ctl.get()->cnt;
+    a.err = &ctl.get()->err;
+    a.bar = &ctl.get()->bar;
+    PhaseTrace trace(st);
+    a.trace = trace.ptr();
+    launch_persistent(ex, "k_dag_persistent", k_dag_persistent, grid, kDagThreads, a);
+    const RedCtl h = finish_persistent(ex, ctl.get(), "toDAG");
+    trace.report(ex, "toDAG");
+    for (uint32_t l = 1; l < L; ++l) {
+      Level& V = c.lev[l];
+      V.n = h.cnt[l];
+      V.hdr = std::move(ohdr[l]);
+      fit_buffer(V.hdr, V.n, st);
+      if (l + 1 < L) {
+        V.ch = std::move(och[l]);
+        fit_buffer(V.ch, 8 * V.n, st);
+      }
+      nnodes += V.n;
+    }
   }
-  check_err(ex, d_err.get(), "toDAG");
   c.st.n_nodes_dag = nnodes;
   c.st.n_nodes = nnodes;
   c.state = SVDAG_S_DAG;
@@ -375,69 +630,75 @@ void phase_reduce_dag(Ctx& c) {
 void phase_reduce_sdag(Ctx& c) {
   if (c.state != SVDAG_S_SVO && c.state != SVDAG_S_DAG)
     throw Error(SVDAG_ERR_INVALID_STATE, "toSDAG: the octree is not a DAG");
+  // an SVO level may hold empty nodes; toSDAG skips them like toDAG
+  if (c.state == SVDAG_S_SVO && c.levels >= 2) throw Error(SVDAG_ERR_INVALID_STATE, "toSDAG on an SVO: run toDAG first");
+  const uint32_t L = c.levels;
+  if (L > kMaxRedLevels) throw Error(SVDAG_ERR_INVALID_ARG, "toSDAG: too many levels");
   const Exec& ex = c.ex;
   const cudaStream_t st = c.stream;
-  DBuf<int> d_err(1, st);
-  SVDAG_CUDA(cudaMemsetAsync(d_err.get(), 0, 4, st));
-  DBuf<uint32_t> d_cnt(1, st);
-  DBuf<unsigned long long> d_left(1, st);
   uint64_t nnodes = 0;
-  const uint8_t* child_inv = nullptr;
-  for (uint32_t lev = c.levels - 1; lev > 0; --lev) {
-    Level& L = c.lev[lev];
-    Level& P = c.lev[lev - 1];
-    const uint64_t n = L.n;
-    if (c.state == SVDAG_S_SVO) {
-      // an SVO level may hold empty nodes; toSDAG skips them like toDAG
-      throw Error(SVDAG_ERR_INVALID_STATE, "toSDAG on an SVO: run toDAG first");
+  if (L >= 2) {
+    RedArgs a{};
+    a.levels = L;
+    uint64_t max_n = 1, max_slots = 32;
+    std::vector<DBuf<uint32_t>> ohdr(L), och(L);
+    std::vector<DBuf<uint8_t>> oinv(L);
+    for (uint32_t l = 0; l < L; ++l) {
+      Level& V = c.lev[l];
+      RedLevel& R = a.lev[l];
+      R.hdr = V.hdr.get();
+      R.ch = (l + 1 < L) ? V.ch.get() : nullptr;
+      R.n = V.n;
+      if (l == 0) continue;
+      if (V.n >= 0xFFFFFFF0ull) throw Error(SVDAG_ERR_OVERFLOW, "toSDAG: more than 2^32 nodes in a level");
+      R.slots = table_slots(V.n);
+      max_n = std::max<uint64_t>(max_n, V.n);
+      max_slots = std::max<uint64_t>(max_slots, R.slots);
+      const uint64_t cap = V.n ? V.n : 1;
+      ohdr[l].alloc(cap, st);
+      oinv[l].alloc(cap, st);
+      if (R.ch) och[l].alloc(8 * cap, st);
+      R.ohdr = ohdr[l].get();
+      R.och = och[l].get();
+      R.oinv = oinv[l].get();
     }
-    DBuf<unsigned long long> tb;
-    Table T = make_table(ex, n, tb);
-    DBuf<uint32_t> slot_of(n ? n : 1, st), cand(8 * (n ? n : 1), st), state(n ? n : 1, st), newid(n ? n : 1, st);
-    DBuf<uint8_t> inv(n ? n : 1, st), var(n ? n : 1, st);
-    const uint32_t* ch = (lev == c.levels - 1) ? nullptr : L.ch.get();
-    if (n) {
-      SVDAG_LAUNCH(ex, k_insert, grid_for(ex, n, 256), 256, 0, T, L.hdr.get(), ch, n, slot_of.get(), d_err.get());
-      SVDAG_LAUNCH(ex, k_sdag_candidates, grid_for(ex, n, 256), 256, 0, T, L.hdr.get(), ch, n, slot_of.get(),
-                   child_inv, inv.get(), cand.get());
-      fill<uint32_t>(ex, state.get(), n, kUndecided);
-      // rounds in groups of 4 between host reads (a round with nothing left
-      // is a no-op), at most 64 before the serial finish
-      int rounds = 0;
-      for (;;) {
-        for (int r = 0; r < 4; ++r) {
-          SVDAG_CUDA(cudaMemsetAsync(d_left.get(), 0, 8, st));
-          SVDAG_LAUNCH(ex, k_sdag_round, grid_for(ex, n, 256), 256, 0, cand.get(), n, state.get(), var.get(),
-                       d_left.get());
-        }
-        rounds += 4;
-        if (read_scalar(ex, d_left.get()) == 0) break;
-        if (rounds >= 64) {
-          SVDAG_LAUNCH(ex, k_sdag_serial, 1, 32, 0, cand.get(), n, state.get(), var.get());
-          break;
-        }
+    const unsigned grid = persistent_grid(ex, k_sdag_persistent, kRedThreads, max_n);
+    DBuf<unsigned long long> slots(max_slots, st), left(1, st);
+    DBuf<uint32_t> slot_of(max_n, st), cand(8 * max_n, st), state(max_n, st), newid(max_n, st), bsum(grid, st);
+    DBuf<uint8_t> inv(max_n, st), var(max_n, st);
+    DBuf<RedCtl> ctl(1, st);
+    SVDAG_CUDA(cudaMemsetAsync(ctl.get(), 0, sizeof(RedCtl), st));
+    a.slots = slots.get();
+    a.slot_of = slot_of.get();
+    a.cand = cand.get();
+    a.state = state.get();
+    a.newid = newid.get();
+    a.bsum = bsum.get();
+    a.inv = inv.get();
+    a.var = var.get();
+    a.left = left.get();
+    a.cnt = ctl.get()->cnt;
+    a.err = &ctl.get()->err;
+    a.bar = &ctl.get()->bar;
+    PhaseTrace trace(st);
+    a.trace = trace.ptr();
+    launch_persistent(ex, "k_sdag_persistent", k_sdag_persistent, grid, kRedThreads, a);
+    const RedCtl h = finish_persistent(ex, ctl.get(), "toSDAG");
+    trace.report(ex, "toSDAG");
+    for (uint32_t l = 1; l < L; ++l) {
+      Level& V = c.lev[l];
+      V.n = h.cnt[l];
+      V.hdr = std::move(ohdr[l]);
+      fit_buffer(V.hdr, V.n, st);
+      V.inv = std::move(oinv[l]);
+      fit_buffer(V.inv, V.n, st);
+      if (l + 1 < L) {
+        V.ch = std::move(och[l]);
+        fit_buffer(V.ch, 8 * V.n, st);
       }
+      nnodes += V.n;
     }
-    tb.release();
-    slot_of.release();
-    device_exclusive_scan<uint32_t>(ex, UniqueFlagIn{state.get()}, n, U32Out{newid.get()}, d_cnt.get());
-    const uint64_t s = read_scalar(ex, d_cnt.get());
-    DBuf<uint32_t> out_hdr(s ? s : 1, st), out_ch(ch ? 8 * (s ? s : 1) : 0, st), corr_id(n ? n : 1, st);
-    DBuf<uint8_t> out_inv(s ? s : 1, st), corr_m(n ? n : 1, st);
-    if (n)
-      SVDAG_LAUNCH(ex, k_compact_sdag, grid_for(ex, n, 256), 256, 0, L.hdr.get(), ch, inv.get(), n, state.get(),
-                   var.get(), newid.get(), out_hdr.get(), out_ch.get(), out_inv.get(), corr_id.get(), corr_m.get());
-    if (P.n)
-      SVDAG_LAUNCH(ex, k_remap_parents_sdag, grid_for(ex, P.n, 256), 256, 0, P.hdr.get(), P.ch.get(), P.n,
-                   corr_id.get(), corr_m.get());
-    L.hdr = std::move(out_hdr);
-    if (ch) L.ch = std::move(out_ch);
-    L.inv = std::move(out_inv);
-    L.n = s;
-    child_inv = L.inv.get();
-    nnodes += s;
   }
-  check_err(ex, d_err.get(), "toSDAG");
   c.st.n_nodes_sdag = nnodes;
   c.st.n_nodes = nnodes;
   c.state = SVDAG_S_SDAG;

@@ -61,6 +61,7 @@ GPU_SYMBOLS = {
     "svdag_last_error": (ctypes.c_char_p, [_VP]),
     "svdag_status_string": (ctypes.c_char_p, [_I]),
     "svdag_synchronize": (_I, [_VP]),
+    "svdag_set_persistent_blocks": (_I, [_VP, _U32]),
     "svdag_upload_triangles": (_I, [_VP, _VP, _U64]),
     "svdag_set_device_triangles": (_I, [_VP, _VP, _U64]),
     "svdag_voxelize": (_I, [_VP, _U32, _VP]),
@@ -479,6 +480,11 @@ class Octree:
                 hdr = np.ascontiguousarray(lev[0], np.uint32)
                 ch = np.ascontiguousarray(lev[1], np.uint32)
             self._check(self._lib.svdag_import_level(self._h, l, len(hdr), hdr.ctypes.data, ch.ctypes.data))
+
+    def set_persistent_blocks(self, blocks):
+        """Cap the reduction kernels' grids at `blocks` SMs (0 = no cap), so
+        that they share the GPU with work on other streams; clones inherit it."""
+        self._check(self._lib.svdag_set_persistent_blocks(self._h, int(blocks)))
 
     def clone(self, stream=None):
         """Device-side copy (GeomOctree's copy constructor); on `stream` (a
