@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--top-k", type=int, default=256)
     ap.add_argument("--train-pairs", type=int, default=2000000)
     ap.add_argument("--epochs", type=int, default=2)
+    ap.add_argument("--train-batch", type=int, default=4096)
+    ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--chunks", type=int, default=256)
     ap.add_argument("--max-depth", type=int, default=11)
     ap.add_argument("--grid", type=int, default=None)
@@ -891,7 +893,7 @@ def run_lossy(args, rank, local, world):
             t0 = time.perf_counter()
             l0 = o.stats()["gpu_launches"]
             st = o.lossy(kind, 3, 5, 0.01, top_k=args.top_k, train_pairs=args.train_pairs, epochs=args.epochs,
-                         seed=args.seed)
+                         seed=args.seed, train_batch=args.train_batch, lr=args.lr)
             torch.cuda.synchronize()
             times.append((time.perf_counter() - t0) * 1e3)
             st["gpu_launches"] = o.stats()["gpu_launches"] - l0
@@ -918,6 +920,7 @@ def run_lossy(args, rank, local, world):
                    "savings_vs_exact": le["nodes_saved"] / max(1, ex["nodes_saved"]),
                    "throughput_vs_exact": (le["merged"] / le["wall_ms"]) / max(1e-9, ex["merged"] / ex["wall_ms"]),
                    "top_k": args.top_k, "train_pairs": args.train_pairs, "epochs": args.epochs,
+                   "train_batch": args.train_batch, "lr": args.lr,
                    "parallelism": "single GPU"},
         "gpu_launches": int(le["gpu_launches"]), "e2e": None,
     }

@@ -22,7 +22,10 @@
 // launch per step covers every chunk of a height.  The DAGs then go through
 // toSDAG and the cross-level merge per chunk, on several streams at once.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <condition_variable>
+#include <functional>
 #include <mutex>
 #include <new>
 #include <thread>
@@ -643,102 +646,154 @@ void batch_build_dags(Batch& B) {
   B.results.resize(N);
   std::vector<uint32_t> sel;
   uint64_t cells = 0;
+  auto flush = [&]() {
+    if (sel.empty()) return;
+    build_wave(B, sel);
+    sel.clear();
+    cells = 0;
+  };
   for (uint32_t c = 0; c < N; ++c) {
     const uint64_t k = 1ull << (3 * (B.chunks[c].depth - 2));
-    if (!sel.empty() && cells + k > (1ull << 30)) {
-      build_wave(B, sel);
-      sel.clear();
-      cells = 0;
-    }
+    if (!sel.empty() && cells + k > (1ull << 30)) flush();
     sel.push_back(c);
     cells += k;
   }
-  build_wave(B, sel);
+  flush();
 }
+
+namespace {
+
+// Chunks for the SSVDAG / CSVDAG reduction workers.
+struct ReduceQueue {
+  std::mutex mu;
+  std::condition_variable cv;
+  std::vector<uint32_t> items;
+  size_t next = 0;
+  bool closed = false;
+  int err_code = SVDAG_OK;
+  std::string err;
+  std::atomic<unsigned> cap{1};  // SMs per reduction grid
+  void push(const std::vector<uint32_t>& sel) {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      items.insert(items.end(), sel.begin(), sel.end());
+    }
+    cv.notify_all();
+  }
+  void close() {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      closed = true;
+    }
+    cv.notify_all();
+  }
+  void fail(int code, const std::string& what) {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      if (err_code == SVDAG_OK) { err_code = code; err = what; }
+    }
+    cv.notify_all();
+  }
+  // next ready chunk; false once the queue is closed and drained, or failed
+  bool pop(uint32_t& c) {
+    std::unique_lock<std::mutex> lk(mu);
+    cv.wait(lk, [&] { return next < items.size() || closed || err_code != SVDAG_OK; });
+    if (err_code != SVDAG_OK || next >= items.size()) return false;
+    c = items[next++];
+    return true;
+  }
+};
+
+// One worker: clones of each ready chunk's DAG on its own stream, reduced
+// with grids of at most q.cap SMs.
+void reduce_worker(Batch& B, ReduceQueue& q, int w, bool sdag, bool csv) {
+  const cudaStream_t sw = B.streams[w];
+  try {
+    SVDAG_CUDA(cudaSetDevice(B.device));
+    uint32_t c;
+    while (q.pop(c)) {
+      BatchResult& R = B.results[c];
+      auto clone_of = [&](const svdag_ctx* src) {
+        std::unique_ptr<svdag_ctx> o(new svdag_ctx());
+        Ctx& X = o->c;
+        const Ctx& S = src->c;
+        X.device = S.device;
+        X.stream = sw;
+        X.ex = B.ex;
+        X.ex.stream = sw;
+        X.ex.launches = &B.worker_launches[w];
+        X.ex.prof = nullptr;
+        X.ex.persistent_blocks = q.cap.load();
+        X.levels = S.levels;
+        X.state = S.state;
+        X.st = S.st;
+        X.lev.resize(S.lev.size());
+        for (size_t l = 0; l < S.lev.size(); ++l) {
+          const Level& a = S.lev[l];
+          Level& b = X.lev[l];
+          b.n = a.n;
+          b.hdr.alloc(a.n ? a.n : 1, sw);
+          if (a.n) SVDAG_CUDA(cudaMemcpyAsync(b.hdr.get(), a.hdr.get(), 4 * a.n, cudaMemcpyDeviceToDevice, sw));
+          if (a.ch.get()) {
+            b.ch.alloc(8 * (a.n ? a.n : 1), sw);
+            if (a.n) SVDAG_CUDA(cudaMemcpyAsync(b.ch.get(), a.ch.get(), 32 * a.n, cudaMemcpyDeviceToDevice, sw));
+          }
+        }
+        return o;
+      };
+      if (sdag) {
+        R.sdag = clone_of(R.dag.get());
+        phase_reduce_sdag(R.sdag->c);
+      }
+      if (csv && R.dag->c.levels >= 2) {
+        R.csv = clone_of(R.dag.get());
+        R.csv->c.child_levels_init = true;  // initChildLevels before the merge, as svbuilder does
+        phase_cross_level_merge(R.csv->c);
+      }
+      SVDAG_CUDA(cudaStreamSynchronize(sw));
+    }
+  } catch (const Error& e) {
+    q.fail(e.code, e.what());
+  } catch (const std::bad_alloc&) {
+    q.fail(SVDAG_ERR_OOM, "host allocation failed");
+  }
+}
+
+// Worker streams live as long as the batch: the results' buffers are
+// stream-ordered allocations on them.
+int reduce_streams(Batch& B, uint32_t n_chunks) {
+  const int W = std::max(1, std::min<int>(B.tuning.streams, int(std::max<uint32_t>(n_chunks, 1))));
+  while (int(B.streams.size()) < W) {
+    cudaStream_t s;
+    SVDAG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    B.streams.push_back(s);
+  }
+  B.worker_launches.assign(W, 0);
+  return W;
+}
+
+}  // namespace
 
 // SSVDAG and CSVDAG of every chunk's DAG, on B.tuning.streams streams.
 void batch_reduce(Batch& B, bool sdag, bool csv) {
   const uint32_t N = uint32_t(B.results.size());
   if (!N || (!sdag && !csv)) return;
   SVDAG_CUDA(cudaStreamSynchronize(B.stream));
-  const int W = std::max(1, std::min<int>(B.tuning.streams, int(N)));
-  // worker streams live as long as the batch: the results' buffers are
-  // stream-ordered allocations on them
-  while (int(B.streams.size()) < W) {
-    cudaStream_t s;
-    SVDAG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    B.streams.push_back(s);
-  }
-  const std::vector<cudaStream_t>& streams = B.streams;
-  std::mutex mu;
-  uint32_t next = 0;
-  std::string err;
-  int err_code = SVDAG_OK;
-  auto work = [&](int w) {
-    try {
-      SVDAG_CUDA(cudaSetDevice(B.device));
-      for (;;) {
-        uint32_t c;
-        {
-          std::lock_guard<std::mutex> lk(mu);
-          if (next >= N || err_code != SVDAG_OK) return;
-          c = next++;
-        }
-        BatchResult& R = B.results[c];
-        auto clone_of = [&](const svdag_ctx* src) {
-          std::unique_ptr<svdag_ctx> o(new svdag_ctx());
-          Ctx& X = o->c;
-          const Ctx& S = src->c;
-          X.device = S.device;
-          X.stream = streams[w];
-          X.ex = B.ex;
-          X.ex.stream = streams[w];
-          X.ex.launches = &B.worker_launches[w];
-          X.ex.prof = nullptr;
-          // W streams run persistent toSDAG / merge kernels side by side:
-          // each grid takes at most its share of the SMs (one block per SM)
-          X.ex.persistent_blocks = std::max(1u, unsigned(B.ex.sm_count / W));
-          X.levels = S.levels;
-          X.state = S.state;
-          X.st = S.st;
-          X.lev.resize(S.lev.size());
-          for (size_t l = 0; l < S.lev.size(); ++l) {
-            const Level& a = S.lev[l];
-            Level& b = X.lev[l];
-            b.n = a.n;
-            b.hdr.alloc(a.n ? a.n : 1, streams[w]);
-            if (a.n) SVDAG_CUDA(cudaMemcpyAsync(b.hdr.get(), a.hdr.get(), 4 * a.n, cudaMemcpyDeviceToDevice, streams[w]));
-            if (a.ch.get()) {
-              b.ch.alloc(8 * (a.n ? a.n : 1), streams[w]);
-              if (a.n)
-                SVDAG_CUDA(cudaMemcpyAsync(b.ch.get(), a.ch.get(), 32 * a.n, cudaMemcpyDeviceToDevice, streams[w]));
-            }
-          }
-          return o;
-        };
-        if (sdag) {
-          R.sdag = clone_of(R.dag.get());
-          phase_reduce_sdag(R.sdag->c);
-        }
-        if (csv && R.dag->c.levels >= 2) {
-          R.csv = clone_of(R.dag.get());
-          R.csv->c.child_levels_init = true;  // initChildLevels before the merge, as svbuilder does
-          phase_cross_level_merge(R.csv->c);
-        }
-        SVDAG_CUDA(cudaStreamSynchronize(streams[w]));
-      }
-    } catch (const Error& e) {
-      std::lock_guard<std::mutex> lk(mu);
-      if (err_code == SVDAG_OK) { err_code = e.code; err = e.what(); }
-    }
-  };
-  B.worker_launches.assign(W, 0);
+  const int W = reduce_streams(B, N);
+  ReduceQueue q;
+  std::vector<uint32_t> all(N);
+  for (uint32_t c = 0; c < N; ++c) all[c] = c;
+  q.push(all);
+  q.close();
+  // W streams run persistent toSDAG / merge kernels side by side: each grid
+  // takes at most its share of the SMs (one block per SM)
+  q.cap = std::max(1u, unsigned(B.ex.sm_count / W));
   std::vector<std::thread> th;
-  for (int w = 1; w < W; ++w) th.emplace_back(work, w);
-  work(0);
+  for (int w = 1; w < W; ++w) th.emplace_back(reduce_worker, std::ref(B), std::ref(q), w, sdag, csv);
+  reduce_worker(B, q, 0, sdag, csv);
   for (auto& t : th) t.join();
   for (auto v : B.worker_launches) B.launches += v;
-  if (err_code != SVDAG_OK) throw Error(err_code, err);
+  if (q.err_code != SVDAG_OK) throw Error(q.err_code, q.err);
 }
 
 }  // namespace svdag
@@ -774,6 +829,10 @@ double wall_ms(const std::chrono::steady_clock::time_point& t0) {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
+// The two stages one after the other: overlapping them (each wave's chunks
+// reduced while the next wave builds, the SMs split between the two) was
+// slower on GB300 -- 1364 against 1080 ms for the 256-chunk benchmark --
+// as the DAG waves slowed from 555 to 1298 ms next to the reductions.
 void run_batch(Batch& B, uint32_t flags) {
   const auto t0 = std::chrono::steady_clock::now();
   svdag::batch_build_dags(B);

@@ -63,7 +63,8 @@ struct CsvArgs {
   uint32_t* prefix;
   uint32_t* newidx;
   uint32_t* bsum;
-  uint8_t* in_check;
+  uint32_t* check_bits;       // check set over the global indices
+  uint32_t smem_words;        // words of the shared-memory bitmap
   unsigned long long* path;
   unsigned long long* best;
   unsigned long long* missing;
@@ -96,6 +97,7 @@ __device__ __forceinline__ uint32_t eff_of(const CsvArgs& a, uint32_t g) {
 
 __global__ void __launch_bounds__(kRedThreads, 1) k_csv_persistent(const CsvArgs a) {
   __shared__ uint32_t sf[256];
+  extern __shared__ uint32_t s_bits[];  // a.smem_words words
   const uint32_t L = a.L, N = a.N;
   unsigned trace_pos = 0;
   trace_mark(a.trace, trace_pos, kStEntry);
@@ -105,7 +107,16 @@ __global__ void __launch_bounds__(kRedThreads, 1) k_csv_persistent(const CsvArgs
     a.own[g] = kNone;
     a.owner[g] = kNone;
     a.best[g] = 0ull;
-    a.in_check[g] = (L >= 2 && g >= a.off[1] && g < a.off[2 < L ? 2 : L]) ? 1 : 0;
+  }
+  {
+    // check set: level 1
+    const uint32_t lo = L >= 2 ? a.off[1] : 0, hi = L >= 2 ? a.off[2] : 0;
+    SVDAG_GRID_STRIDE(w, uint64_t((N + 31) >> 5)) {
+      const uint32_t b0 = uint32_t(w) << 5;
+      uint32_t v = 0;
+      for (uint32_t k = 0; k < 32; ++k) v |= uint32_t(b0 + k >= lo && b0 + k < hi) << k;
+      a.check_bits[w] = v;
+    }
   }
   if (blockIdx.x == 0) {
     for (int m = threadIdx.x; m < 256; m += blockDim.x) a.first[m] = kNone;
@@ -187,26 +198,48 @@ __global__ void __launch_bounds__(kRedThreads, 1) k_csv_persistent(const CsvArgs
 
   // ---- check set, top-down from level 1 (geom_octree_extension.cpp:1331-1407):
   // matched nodes record their match; unmatched ones put their children into
-  // the next level's set
+  // the next level's set.  The set is a bitmap over the global indices.  A
+  // block first marks the children in a shared-memory copy of the child
+  // level's words (when it fits), then ORs its non-zero words into the
+  // bitmap: children are shared by many parents, and per-child global
+  // stores would pile onto the same few L2 sectors.
   for (uint32_t l = 1; l < L; ++l) {
     const uint32_t g0 = a.off[l], n = a.off[l + 1] - g0;
     if (n == 0) continue;
+    const uint32_t c0 = (l + 1 < L) ? a.off[l + 1] : 0, cn = (l + 1 < L) ? a.off[l + 2] - c0 : 0;
+    const uint32_t w0 = c0 >> 5, words = cn ? ((c0 + cn + 31) >> 5) - w0 : 0;
+    const bool local = cn && words <= a.smem_words;
+    if (local) {
+      for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) s_bits[w] = 0;
+      __syncthreads();
+    }
     SVDAG_GRID_STRIDE(i, uint64_t(n)) {
       const uint32_t g = g0 + uint32_t(i);
-      if (!a.in_check[g]) continue;
+      if (!((a.check_bits[g >> 5] >> (g & 31)) & 1u)) continue;
       const uint32_t cd = a.cand[g];
       if (cd != kNone) { a.own[g] = cd; continue; }
-      if (l + 1 >= L) continue;
+      if (!cn) continue;
       const uint32_t m = a.hdr[l][i] & 0xFFu;
       uint32_t c[8];
       load_children(a.ch[l], i, c);
-      const uint32_t base = a.off[l + 1];
-      // shared children are reached from many parents: write only a byte
-      // that does not hold the mark yet (a stale 0 from L1 only repeats a
-      // store; marks never clear)
 #pragma unroll
-      for (int j = 0; j < 8; ++j)
-        if (((m >> j) & 1u) && !a.in_check[base + c[j]]) a.in_check[base + c[j]] = 1;
+      for (int j = 0; j < 8; ++j) {
+        if (!((m >> j) & 1u)) continue;
+        const uint32_t x = c0 + c[j];
+        if (local) {
+          atomicOr(&s_bits[(x >> 5) - w0], 1u << (x & 31));
+        } else if (!((a.check_bits[x >> 5] >> (x & 31)) & 1u)) {
+          // a stale 0 from L1 only repeats the atomic; marks never clear
+          atomicOr(&a.check_bits[x >> 5], 1u << (x & 31));
+        }
+      }
+    }
+    if (local) {
+      __syncthreads();
+      for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) {
+        const uint32_t v = s_bits[w];
+        if (v && (a.check_bits[w0 + w] & v) != v) atomicOr(&a.check_bits[w0 + w], v);
+      }
     }
     SVDAG_STEP(a, l, kStCheck);
   }
@@ -387,12 +420,18 @@ void phase_cross_level_merge(Ctx& c) {
   // the largest class-id domain is levels 1..L-2 (height 1)
   const uint64_t dom = (L >= 3) ? uint64_t(a.off[L - 1]) - a.off[1] : 0;
   const uint64_t Nn = N ? N : 1, dn = dom ? dom : 1;
-  const unsigned grid = persistent_grid(ex, k_csv_persistent, kRedThreads, Nn);
+  // shared-memory bitmap: the largest child level's words, up to 160 KB
+  uint32_t smem_words = 0;
+  for (uint32_t l = 2; l < L; ++l)
+    smem_words = std::max<uint32_t>(smem_words, ((a.off[l + 1] + 31) >> 5) - (a.off[l] >> 5));
+  smem_words = std::min<uint32_t>(smem_words, 40960);
+  a.smem_words = smem_words;
+  const unsigned grid = persistent_grid(ex, k_csv_persistent, kRedThreads, Nn, 4 * smem_words);
   DBuf<unsigned long long> slots(table_slots(dn), st), path(Nn, st), best(Nn, st), missing(1, st);
   DBuf<uint32_t> tid_a(Nn, st), tid_b(Nn, st), khdr(dn, st), kch(8 * dn, st), slot_of(dn, st), first(256, st),
       cand(Nn, st), own(Nn, st), owner(Nn, st), bdesc(Nn, st), corr(Nn, st), prefix(Nn, st), newidx(Nn, st),
       bsum(grid, st);
-  DBuf<uint8_t> in_check(Nn, st);
+  DBuf<uint32_t> check_bits((Nn + 31) / 32, st);
   DBuf<RedCtl> ctl(1, st);
   SVDAG_CUDA(cudaMemsetAsync(ctl.get(), 0, sizeof(RedCtl), st));
   a.slots = slots.get();
@@ -410,7 +449,7 @@ void phase_cross_level_merge(Ctx& c) {
   a.prefix = prefix.get();
   a.newidx = newidx.get();
   a.bsum = bsum.get();
-  a.in_check = in_check.get();
+  a.check_bits = check_bits.get();
   a.path = path.get();
   a.best = best.get();
   a.missing = missing.get();
@@ -419,7 +458,7 @@ void phase_cross_level_merge(Ctx& c) {
   a.bar = &ctl.get()->bar;
   PhaseTrace trace(st);
   a.trace = trace.ptr();
-  launch_persistent(ex, "k_csv_persistent", k_csv_persistent, grid, kRedThreads, a);
+  launch_persistent(ex, "k_csv_persistent", k_csv_persistent, grid, kRedThreads, 4 * smem_words, a);
   uint64_t n_missing = 0;
   SVDAG_CUDA(cudaMemcpyAsync(&n_missing, missing.get(), 8, cudaMemcpyDeviceToHost, st));
   const RedCtl h = finish_persistent(ex, ctl.get(), "mergeAcrossAllLevels");

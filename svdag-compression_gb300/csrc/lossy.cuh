@@ -13,6 +13,8 @@ struct LossyConfig {
   uint64_t train_pairs = 2000000;
   uint32_t epochs = 2;
   uint64_t seed = 1;
+  uint32_t train_batch = 4096;  // learned: pairs per training step
+  float lr = 1e-3f;             // learned: Adam learning rate
 };
 
 struct LossyResult {

@@ -34,15 +34,6 @@ namespace svdag {
 namespace {
 
 constexpr int kIn = 512, kH = 256, kOut = 64;
-// training: pairs per batch (rows = 2x), Adam learning rate
-#ifndef SVDAG_MLP_BATCH
-#define SVDAG_MLP_BATCH 4096
-#endif
-#ifndef SVDAG_MLP_LR
-#define SVDAG_MLP_LR 1e-3f
-#endif
-constexpr int kTrainBatch = SVDAG_MLP_BATCH;
-constexpr float kTrainLr = SVDAG_MLP_LR;
 
 // ---------------------------------------------------------------------------
 // Tensor-core GEMM on fp16 operands.  C[M x N] = op(A)[M x K] * op(B)[K x N]
@@ -765,7 +756,7 @@ struct LearnedProposer : LossyProposer {
 
   // Training pairs: half within the bands (near pairs), half uniform, drawn
   // on the device (k_sample_pairs), rounded up to whole batches of
-  // kTrainBatch pairs; their exact targets (k_pair_target).  One training
+  // cfg.train_batch pairs; their exact targets (k_pair_target).  One training
   // step -- batch setup, forward, loss, backward with the fused bias and
   // ReLU gradients (the weight gradients on a parallel branch), Adam, step
   // counter -- is captured once as a CUDA graph and replayed for every batch
@@ -776,7 +767,7 @@ struct LearnedProposer : LossyProposer {
     const Exec& ex = c.ex;
     const cudaStream_t st = c.stream;
     const uint32_t n = S.n;
-    const int B = kTrainBatch;
+    const int B = int(cfg.train_batch);
     const uint64_t batches = std::max<uint64_t>(1, (std::max<uint64_t>(1024, cfg.train_pairs) + B - 1) / B);
     const uint64_t np = batches * B;
     DBuf<uint2> pairs(np, st);
@@ -801,7 +792,7 @@ struct LearnedProposer : LossyProposer {
                    rows.get(), work.t.get());
       mlp_loss_grad(gx, net, work, X.get(), rows.get(), B, &side);
       SVDAG_LAUNCH(gx, k_adam_dev, grid_for(gx, Mlp::total(), 256), 256, 0, net.w.get(), net.wh.get(), net.g.get(),
-                   net.m.get(), net.v.get(), Mlp::total(), kTrainLr, 0.9f, 0.999f, counter.get());
+                   net.m.get(), net.v.get(), Mlp::total(), cfg.lr, 0.9f, 0.999f, counter.get());
       SVDAG_LAUNCH(gx, k_step_advance, 1, 1, 0, counter.get());
     } catch (...) {
       cudaStreamEndCapture(st, &graph);
@@ -977,7 +968,12 @@ extern "C" int svdag_lossy_dag(svdag_ctx* h, const svdag_lossy_params* p, svdag_
     cfg.train_pairs = p->train_pairs ? p->train_pairs : 2000000;
     cfg.epochs = p->train_epochs ? p->train_epochs : 2;
     cfg.seed = p->seed;
+    cfg.train_batch = p->train_batch ? p->train_batch : 4096;
+    cfg.lr = p->train_lr > 0.f ? p->train_lr : 1e-3f;
     if (cfg.top_k > 512) throw svdag::Error(SVDAG_ERR_INVALID_ARG, "lossy: top_k above 512");
+    if (cfg.train_batch % 64 || cfg.train_batch < 256 || cfg.train_batch > 65536)
+      throw svdag::Error(SVDAG_ERR_INVALID_ARG, "lossy: train_batch must be a multiple of 64 in [256, 65536]");
+    if (!(cfg.lr < 1.f)) throw svdag::Error(SVDAG_ERR_INVALID_ARG, "lossy: train_lr must be below 1");
     svdag::LossyResult r;
     svdag::lossy_run(c, cfg, int(p->proposer), r);
     if (out) {

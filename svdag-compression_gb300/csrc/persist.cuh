@@ -140,10 +140,11 @@ struct NoDeduce {
 };
 
 // Cooperative launch of a persistent kernel with `grid` blocks of `threads`
-// threads, counted and (when profiling) timed like SVDAG_LAUNCH.
+// threads and `smem` bytes of dynamic shared memory, counted and (when
+// profiling) timed like SVDAG_LAUNCH.
 template <class... KArgs>
 void launch_persistent(const Exec& ex, const char* name, void (*kern)(KArgs...), unsigned grid, unsigned threads,
-                       typename NoDeduce<KArgs>::type... args) {
+                       size_t smem, typename NoDeduce<KArgs>::type... args) {
   void* params[] = {(void*)&args...};
   cudaEvent_t a = nullptr, b = nullptr;
   if (ex.prof) {
@@ -151,7 +152,7 @@ void launch_persistent(const Exec& ex, const char* name, void (*kern)(KArgs...),
     b = ex.prof->get();
     SVDAG_CUDA(cudaEventRecord(a, ex.stream));
   }
-  SVDAG_CUDA(cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(threads), params, 0, ex.stream));
+  SVDAG_CUDA(cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(threads), params, smem, ex.stream));
   if (ex.launches) ++*ex.launches;
   if (ex.prof) {
     SVDAG_CUDA(cudaEventRecord(b, ex.stream));
@@ -160,20 +161,23 @@ void launch_persistent(const Exec& ex, const char* name, void (*kern)(KArgs...),
 }
 
 // Blocks for a persistent kernel of `threads` threads per block over at most
-// `work` items per pass: no more than the work needs (four items per thread),
+// `work` items per pass: no more than the work needs (an item per thread: the
+// passes are latency-bound gathers),
 // one per SM at most, and at most ex.persistent_blocks when the caller runs
 // several persistent phases side by side.  A block of 1024 threads at <= 64
 // registers fills an SM; a cooperative launch starts only when all of its
 // blocks can be resident, so persistent kernels on different streams that
 // do not fit together run one after the other rather than deadlock.
 template <class K>
-unsigned persistent_grid(const Exec& ex, K kern, unsigned threads, uint64_t work) {
+unsigned persistent_grid(const Exec& ex, K kern, unsigned threads, uint64_t work, size_t smem = 0) {
+  if (smem > 48 * 1024)
+    SVDAG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   int per_sm = 0;
-  SVDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, int(threads), 0));
+  SVDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, int(threads), smem));
   if (per_sm < 1) throw Error(SVDAG_ERR_CUDA, "persistent kernel cannot be resident");
   uint64_t cap = uint64_t(ex.sm_count);
   if (ex.persistent_blocks) cap = std::min<uint64_t>(cap, ex.persistent_blocks);
-  const uint64_t want = std::max<uint64_t>(1, (work + 4ull * threads - 1) / (4ull * threads));
+  const uint64_t want = std::max<uint64_t>(1, (work + threads - 1) / threads);
   return unsigned(std::min<uint64_t>(want, cap));
 }
 

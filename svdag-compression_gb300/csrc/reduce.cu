@@ -607,7 +607,7 @@ void phase_reduce_dag(Ctx& c) {
     a.bar = &ctl.get()->bar;
     PhaseTrace trace(st);
     a.trace = trace.ptr();
-    launch_persistent(ex, "k_dag_persistent", k_dag_persistent, grid, kDagThreads, a);
+    launch_persistent(ex, "k_dag_persistent", k_dag_persistent, grid, kDagThreads, 0, a);
     const RedCtl h = finish_persistent(ex, ctl.get(), "toDAG");
     trace.report(ex, "toDAG");
     for (uint32_t l = 1; l < L; ++l) {
@@ -682,7 +682,7 @@ void phase_reduce_sdag(Ctx& c) {
     a.bar = &ctl.get()->bar;
     PhaseTrace trace(st);
     a.trace = trace.ptr();
-    launch_persistent(ex, "k_sdag_persistent", k_sdag_persistent, grid, kRedThreads, a);
+    launch_persistent(ex, "k_sdag_persistent", k_sdag_persistent, grid, kRedThreads, 0, a);
     const RedCtl h = finish_persistent(ex, ctl.get(), "toSDAG");
     trace.report(ex, "toSDAG");
     for (uint32_t l = 1; l < L; ++l) {

@@ -121,7 +121,8 @@ GPU_SYMBOLS = {
 class LossyParams(ctypes.Structure):
     _fields_ = [("levels_above_min", ctypes.c_uint32), ("levels_above_max", ctypes.c_uint32),
                 ("max_error", ctypes.c_double), ("proposer", ctypes.c_uint32), ("top_k", ctypes.c_uint32),
-                ("train_pairs", ctypes.c_uint64), ("train_epochs", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
+                ("train_pairs", ctypes.c_uint64), ("train_epochs", ctypes.c_uint32), ("seed", ctypes.c_uint64),
+                ("train_batch", ctypes.c_uint32), ("train_lr", ctypes.c_float)]
 
 
 class _LossyStats(ctypes.Structure):
@@ -425,9 +426,10 @@ class Octree:
     LOSSY = {"exact": 0, "learned": 1, "untrained": 2}
 
     def lossy(self, proposer="exact", min_above=3, max_above=5, max_error=0.01, top_k=16, train_pairs=0,
-              epochs=0, seed=1):
+              epochs=0, seed=1, train_batch=0, lr=0.0):
         """Lossy LSVDAG on a DAG (svdag_lossy_dag); returns its statistics."""
-        p = LossyParams(min_above, max_above, max_error, self.LOSSY[proposer], top_k, train_pairs, epochs, seed)
+        p = LossyParams(min_above, max_above, max_error, self.LOSSY[proposer], top_k, train_pairs, epochs, seed,
+                        train_batch, lr)
         s = _LossyStats()
         self._check(self._lib.svdag_lossy_dag(self._h, ctypes.byref(p), ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in _LossyStats._fields_}
