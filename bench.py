@@ -73,7 +73,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--reduction-sms", type=int, default=None,
                     help="SMs the SSVDAG and CSVDAG reductions may take while the next step builds (pipelined "
-                         "steps; default a quarter of the GPU; 0 = all)")
+                         "steps; default a quarter of the GPU, all of it for a chunked build; 0 = all)")
     ap.add_argument("--no-pipeline", action="store_true",
                     help="terrain/city: run the timed steps one after another instead of overlapping a step's "
                          "SSVDAG / CSVDAG reductions with the next step's voxelization")
@@ -532,23 +532,28 @@ def level_info(sv, base, s_last, args):
 
 def reduction_sms(args, torch, dev):
     """SMs each of the SSVDAG and CSVDAG reductions may take while the next
-    step voxelizes (their persistent kernels start only when their whole grid
-    fits, so a full-GPU grid would wait for, then exclude, the build)."""
+    step builds (their persistent kernels start only when their whole grid
+    fits, so a full-GPU grid would wait for, then exclude, the build): a
+    quarter of the GPU beside a plain build (buildSVO + one toDAG); all of it
+    beside a chunked build (buildDAG), which itself runs a full-GPU toDAG per
+    chunk that capped reductions would only hold up (GB300, depth-15 city:
+    13,201 Mvoxels/s uncapped, 12,114 with 19 SMs each)."""
     if args.reduction_sms is not None:
         return max(0, args.reduction_sms)
+    if args.step_level:
+        return 0
     return max(1, torch.cuda.get_device_properties(dev).multi_processor_count // 4)
 
 
 def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
     """The same step through the C ABI as a host program would call it:
-    triangles copied in from pinned host memory (svdag_upload_triangles),
-    the build, and every level of both result pools (headers, children,
-    child levels, invariants) copied out into pinned host buffers
-    (svdag_download_level)."""
+    triangles copied in from pinned host memory (cudaMemcpyAsync into a
+    device buffer, then svdag_set_device_triangles), the build, and every
+    level of both result pools (headers, children, child levels, invariants)
+    copied out into pinned host buffers (svdag_download_level)."""
     import ctypes
 
     pinned = torch.from_numpy(tris).pin_memory()
-    ptr = pinned.data_ptr()
     T = tris.shape[0]
     o = sv.Octree(device=local, stream=stream.cuda_stream)
     red_streams = [torch.cuda.Stream(device=local), torch.cuda.Stream(device=local)]
@@ -585,13 +590,33 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
             nbytes += n.value * (4 + (0 if leaf else 32) + (0 if (leaf or sdag) else 8) + (1 if sdag else 0))
         return nbytes
 
-    def build_one():
-        assert lib.svdag_upload_triangles(o._h, ptr, T) == 0
+    # the step's triangles copied from pinned host memory into one of two
+    # device buffers on a copy stream (cudaMemcpyAsync), then handed to the
+    # builder (svdag_set_device_triangles): pipelined, step i+1's copy runs
+    # while step i builds; a buffer is refilled only after the build that
+    # read it
+    dev_tris = [torch.empty_like(pinned, device=torch.device("cuda", local)) for _ in range(2)]
+    copy_stream = torch.cuda.Stream(device=local)
+    copied = [torch.cuda.Event(), torch.cuda.Event()]
+    freed = [torch.cuda.Event(), torch.cuda.Event()]
+
+    def upload(k):
+        b = k % 2
+        copy_stream.wait_event(freed[b])
+        with torch.cuda.stream(copy_stream):
+            dev_tris[b].copy_(pinned, non_blocking=True)
+            copied[b].record(copy_stream)
+
+    def build_one(k):
+        b = k % 2
+        stream.wait_event(copied[b])
+        assert lib.svdag_set_device_triangles(o._h, dev_tris[b].data_ptr(), T) == 0
         if args.step_level:
             o.buildDAG(args.levels, args.step_level)
         else:
             o.buildSVO(args.levels)
             o.toDAG()
+        freed[b].record(stream)
         o.initChildLevels()
 
     red_sms = 0 if args.no_pipeline else reduction_sms(args, torch, torch.device("cuda", local))
@@ -622,8 +647,9 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
         stream.wait_stream(red_streams[1])
         return d2h
 
-    for _ in range(max(1, args.warmup)):
-        build_one()
+    for k in range(max(1, args.warmup)):
+        upload(k)
+        build_one(k)
         end_one(start_one())
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -632,10 +658,16 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
     e0.record(stream)
     d2h = 0
     pending = None
-    for _ in range(args.steps):
-        # the next step's upload and voxelization overlap the previous
-        # step's reductions and read-back, unless --no-pipeline
-        build_one()
+    upload(0)
+    for k in range(args.steps):
+        # the next step's upload overlaps this step's build, and this step's
+        # build the previous step's reductions and read-back, unless
+        # --no-pipeline
+        if not args.no_pipeline and k + 1 < args.steps:
+            upload(k + 1)
+        build_one(k)
+        if args.no_pipeline and k + 1 < args.steps:
+            upload(k + 1)
         if pending is not None:
             d2h = end_one(pending)
             pending = None
@@ -652,9 +684,10 @@ def run_e2e(args, sv, torch, stream, local, tris, voxels, have_csv):
     return {"value": voxels / (ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms, "wall_ms_per_step": wall,
             "h2d_bytes_per_step": int(36 * T), "d2h_bytes_per_step": int(d2h),
             "pipelined": not args.no_pipeline, "reduction_sms": red_sms,
-            "path": "C ABI: svdag_upload_triangles from pinned host memory, build, svdag_download_level of every "
-                    "level of the SSVDAG and the CSVDAG into pinned host buffers; a step's upload and "
-                    "voxelization overlap the previous step's reductions and read-back"}
+            "path": "C ABI: the step's triangles copied from pinned host memory (cudaMemcpyAsync on a copy stream, "
+                    "two device buffers) and handed to svdag_set_device_triangles, build, svdag_download_level "
+                    "of every level of the SSVDAG and the CSVDAG into pinned host buffers; step i+1's upload "
+                    "overlaps step i's build, which overlaps step i-1's reductions and read-back"}
 
 
 # ---------------------------------------------------------------------------

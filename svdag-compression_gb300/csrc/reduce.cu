@@ -27,6 +27,7 @@
 // with a single read of the reduced counts at the end.  The per-level
 // toDAG kernels serve the entry point that works in caller-provided scratch.
 #include <algorithm>
+#include <cstdlib>
 
 #include "ctx.cuh"
 #include "dedup.cuh"
@@ -218,6 +219,7 @@ struct RedArgs {
   int* err;
   GridBar* bar;
   unsigned long long* trace;  // step trace or null
+  uint32_t top;               // toDAG: deepest level still to reduce (levels below: done by bulk launches)
 };
 
 // Level-ordered ids of the flagged nodes of this block's share:
@@ -255,77 +257,79 @@ __global__ void __launch_bounds__(kDagThreads, 1) k_dag_persistent(const RedArgs
   trace_mark(a.trace, trace_pos, kStEntry);
   const uint32_t L = a.levels;  // >= 2
   const RedLevel& leaf = a.lev[L - 1];
+  const uint32_t inner0 = a.top == L - 1 ? L - 2 : a.top;  // first inner level reduced here
   if (blockIdx.x == 0)
     for (int m = threadIdx.x; m < 256; m += blockDim.x) a.first[m] = kNone;
-  if (L >= 3) clear_slots(a.slots, a.lev[L - 2].slots);
+  if (inner0 >= 1) clear_slots(a.slots, a.lev[inner0].slots);
   for (int m = threadIdx.x; m < 256; m += blockDim.x) sf[m] = kNone;
   SVDAG_STEP(a, L - 1, kStPrologue);
-
-  // leaf level: first occurrence of every mask (four headers per 16-byte load)
-  {
-    const uint64_t n4 = leaf.n / 4;
-    const uint4* h4 = reinterpret_cast<const uint4*>(leaf.hdr);
-    SVDAG_GRID_STRIDE(q, n4) {
-      const uint4 w = h4[q];
-      const uint32_t hv[4] = {w.x, w.y, w.z, w.w};
+  if (a.top == L - 1) {
+    // leaf level: first occurrence of every mask (four headers per 16-byte load)
+    {
+      const uint64_t n4 = leaf.n / 4;
+      const uint4* h4 = reinterpret_cast<const uint4*>(leaf.hdr);
+      SVDAG_GRID_STRIDE(q, n4) {
+        const uint4 w = h4[q];
+        const uint32_t hv[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const uint32_t m = hv[j] & 0xFFu, i = uint32_t(4 * q + j);
-        if (m && sf[m] > i) atomicMin(&sf[m], i);  // read first: common masks repeat
+        for (int j = 0; j < 4; ++j) {
+          const uint32_t m = hv[j] & 0xFFu, i = uint32_t(4 * q + j);
+          if (m && sf[m] > i) atomicMin(&sf[m], i);  // read first: common masks repeat
+        }
+      }
+      SVDAG_GRID_STRIDE(i, leaf.n - 4 * n4) {
+        const uint32_t k = uint32_t(4 * n4 + i), m = leaf.hdr[k] & 0xFFu;
+        if (m && sf[m] > k) atomicMin(&sf[m], k);
       }
     }
-    SVDAG_GRID_STRIDE(i, leaf.n - 4 * n4) {
-      const uint32_t k = uint32_t(4 * n4 + i), m = leaf.hdr[k] & 0xFFu;
-      if (m && sf[m] > k) atomicMin(&sf[m], k);
-    }
-  }
-  __syncthreads();
-  for (int m = threadIdx.x; m < 256; m += blockDim.x)
-    if (sf[m] != kNone) atomicMin(&a.first[m], sf[m]);
-  SVDAG_STEP(a, L - 1, kStLeafFirst);
+    __syncthreads();
+    for (int m = threadIdx.x; m < 256; m += blockDim.x)
+      if (sf[m] != kNone) atomicMin(&a.first[m], sf[m]);
+    SVDAG_STEP(a, L - 1, kStLeafFirst);
 
-  // rank of each mask by first occurrence (every block), the reduced leaf
-  // level (block 0) and the leaves' parents
-  for (int m = threadIdx.x; m < 256; m += blockDim.x) sf[m] = a.first[m];
-  __syncthreads();
-  uint32_t present = 0;
-  for (int m = threadIdx.x; m < 256; m += blockDim.x) {
-    uint32_t r;
-    if (sf[m] != kNone) {
-      r = 0;
-      for (int k = 0; k < 256; ++k) r += (sf[k] < sf[m]) ? 1u : 0u;
-      if (blockIdx.x == 0) leaf.ohdr[r] = uint32_t(m);
-      ++present;
-    } else {
-      // a pointer to an empty node (only a joined chunk root can be one) maps
-      // to 0, the reference's default correspondence (geom_octree.cpp:493-496)
-      r = (m == 0) ? 0u : kNone;
+    // rank of each mask by first occurrence (every block), the reduced leaf
+    // level (block 0) and the leaves' parents
+    for (int m = threadIdx.x; m < 256; m += blockDim.x) sf[m] = a.first[m];
+    __syncthreads();
+    uint32_t present = 0;
+    for (int m = threadIdx.x; m < 256; m += blockDim.x) {
+      uint32_t r;
+      if (sf[m] != kNone) {
+        r = 0;
+        for (int k = 0; k < 256; ++k) r += (sf[k] < sf[m]) ? 1u : 0u;
+        if (blockIdx.x == 0) leaf.ohdr[r] = uint32_t(m);
+        ++present;
+      } else {
+        // a pointer to an empty node (only a joined chunk root can be one) maps
+        // to 0, the reference's default correspondence (geom_octree.cpp:493-496)
+        r = (m == 0) ? 0u : kNone;
+      }
+      sr[m] = r;
     }
-    sr[m] = r;
-  }
-  present = block_sum(present);
-  if (blockIdx.x == 0 && threadIdx.x == 0) a.cnt[L - 1] = present;
-  {
-    const RedLevel& P = a.lev[L - 2];
-    SVDAG_GRID_STRIDE(p, P.n) {
-      const uint32_t m = P.hdr[p] & 0xFFu;
-      if (!m) continue;
-      uint32_t c[8];
-      load_children(P.ch, p, c);
+    present = block_sum(present);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.cnt[L - 1] = present;
+    {
+      const RedLevel& P = a.lev[L - 2];
+      SVDAG_GRID_STRIDE(p, P.n) {
+        const uint32_t m = P.hdr[p] & 0xFFu;
+        if (!m) continue;
+        uint32_t c[8];
+        load_children(P.ch, p, c);
 #pragma unroll
-      for (int j = 0; j < 8; ++j)
-        if ((m >> j) & 1u) {
-          // an empty leaf never has a set parent bit after cleanEmptyNodes;
-          // the reference's zero-initialised correspondence is kept for it
-          const uint32_t lm = leaf.hdr[c[j]] & 0xFFu;
-          c[j] = lm ? sr[lm] : 0u;
-        }
-      store_children(P.ch, p, c);
+        for (int j = 0; j < 8; ++j)
+          if ((m >> j) & 1u) {
+            // an empty leaf never has a set parent bit after cleanEmptyNodes;
+            // the reference's zero-initialised correspondence is kept for it
+            const uint32_t lm = leaf.hdr[c[j]] & 0xFFu;
+            c[j] = lm ? sr[lm] : 0u;
+          }
+        store_children(P.ch, p, c);
+      }
     }
+    SVDAG_STEP(a, L - 1, kStLeafRank);
   }
-  SVDAG_STEP(a, L - 1, kStLeafRank);
 
-  for (uint32_t lev = L - 2; lev >= 1; --lev) {
+  for (uint32_t lev = inner0; lev >= 1; --lev) {
     const RedLevel& V = a.lev[lev];
     const Table T{a.slots, V.slots - 1};
     SVDAG_GRID_STRIDE(i, V.n) {
@@ -558,6 +562,19 @@ __global__ void __launch_bounds__(kRedThreads, 1) k_sdag_persistent(const RedArg
 
 }  // namespace
 
+// Bottom levels above this many nodes are reduced by ordinary launches at
+// full occupancy before the persistent kernel takes the rest: on levels of
+// hundreds of millions of nodes (the chunks of a depth-15 scene) the hash
+// inserts and gathers want every warp slot of an SM, and the launches cost
+// nothing next to their work.  SVDAG_BULK_LEVEL_NODES in the environment
+// overrides the threshold.
+constexpr uint64_t kBulkLevelNodes = 32ull << 20;
+uint64_t bulk_level_nodes() {
+  const char* e = std::getenv("SVDAG_BULK_LEVEL_NODES");
+  if (!e || !*e) return kBulkLevelNodes;
+  return std::strtoull(e, nullptr, 10);
+}
+
 void phase_reduce_dag(Ctx& c) {
   if (c.state != SVDAG_S_SVO && c.state != SVDAG_S_DAG)
     throw Error(SVDAG_ERR_INVALID_STATE, "toDAG: the octree is not an SVO or DAG");
@@ -571,6 +588,11 @@ void phase_reduce_dag(Ctx& c) {
     a.levels = L;
     uint64_t max_n = 1, max_slots = 32;
     std::vector<DBuf<uint32_t>> ohdr(L), och(L);
+    // levels reduced by bulk launches: the bottom ones above kBulkLevelNodes
+    const uint64_t bulk = bulk_level_nodes();
+    uint32_t top = L - 1;
+    while (top >= 1 && c.lev[top].n > bulk) --top;
+    a.top = top;
     for (uint32_t l = 0; l < L; ++l) {
       Level& V = c.lev[l];
       RedLevel& R = a.lev[l];
@@ -583,32 +605,66 @@ void phase_reduce_dag(Ctx& c) {
       } else {
         if (V.n >= 0xFFFFFFF0ull) throw Error(SVDAG_ERR_OVERFLOW, "toDAG: more than 2^32 nodes in a level");
         R.slots = table_slots(V.n);
-        max_n = std::max<uint64_t>(max_n, V.n);
-        max_slots = std::max<uint64_t>(max_slots, R.slots);
+        if (l <= top) {
+          max_n = std::max<uint64_t>(max_n, V.n);
+          max_slots = std::max<uint64_t>(max_slots, R.slots);
+        }
         ohdr[l].alloc(V.n ? V.n : 1, st);
         och[l].alloc(8 * (V.n ? V.n : 1), st);
         R.och = och[l].get();
       }
       R.ohdr = ohdr[l].get();
     }
-    const unsigned grid = persistent_grid(ex, k_dag_persistent, kDagThreads, std::max<uint64_t>(max_n, c.lev[L - 1].n));
-    DBuf<unsigned long long> slots(L >= 3 ? max_slots : 1, st);
-    DBuf<uint32_t> slot_of(max_n, st), rep(max_n, st), newid(max_n, st), bsum(grid, st), first(256, st);
     DBuf<RedCtl> ctl(1, st);
     SVDAG_CUDA(cudaMemsetAsync(ctl.get(), 0, sizeof(RedCtl), st));
-    a.slots = slots.get();
-    a.slot_of = slot_of.get();
-    a.rep = rep.get();
-    a.newid = newid.get();
-    a.bsum = bsum.get();
-    a.first = first.get();
-    a.cnt = ctl.get()->cnt;
-    a.err = &ctl.get()->err;
-    a.bar = &ctl.get()->bar;
+    RedCtl* d_ctl = ctl.get();
+    // bulk levels, bottom-up (no host synchronisation: counts go to the control block)
+    for (uint32_t lev = L - 1; lev > top; --lev) {
+      const Level& V = c.lev[lev];
+      Level& P = c.lev[lev - 1];
+      const uint64_t n = V.n;
+      if (lev == L - 1) {
+        DBuf<uint32_t> first(256, st), rank(256, st);
+        fill<uint32_t>(ex, first.get(), 256, kNone);
+        SVDAG_LAUNCH(ex, k_leaf_first, grid_for(ex, n, 256, 4), 256, 0, V.hdr.get(), n, first.get());
+        SVDAG_LAUNCH(ex, k_leaf_rank, 1, 256, 0, first.get(), rank.get(), ohdr[lev].get(), &d_ctl->cnt[lev]);
+        if (P.n)
+          SVDAG_LAUNCH(ex, k_remap_parents_leafrank, grid_for(ex, P.n, 256), 256, 0, P.hdr.get(), P.ch.get(), P.n,
+                       V.hdr.get(), rank.get());
+      } else {
+        DBuf<unsigned long long> tb;
+        const Table T = make_table(ex, n, tb);
+        DBuf<uint32_t> slot_of(n, st), rep(n, st), newid(n, st), corr(n, st);
+        SVDAG_LAUNCH(ex, k_insert, grid_for(ex, n, 256), 256, 0, T, V.hdr.get(), V.ch.get(), n, slot_of.get(),
+                     &d_ctl->err);
+        SVDAG_LAUNCH(ex, k_rep, grid_for(ex, n, 256), 256, 0, T, slot_of.get(), n, rep.get());
+        tb.release();
+        device_exclusive_scan<uint32_t>(ex, RepFlagIn{rep.get()}, n, U32Out{newid.get()}, &d_ctl->cnt[lev]);
+        SVDAG_LAUNCH(ex, k_compact_dag, grid_for(ex, n, 256), 256, 0, V.hdr.get(), V.ch.get(), n, rep.get(),
+                     newid.get(), ohdr[lev].get(), och[lev].get(), corr.get());
+        if (P.n)
+          SVDAG_LAUNCH(ex, k_remap_parents, grid_for(ex, P.n, 256), 256, 0, P.hdr.get(), P.ch.get(), P.n, corr.get());
+      }
+    }
     PhaseTrace trace(st);
-    a.trace = trace.ptr();
-    launch_persistent(ex, "k_dag_persistent", k_dag_persistent, grid, kDagThreads, 0, a);
-    const RedCtl h = finish_persistent(ex, ctl.get(), "toDAG");
+    if (top >= 1) {
+      const uint64_t work = top == L - 1 ? std::max<uint64_t>(max_n, c.lev[L - 1].n) : max_n;
+      const unsigned grid = persistent_grid(ex, k_dag_persistent, kDagThreads, work);
+      DBuf<unsigned long long> slots(max_slots, st);
+      DBuf<uint32_t> slot_of(max_n, st), rep(max_n, st), newid(max_n, st), bsum(grid, st), first(256, st);
+      a.slots = slots.get();
+      a.slot_of = slot_of.get();
+      a.rep = rep.get();
+      a.newid = newid.get();
+      a.bsum = bsum.get();
+      a.first = first.get();
+      a.cnt = d_ctl->cnt;
+      a.err = &d_ctl->err;
+      a.bar = &d_ctl->bar;
+      a.trace = trace.ptr();
+      launch_persistent(ex, "k_dag_persistent", k_dag_persistent, grid, kDagThreads, 0, a);
+    }
+    const RedCtl h = finish_persistent(ex, d_ctl, "toDAG");
     trace.report(ex, "toDAG");
     for (uint32_t l = 1; l < L; ++l) {
       Level& V = c.lev[l];

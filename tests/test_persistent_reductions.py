@@ -101,3 +101,64 @@ def test_deep_narrow_octree():
     c.mergeAcrossAllLevels()
     assert oracle_py.pool_digest(c.pool()) == oracle_py.pool_digest(rc.pool())
     assert c.stats()["n_cross_level_merged"] == rc.stats()["n_cross_level_merged"]
+
+
+@pytest.mark.parametrize("blocks", [1, 3])
+def test_capped_grids_give_the_same_result(blocks):
+    """svdag_set_persistent_blocks caps the reduction grids; one block (the
+    barrier's trivial case, every wait of the SSVDAG resolution inside one
+    block) and three blocks give the reference's digests."""
+    name = "terrain129_L9"
+    g = G[name]
+    o = sv.Octree()
+    o.set_persistent_blocks(blocks)
+    o.upload_triangles(SCENES[name]())
+    o.buildSVO(g["levels"])
+    o.toDAG()
+    o.initChildLevels()
+    assert oracle_py.pool_digest(o.pool()) == g["dag"]["digest"]
+    s, c = o.clone(), o.clone()
+    s.toSDAG()
+    assert oracle_py.pool_digest(s.pool()) == g["sdag"]["digest"]
+    assert c.mergeAcrossAllLevels() == g["nCrossLevelMerged"]
+    assert oracle_py.pool_digest(c.pool()) == g["csv"]["digest"]
+
+
+def test_phase_trace_reports_steps(monkeypatch, capfd):
+    """SVDAG_PHASE_TRACE prints each phase's step times (stderr) and changes
+    no result."""
+    name = "ico3_L6"
+    g = G[name]
+    monkeypatch.setenv("SVDAG_PHASE_TRACE", "1")
+    o = sv.Octree()
+    o.upload_triangles(SCENES[name]())
+    o.buildSVO(g["levels"])
+    o.toDAG()
+    o.initChildLevels()
+    s = o.clone()
+    s.toSDAG()
+    err = capfd.readouterr().err
+    assert "[svdag trace] toDAG" in err and "[svdag trace] toSDAG" in err
+    assert "candidates" in err and "insert" in err
+    assert oracle_py.pool_digest(s.pool()) == g["sdag"]["digest"]
+
+
+@pytest.mark.parametrize("bulk", ["0", "2000"])
+def test_bulk_levels_then_persistent(monkeypatch, bulk):
+    """toDAG reduces its largest bottom levels with ordinary launches and the
+    rest with the persistent kernel (the threshold is lowered so that small
+    scenes take both paths; 0 = every level by launches): the reference's
+    digests either way."""
+    monkeypatch.setenv("SVDAG_BULK_LEVEL_NODES", bulk)
+    for name in ["terrain129_L9", "ico5_L7"]:
+        g = G[name]
+        o = sv.Octree()
+        o.upload_triangles(SCENES[name]())
+        o.buildSVO(g["levels"])
+        o.toDAG()
+        o.initChildLevels()
+        assert o.stats()["n_nodes_dag"] == g["nNodesDAG"]
+        assert oracle_py.pool_digest(o.pool()) == g["dag"]["digest"]
+        s = o.clone()
+        s.toSDAG()
+        assert oracle_py.pool_digest(s.pool()) == g["sdag"]["digest"]
