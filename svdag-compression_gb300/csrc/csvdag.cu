@@ -420,11 +420,11 @@ void phase_cross_level_merge(Ctx& c) {
   // the largest class-id domain is levels 1..L-2 (height 1)
   const uint64_t dom = (L >= 3) ? uint64_t(a.off[L - 1]) - a.off[1] : 0;
   const uint64_t Nn = N ? N : 1, dn = dom ? dom : 1;
-  // shared-memory bitmap: the largest child level's words, up to 160 KB
+  // shared-memory bitmap: the largest child level's words, up to kMaxPersistentSmem
   uint32_t smem_words = 0;
   for (uint32_t l = 2; l < L; ++l)
     smem_words = std::max<uint32_t>(smem_words, ((a.off[l + 1] + 31) >> 5) - (a.off[l] >> 5));
-  smem_words = std::min<uint32_t>(smem_words, 40960);
+  smem_words = std::min<uint32_t>(smem_words, uint32_t(kMaxPersistentSmem / 4));
   a.smem_words = smem_words;
   const unsigned grid = persistent_grid(ex, k_csv_persistent, kRedThreads, Nn, 4 * smem_words);
   DBuf<unsigned long long> slots(table_slots(dn), st), path(Nn, st), best(Nn, st), missing(1, st);

@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <mutex>
 #include <type_traits>
 #include <vector>
 
@@ -168,10 +169,28 @@ void launch_persistent(const Exec& ex, const char* name, void (*kern)(KArgs...),
 // registers fills an SM; a cooperative launch starts only when all of its
 // blocks can be resident, so persistent kernels on different streams that
 // do not fit together run one after the other rather than deadlock.
+// Largest dynamic shared memory of a persistent launch.
+constexpr size_t kMaxPersistentSmem = 160 * 1024;
+
+// Raises a kernel's dynamic shared-memory limit to kMaxPersistentSmem, once
+// per (kernel, device): host threads that launch the same kernel with
+// different sizes must not lower the limit under each other's launches.
+inline void allow_persistent_smem(const void* kern) {
+  static std::mutex mu;
+  static std::vector<std::pair<const void*, int>> done;
+  int dev = 0;
+  SVDAG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  for (const auto& d : done)
+    if (d.first == kern && d.second == dev) return;
+  SVDAG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kMaxPersistentSmem)));
+  done.emplace_back(kern, dev);
+}
+
 template <class K>
 unsigned persistent_grid(const Exec& ex, K kern, unsigned threads, uint64_t work, size_t smem = 0) {
-  if (smem > 48 * 1024)
-    SVDAG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  if (smem > kMaxPersistentSmem) throw Error(SVDAG_ERR_INVALID_ARG, "persistent kernel: shared memory above the limit");
+  if (smem > 48 * 1024) allow_persistent_smem((const void*)kern);
   int per_sm = 0;
   SVDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, int(threads), smem));
   if (per_sm < 1) throw Error(SVDAG_ERR_CUDA, "persistent kernel cannot be resident");
