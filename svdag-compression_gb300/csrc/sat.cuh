@@ -512,7 +512,9 @@ SAT_HD void pair_basic(const float t[9], const float* tp, const double* c, const
 }
 
 // Slab classification of the pair (see Slab).
-SAT_HD void pair_slabs(Pair32& P) {
+// Slab classes of the pair: per axis and side, whether the triangle is
+// outside, inside or across the child slab (or undecided).
+SAT_HD void pair_slab_classes(Pair32& P) {
   if (!P.fast) return;
   const float* t = P.t;
   const NodeBoxes& nb = P.nb;
@@ -557,6 +559,15 @@ SAT_HD void pair_slabs(Pair32& P) {
     }
   }
   P.slab = slab;
+}
+
+// Grid-plane tangency and axis-aligned triangles (only the full test reads
+// them).
+SAT_HD void pair_tangency(Pair32& P) {
+  if (!P.fast) return;
+  const float* t = P.t;
+  const NodeBoxes& nb = P.nb;
+  const float h = P.h, clo = nb.clo;
   // Grid-plane tangency.  When the three vertices share coordinate q
   // (t_q constant) and the child face lies exactly on that plane
   // (t_q - c_q = +-h exactly, c_q an fp32 value), the reference's fp64
@@ -590,6 +601,38 @@ SAT_HD void pair_slabs(Pair32& P) {
     }
   }
   P.tang = tang;
+}
+
+SAT_HD void pair_slabs(Pair32& P) {
+  pair_slab_classes(P);
+  pair_tangency(P);
+}
+
+// child_fast() of all 8 children at once: hit = children whose three slabs
+// are inside, full = children the slabs leave undecided (neither inside on
+// every axis nor outside on one); the rest do not overlap.
+SAT_HD void child_masks(const Pair32& P, uint32_t& hit, uint32_t& full) {
+  if (!P.fast) {
+    hit = 0;
+    full = 0xFFu;
+    return;
+  }
+  // children on side s of axis q: X 0x0F / 0xF0, Y 0x33 / 0xCC, Z 0x55 / 0xAA
+  const uint32_t side[6] = {0x0Fu, 0xF0u, 0x33u, 0xCCu, 0x55u, 0xAAu};
+  uint32_t in = 0xFFu, out = 0;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    uint32_t inq = 0;
+#pragma unroll
+    for (int sd = 0; sd < 2; ++sd) {
+      const uint32_t c = (P.slab >> (2 * (2 * q + sd))) & 3u;
+      if (c == kSlabIn) inq |= side[2 * q + sd];
+      if (c == kSlabOut) out |= side[2 * q + sd];
+    }
+    in &= inq;
+  }
+  hit = in;
+  full = 0xFFu & ~in & ~out;
 }
 
 SAT_HD void pair_setup(const float t[9], const float* tp, const double* c, const NodeBoxes& nb, double k,

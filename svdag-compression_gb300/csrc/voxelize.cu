@@ -145,15 +145,12 @@ __global__ void __launch_bounds__(kExpandThreads, SVDAG_EXPAND_MIN_BLOCKS) k_exp
       nb.chi[4] = b.x; nb.chi[5] = b.y; nb.clo = b.z; nb.ok = b.w;
       sat::Pair32 PP;
       sat::pair_core(tri, tp, ctr + 3ull * node, nb, k, PP);
-      sat::pair_slabs(PP);
-      uint32_t full = 0;
-      for (int ci = 7; ci >= 0; --ci) {
-        const int f = sat::child_fast(PP, ci);
-        if (f == 1) hits |= 1u << ci;
-        else if (f == 2) full |= 1u << ci;
-      }
+      sat::pair_slab_classes(PP);
+      uint32_t full;
+      sat::child_masks(PP, hits, full);
       s_node[tid] = node;
       if (full) {
+        sat::pair_tangency(PP);
         // this pair's undecided children in consecutive queue slots, and the
         // pair data the full test reads (pairs the slabs decide skip both)
         uint32_t slot = atomicAdd(&s_qn, uint32_t(__popc(full)));
