@@ -404,10 +404,11 @@ __global__ void __launch_bounds__(kRedThreads, 1) k_sdag_persistent(const RedArg
     }
     SVDAG_STEP(a, lev, kStInsert);
 
-    // invariance bits and the candidates of the 7 normalised variants: eight
-    // lanes per node, lane v looks variant v up (v = 0: the raw key's first
-    // occurrence from the insert), so a node costs one lookup's latency;
-    // lane k loads child k's invariance bits once and the group shares them
+    // invariance bits and the candidates of the variants: eight lanes per
+    // node, all on the same path -- lane v looks variant v up (v = 0: the raw
+    // key, whose first occurrence the table holds), lanes 1-3 also test the
+    // node's invariance on X, Y, Z (n == n.mirror(axis), geom_octree.cpp:604-606),
+    // and lane k loads child k's invariance bits, shared by shuffles
     {
       const int v = threadIdx.x & 7;
       const int g0 = int(threadIdx.x & 24);  // first lane of the group in the warp
@@ -421,21 +422,11 @@ __global__ void __launch_bounds__(kRedThreads, 1) k_sdag_persistent(const RedArg
         uint32_t cinv[8];  // invariance bits of the child at mirrored position k
 #pragma unroll
         for (int k = 0; k < 8; ++k) cinv[k] = __shfl_sync(gmask, mine, g0 | (k ^ flip));
-        if (v == 0) {
-          const uint32_t s = a.slot_of[i];
-          a.cand[i] = (s == kNone) ? kNone : uint32_t(a.slots[s]);
-          // invariance on X, Y, Z (geom_octree.cpp:604-606): n == n.mirror(axis)
-          uint32_t iv = 0;
-          uint32_t mh, mc[8];
-          mirror_node(h, c, 4, mh, mc); if (same_key(h, c, mh, mc)) iv |= 1u;
-          mirror_node(h, c, 2, mh, mc); if (same_key(h, c, mh, mc)) iv |= 2u;
-          mirror_node(h, c, 1, mh, mc); if (same_key(h, c, mh, mc)) iv |= 4u;
-          a.inv[i] = uint8_t(iv);
-          a.state[i] = kUndecided;
-          continue;
-        }
         uint32_t vh, vc[8];
         mirror_node(h, c, flip, vh, vc);
+        // lanes 1, 2, 3 hold the X, Y, Z mirrors (flips 4, 2, 1)
+        const bool inv_bit = (v >= 1 && v <= 3) && same_key(h, c, vh, vc);
+        const unsigned ib = __ballot_sync(gmask, inv_bit) >> g0;
         if (child_inv) {
           // invertInvs (geom_octree.cpp:822-831): drop the mirror bit of an
           // axis of this variant when the child is invariant on it
@@ -450,7 +441,12 @@ __global__ void __launch_bounds__(kRedThreads, 1) k_sdag_persistent(const RedArg
           }
           vh &= ~((clrx << 8) | (clry << 16) | (clrz << 24));
         }
-        a.cand[uint64_t(v) * n + i] = table_find(T, V.hdr, V.ch, vh, vc);
+        // lane 0: an empty node (never in a DAG) has no slot and no candidate
+        a.cand[uint64_t(v) * n + i] = (v == 0 && (h & 0xFFu) == 0) ? kNone : table_find(T, V.hdr, V.ch, vh, vc);
+        if (v == 0) {
+          a.inv[i] = uint8_t((ib >> 1) & 7u);  // bit 0 X (lane 1), 1 Y (lane 2), 2 Z (lane 3)
+          a.state[i] = kUndecided;
+        }
       }
     }
     SVDAG_STEP(a, lev, kStCandidates);
