@@ -114,6 +114,17 @@ def rank_info():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
 
 
+def max_over_ranks(value, torch, device, world):
+    """The largest of the ranks' values (replicas: the job's time is its
+    slowest rank's); the value itself on one rank.  `device` holds the
+    reduction tensor: a CUDA device under NCCL, the CPU under gloo."""
+    if world <= 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
@@ -379,11 +390,7 @@ def run_ours(args, rank, local, world):
                     extra += o.stats()["gpu_launches"]
         e1.record(stream)
         torch.cuda.synchronize()
-        ms_total = e0.elapsed_time(e1)
-        if world > 1:
-            t = torch.tensor([ms_total], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms_total = float(t.item())
+        ms_total = max_over_ranks(e0.elapsed_time(e1), torch, dev, world)
         base.profile(False)
         prof = {}
         for ph in phase_prof.values():
