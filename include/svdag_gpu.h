@@ -121,7 +121,11 @@ int svdag_build_dag(svdag_ctx* ctx, uint32_t levels, uint32_t step_level, const 
  * predicates decided in fp64.  Host buffers; synchronous. */
 int svdag_tri_box_children(svdag_ctx* ctx, const float* tris, const double* centers, const double* half_sides,
                            uint64_t n, uint8_t* masks, uint64_t* fallbacks);
-/* GeomOctree::toDAG (src/symvox/geom_octree.cpp:462-548) */
+/* GeomOctree::toDAG (src/symvox/geom_octree.cpp:462-548).  toDAG and toSDAG
+ * rewrite the parent levels in place as they go: when either fails on the
+ * device (SVDAG_ERR_OVERFLOW: hash probe limit; SVDAG_ERR_TIMEOUT: a grid
+ * barrier of the persistent kernel ran out), the octree is left EMPTY and
+ * must be rebuilt. */
 int svdag_reduce_dag(svdag_ctx* ctx);
 /* GeomOctree::sortByEffectiveRefCount (src/symvox/geom_octree_extension.cpp:
  * 521-620): every level of a DAG reordered by effective reference count

@@ -660,7 +660,14 @@ void phase_reduce_dag(Ctx& c) {
       a.trace = trace.ptr();
       launch_persistent(ex, "k_dag_persistent", k_dag_persistent, grid, kDagThreads, 0, a);
     }
-    const RedCtl h = finish_persistent(ex, d_ctl, "toDAG");
+    RedCtl h;
+    try {
+      h = finish_persistent(ex, d_ctl, "toDAG");
+    } catch (const Error&) {
+      // the parents were remapped in place: the octree must be rebuilt
+      c.state = SVDAG_S_EMPTY;
+      throw;
+    }
     trace.report(ex, "toDAG");
     for (uint32_t l = 1; l < L; ++l) {
       Level& V = c.lev[l];
@@ -735,7 +742,14 @@ void phase_reduce_sdag(Ctx& c) {
     PhaseTrace trace(st);
     a.trace = trace.ptr();
     launch_persistent(ex, "k_sdag_persistent", k_sdag_persistent, grid, kRedThreads, 0, a);
-    const RedCtl h = finish_persistent(ex, ctl.get(), "toSDAG");
+    RedCtl h;
+    try {
+      h = finish_persistent(ex, ctl.get(), "toSDAG");
+    } catch (const Error&) {
+      // the parents were remapped in place: the octree must be rebuilt
+      c.state = SVDAG_S_EMPTY;
+      throw;
+    }
     trace.report(ex, "toSDAG");
     for (uint32_t l = 1; l < L; ++l) {
       Level& V = c.lev[l];
