@@ -257,7 +257,7 @@ struct PhaseTrace {
     }
     std::fprintf(stderr, "[svdag trace] %s: %.1f us over %u marks\n", phase,
                  n > 1 ? double(h[2 * (n - 1) + 1] - h[1]) * 1e-3 : 0.0, n);
-    for (int s = 0; s < kStNumSteps; ++s) {
+    for (int s = 0; s < int(kStNumSteps); ++s) {
       if (!cnt[s]) continue;
       std::fprintf(stderr, "[svdag trace]   %-16s %9.1f us  x%-3u", kNames[s], tot[s], cnt[s]);
       for (int l = 0; l < kLv; ++l)

@@ -620,10 +620,8 @@ SAT_HD void child_masks(const Pair32& P, uint32_t& hit, uint32_t& full) {
   // children on side s of axis q: X 0x0F / 0xF0, Y 0x33 / 0xCC, Z 0x55 / 0xAA
   const uint32_t side[6] = {0x0Fu, 0xF0u, 0x33u, 0xCCu, 0x55u, 0xAAu};
   uint32_t in = 0xFFu, out = 0;
-#pragma unroll
   for (int q = 0; q < 3; ++q) {
     uint32_t inq = 0;
-#pragma unroll
     for (int sd = 0; sd < 2; ++sd) {
       const uint32_t c = (P.slab >> (2 * (2 * q + sd))) & 3u;
       if (c == kSlabIn) inq |= side[2 * q + sd];
