@@ -162,3 +162,29 @@ def test_bulk_levels_then_persistent(monkeypatch, bulk):
         s = o.clone()
         s.toSDAG()
         assert oracle_py.pool_digest(s.pool()) == g["sdag"]["digest"]
+
+
+def test_concurrent_merges_with_large_bitmaps():
+    """Four merges of the 2048² depth-12 terrain's DAG at once, from four host
+    threads on four streams: their check-set bitmaps exceed 48 KB of shared
+    memory, so the kernel's shared-memory limit is raised -- once, never
+    lowered under another thread's launch.  Each result is the reference's."""
+    torch = pytest.importorskip("torch")
+    name = "terrain2048_L12"
+    g = G[name]
+    o = sv.Octree()
+    o.upload_triangles(SCENES[name]())
+    o.buildSVO(g["levels"])
+    o.toDAG()
+    o.initChildLevels()
+    streams = [torch.cuda.Stream() for _ in range(4)]
+    clones = [o.clone(stream=s.cuda_stream) for s in streams]
+
+    def run(c):
+        merged = c.mergeAcrossAllLevels()
+        return merged, oracle_py.pool_digest(c.pool())
+
+    with concurrent.futures.ThreadPoolExecutor(4) as ex:
+        for merged, digest in ex.map(run, clones):
+            assert merged == g["nCrossLevelMerged"]
+            assert digest == g["csv"]["digest"]
