@@ -327,7 +327,9 @@ typedef struct svdag_batch svdag_batch;
 enum { SVDAG_BATCH_SDAG = 1, SVDAG_BATCH_CSVDAG = 2 };
 enum { SVDAG_BATCH_RESULT_DAG = 0, SVDAG_BATCH_RESULT_SDAG = 1, SVDAG_BATCH_RESULT_CSVDAG = 2 };
 typedef struct svdag_batch_tuning {
-  double table_factor; /* hash slots per cell of a height (rounded up to a power of two), 1.25..16 */
+  double table_factor; /* hash slots per key of a height (rounded up to a power of two), 1.25..16: per cell
+                          until a height has been seen, then per expected distinct key (twice the
+                          largest share of distinct keys among the cells seen at that height) */
   uint32_t threads;    /* block size of the per-height kernels, 64..1024, multiple of 32 */
   uint32_t streams;    /* chunks reduced concurrently in the SSVDAG / CSVDAG stage, 1..64 */
 } svdag_batch_tuning;
@@ -335,6 +337,8 @@ typedef struct svdag_batch_stats {
   double dag_ms;       /* wall time of the batched toDAG stage of the last build */
   double reduce_ms;    /* wall time of the SSVDAG / CSVDAG stage */
   uint64_t gpu_launches;
+  uint64_t table_retries; /* heights redone with a full-size hash table after the
+                             estimated one proved too small (all builds) */
 } svdag_batch_stats;
 int svdag_batch_create(svdag_batch** out, int device, void* stream);
 int svdag_batch_destroy(svdag_batch* batch);

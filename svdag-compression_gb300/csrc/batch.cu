@@ -25,6 +25,7 @@
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
+#include <cstdlib>
 #include <functional>
 #include <mutex>
 #include <new>
@@ -229,16 +230,22 @@ __device__ __forceinline__ uint64_t key_hash(uint32_t chunk, uint32_t m, const u
 
 constexpr int kGBits = 40;  // cell index bits in a slot (the rest: hash tag)
 constexpr uint64_t kGMask = (1ull << kGBits) - 1;
+// Probes after which an insert into a table sized from an estimate gives up
+// (the table is then rebuilt at full size).
+constexpr uint64_t kProbeLimit = 512;
 
 // Probe for the key of cell g; returns its slot (inserted, or found holding
-// an equal key, lowered to g when g is smaller), or ~0 when the table is full.
+// an equal key, lowered to g when g is smaller), or ~0 when `limit` + 1 slots
+// were probed without either (always the case for a full table when limit =
+// mask).
 __device__ __forceinline__ uint64_t batch_probe(const HeightView& V, uint64_t g, uint32_t chunk, uint32_t m,
                                                 const uint32_t ids[8], uint64_t hk,
-                                                unsigned long long* __restrict__ slots, uint64_t mask) {
+                                                unsigned long long* __restrict__ slots, uint64_t mask,
+                                                uint64_t limit) {
   const uint64_t tag = hk >> kGBits;
   const unsigned long long mine = (tag << kGBits) | g;
   uint64_t pos = hk & mask;
-  for (uint64_t probe = 0; probe <= mask; ++probe) {
+  for (uint64_t probe = 0; probe <= limit; ++probe) {
     unsigned long long cur = __ldcg(&slots[pos]);
     if (cur == kEmpty64) {
       const unsigned long long prev = atomicCAS(&slots[pos], kEmpty64, mine);
@@ -266,11 +273,19 @@ __device__ __forceinline__ uint64_t batch_probe(const HeightView& V, uint64_t g,
 // holds it (~0 for empty cells).  Lanes of a warp with the same key -- runs
 // of identical cells are common in solid or empty regions -- probe once: the
 // lowest such lane (also the smallest cell index) probes for all of them.
+// A probe that gives up sets *err; with limit < mask (a table sized from an
+// estimate) the other warps then stop early, as the insert will be redone.
 __global__ void k_batch_insert(HeightView V, uint64_t total, unsigned long long* __restrict__ slots, uint64_t mask,
-                               uint64_t* __restrict__ slot_of, int* err) {
+                               uint64_t limit, uint64_t* __restrict__ slot_of, int* err) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint64_t warps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
   for (uint64_t w = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; (w << 5) < total; w += warps) {
+    if (limit < mask) {
+      // warp-uniform: every lane takes the flag lane 0 read
+      int stop = 0;
+      if (lane == 0) stop = *reinterpret_cast<volatile int*>(err);
+      if (__shfl_sync(0xFFFFFFFFu, stop, 0)) return;
+    }
     const uint64_t g = (w << 5) + lane;
     uint32_t e = 0, ids[8], m = 0;
     bool part = false;
@@ -294,21 +309,24 @@ __global__ void k_batch_insert(HeightView V, uint64_t total, unsigned long long*
 #pragma unroll
     for (int k = 0; k < 8; ++k) same &= __shfl_sync(act, ids[k], lead) == ids[k];
     uint64_t pos = 0;
-    if (int(lane) == lead) pos = batch_probe(V, g, chunk, m, ids, hk, slots, mask);
+    if (int(lane) == lead) pos = batch_probe(V, g, chunk, m, ids, hk, slots, mask, limit);
     const uint64_t lpos = __shfl_sync(act, pos, lead);
-    if (int(lane) != lead) pos = same ? lpos : batch_probe(V, g, chunk, m, ids, hk, slots, mask);
+    if (int(lane) != lead) pos = same ? lpos : batch_probe(V, g, chunk, m, ids, hk, slots, mask, limit);
     if (pos == ~0ull) atomicExch(err, 1);
     slot_of[g] = pos;
   }
 }
 
 // The representative (smallest index with the same key) of every non-empty
-// cell: the index its slot holds once every insert is done.
-__global__ void k_batch_rep(uint64_t total, const unsigned long long* __restrict__ slots,
-                            uint64_t* __restrict__ rep) {
+// cell: the index its slot holds once every insert is done.  Nothing to do
+// when an insert into an estimated table gave up (retry non-null and set:
+// slot_of is incomplete and the height is redone).
+__global__ void k_batch_rep(uint64_t total, const unsigned long long* __restrict__ slots, uint64_t mask,
+                            const int* __restrict__ retry, uint64_t* __restrict__ rep) {
+  if (retry && *retry) return;
   for (uint64_t g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; g < total; g += uint64_t(gridDim.x) * blockDim.x) {
     const uint64_t p = rep[g];
-    rep[g] = p == ~0ull ? ~0ull : (slots[p] & kGMask);
+    rep[g] = p > mask ? ~0ull : (slots[p] & kGMask);
   }
 }
 
@@ -487,12 +505,17 @@ void build_wave(Batch& B, const std::vector<uint32_t>& sel) {
   DBuf<uint64_t> d_nb(N, st);
   DBuf<uint32_t> first(256ull * N, st), rank(256ull * N, st), leaf_hdr(256ull * N, st), leaf_cnt(N, st);
   DBuf<unsigned long long> vox(N, st);
-  DBuf<int> d_err(1, st);
+  DBuf<int> d_err(1, st), d_retry(1, st);
   SVDAG_CUDA(cudaMemcpyAsync(d_bricks.get(), hb.data(), sizeof(void*) * N, cudaMemcpyHostToDevice, st));
   SVDAG_CUDA(cudaMemcpyAsync(d_nb.get(), hn.data(), 8ull * N, cudaMemcpyHostToDevice, st));
   SVDAG_CUDA(cudaMemsetAsync(first.get(), 0xFF, 4 * 256ull * N, st));
   SVDAG_CUDA(cudaMemsetAsync(vox.get(), 0, 8ull * N, st));
   SVDAG_CUDA(cudaMemsetAsync(d_err.get(), 0, 4, st));
+  SVDAG_CUDA(cudaMemsetAsync(d_retry.get(), 0, 4, st));
+  // SVDAG_BATCH_TABLE_SHARE replaces the learned distinct-key shares (every
+  // height) with a fixed one: small values force the full-size rebuild
+  double share_env = 0;
+  if (const char* e = std::getenv("SVDAG_BATCH_TABLE_SHARE")) share_env = std::atof(e);
   {
     uint64_t mx = 0;
     for (auto v : hn) mx = std::max(mx, v);
@@ -579,30 +602,60 @@ void build_wave(Batch& B, const std::vector<uint32_t>& sel) {
     V.is_top = d_top.get();
     V.h = h;
 
-    // hash table sized from the cell count (load <= 1 / B.tuning.table_factor)
-    const uint64_t size = next_pow2(uint64_t(double(std::max<uint64_t>(total, 16)) * B.tuning.table_factor));
-    DBuf<unsigned long long> slots(size, st);
-    SVDAG_CUDA(cudaMemsetAsync(slots.get(), 0xFF, 8 * size, st));
+    // Hash table: load <= 1 / B.tuning.table_factor over every cell of the
+    // height (full size), or over twice the largest share of distinct keys
+    // that earlier waves and builds saw at this height -- the distinct keys
+    // are a few per cent of the cells on the lowest heights, so the table is
+    // much smaller to clear and to probe.  An insert into the smaller table
+    // that probes kProbeLimit slots in vain sets d_retry, and the height is
+    // redone with the full-size table.
     const unsigned tb = B.tuning.threads;
     if (total >= (1ull << 32)) throw Error(SVDAG_ERR_OVERFLOW, "batch: more than 2^32 cells on one height");
+    const uint64_t full = next_pow2(uint64_t(double(std::max<uint64_t>(total, 16)) * B.tuning.table_factor));
+    const double share = share_env > 0 ? share_env : (h < B.distinct_share.size() ? B.distinct_share[h] : 0.0);
+    uint64_t size = full;
+    if (share > 0) {
+      const double keys = std::max(2.0 * share * double(total), 65536.0);
+      size = std::min(full, next_pow2(uint64_t(keys * B.tuning.table_factor)));
+    }
     DBuf<uint64_t> rep(total, st);
     DBuf<uint32_t> newid(total, st);
-    SVDAG_LAUNCH(ex, k_batch_insert, grid_for(ex, total, tb, 8), tb, 0, V, total, slots.get(), size - 1, rep.get(),
-                 d_err.get());
-    SVDAG_LAUNCH(ex, k_batch_rep, grid_for(ex, total, tb, 8), tb, 0, total, slots.get(), rep.get());
-    slots.release();
     DBuf<uint32_t> d_total(1, st);
-    device_exclusive_scan<uint32_t>(ex, RepIn{rep.get()}, total, U32Out{newid.get()}, d_total.get());
-    // DAG nodes of each entry: newid range [newid at its first cell, next entry's)
+    auto dedup = [&](uint64_t tsize) {
+      const bool bounded = tsize < full;
+      DBuf<unsigned long long> slots(tsize, st);
+      SVDAG_CUDA(cudaMemsetAsync(slots.get(), 0xFF, 8 * tsize, st));
+      SVDAG_LAUNCH(ex, k_batch_insert, grid_for(ex, total, tb, 8), tb, 0, V, total, slots.get(), tsize - 1,
+                   bounded ? std::min<uint64_t>(kProbeLimit, tsize - 1) : tsize - 1, rep.get(),
+                   bounded ? d_retry.get() : d_err.get());
+      SVDAG_LAUNCH(ex, k_batch_rep, grid_for(ex, total, tb, 8), tb, 0, total, slots.get(), tsize - 1,
+                   bounded ? d_retry.get() : nullptr, rep.get());
+      slots.release();
+      device_exclusive_scan<uint32_t>(ex, RepIn{rep.get()}, total, U32Out{newid.get()}, d_total.get());
+    };
+    // DAG nodes of each entry: newid range [newid at its first cell, next
+    // entry's); read together with the retry flag (one synchronisation)
     std::vector<uint64_t> rep_base(n + 1);
-    {
+    auto read_bases = [&]() -> bool {
       std::vector<uint32_t> h_nid(n + 1);
+      int retry = 0;
       for (uint32_t e = 0; e < n; ++e)
         SVDAG_CUDA(cudaMemcpyAsync(&h_nid[e], newid.get() + base[e], 4, cudaMemcpyDeviceToHost, st));
       SVDAG_CUDA(cudaMemcpyAsync(&h_nid[n], d_total.get(), 4, cudaMemcpyDeviceToHost, st));
+      SVDAG_CUDA(cudaMemcpyAsync(&retry, d_retry.get(), 4, cudaMemcpyDeviceToHost, st));
       SVDAG_CUDA(cudaStreamSynchronize(st));
       for (uint32_t e = 0; e <= n; ++e) rep_base[e] = h_nid[e];
+      return retry == 0;
+    };
+    dedup(size);
+    if (!read_bases()) {
+      ++B.table_retries;
+      SVDAG_CUDA(cudaMemsetAsync(d_retry.get(), 0, 4, st));
+      dedup(full);
+      read_bases();
     }
+    if (B.distinct_share.size() <= h) B.distinct_share.resize(h + 1, 0.0);
+    B.distinct_share[h] = std::max(B.distinct_share[h], double(rep_base[n]) / double(total));
     DBuf<uint64_t> d_rep_base(n, st);
     SVDAG_CUDA(cudaMemcpyAsync(d_rep_base.get(), rep_base.data(), 8ull * n, cudaMemcpyHostToDevice, st));
     const uint64_t nodes = rep_base[n];
@@ -1045,6 +1098,7 @@ int svdag_batch_get_stats(const svdag_batch* h, svdag_batch_stats* out) {
   out->dag_ms = h->b.dag_ms;
   out->reduce_ms = h->b.reduce_ms;
   out->gpu_launches = h->b.launches;
+  out->table_retries = h->b.table_retries;
   return SVDAG_OK;
 }
 

@@ -128,6 +128,12 @@ struct Batch {
   std::vector<cudaStream_t> streams;
   std::string last_error;
   double dag_ms = 0, reduce_ms = 0;
+  // Largest share of distinct keys among the cells of each height seen by
+  // earlier waves and builds (0 = none yet): later tables of that height are
+  // sized for twice that share; a table that proves too small is rebuilt at
+  // full size (table_retries counts those).
+  std::vector<double> distinct_share;
+  uint64_t table_retries = 0;
 };
 void batch_build_dags(Batch& B);
 void batch_reduce(Batch& B, bool sdag, bool csv);

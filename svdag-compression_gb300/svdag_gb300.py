@@ -137,7 +137,8 @@ class BatchTuning(ctypes.Structure):
 
 
 class _BatchStats(ctypes.Structure):
-    _fields_ = [("dag_ms", ctypes.c_double), ("reduce_ms", ctypes.c_double), ("gpu_launches", ctypes.c_uint64)]
+    _fields_ = [("dag_ms", ctypes.c_double), ("reduce_ms", ctypes.c_double), ("gpu_launches", ctypes.c_uint64),
+                ("table_retries", ctypes.c_uint64)]
 
 HOST_SYMBOLS = {
     "svdag_synth_icosphere_count": (_U64, [_U32]),
@@ -634,7 +635,7 @@ class Batch:
     def stats(self):
         s = _BatchStats()
         self._check(self._lib.svdag_batch_get_stats(self._h, ctypes.byref(s)))
-        return {"dag_ms": s.dag_ms, "reduce_ms": s.reduce_ms, "gpu_launches": s.gpu_launches}
+        return {k: getattr(s, k) for k, _ in _BatchStats._fields_}
 
 
 class Mlp:

@@ -91,3 +91,36 @@ def test_batch_settings_and_autotune_keep_results():
     for i in range(len(cs)):
         assert first_mismatch(B.result(i, "sdag").pool(), want[i]) is None
     assert B.stats()["gpu_launches"] > 0
+
+
+@pytest.mark.parametrize("share", ["1e-9", None])
+def test_estimated_tables_keep_results(monkeypatch, share):
+    """The per-height hash tables are sized from the distinct-key shares seen
+    by earlier builds; a table that proves too small is rebuilt at full size.
+    Forced tiny estimates (SVDAG_BATCH_TABLE_SHARE: the smallest table, 2^17
+    slots, against the distinct keys of a depth-10 chunk's lowest heights)
+    and the learned ones (second build) give the plain form's pools."""
+    cs = chunks(13, 6, depths=(4, 5, 6)) + [(10, sv.noise_bricks(10, 4242, 0.3)), (8, sv.noise_bricks(8, 4243, 0.12))]
+    want = []
+    for d, b in cs:
+        o = sv.Octree()
+        o.import_bricks(d, b)
+        o.toDAG()
+        s = o.clone()
+        s.toSDAG()
+        want.append((o.pool(), s.pool()))
+    if share is not None:
+        monkeypatch.setenv("SVDAG_BATCH_TABLE_SHARE", share)
+    B = sv.Batch()
+    for d, b in cs:
+        B.add_chunk(d, b)
+    for _ in range(2):
+        B.build(sdag=True, csvdag=False)
+        for i in range(len(cs)):
+            assert first_mismatch(B.result(i, "dag").pool(), want[i][0]) is None, i
+            assert first_mismatch(B.result(i, "sdag").pool(), want[i][1]) is None, i
+    retries = B.stats()["table_retries"]
+    if share is not None:
+        assert retries > 0
+    else:
+        assert retries == 0
