@@ -58,7 +58,7 @@ def parse():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--pixel-tolerance", type=float, default=1.0)
-    ap.add_argument("--top-k", type=int, default=256)
+    ap.add_argument("--top-k", type=int, default=384)
     ap.add_argument("--train-pairs", type=int, default=2000000)
     ap.add_argument("--epochs", type=int, default=2)
     ap.add_argument("--train-batch", type=int, default=4096)
