@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "svdag_gpu.h"
@@ -60,7 +61,35 @@ struct Exec {
   uint64_t* launches = nullptr;  // incremented once per kernel launch
   Profiler* prof = nullptr;      // non-null while kernel timing is enabled
   unsigned persistent_blocks = 0;  // cap on a persistent kernel's grid (0 = one block per SM)
+  // Launch with programmatic stream serialisation: the kernel may be
+  // scheduled while the previous kernel on the stream is still running; it
+  // must begin with pdl_wait() (which returns once that kernel has completed
+  // and its memory operations are visible) before touching global memory.
+  bool pdl = false;
 };
+
+// Programmatic dependent launch (sm_90+): the wait blocks until the grid this
+// one depends on has completed (a no-op for a grid launched without the
+// attribute); the trigger lets the next grid on the stream be scheduled once
+// every block of this one has issued it (or exited).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+template <class... KArgs, class... Args>
+inline cudaError_t launch_pdl(cudaStream_t st, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 // Grid for a grid-stride loop over n items.
 inline unsigned grid_for(const Exec& ex, uint64_t n, unsigned threads, unsigned per_sm = 16) {
@@ -79,7 +108,11 @@ inline unsigned grid_for(const Exec& ex, uint64_t n, unsigned threads, unsigned 
       b__ = p__->get();                                                  \
       SVDAG_CUDA(cudaEventRecord(a__, (ex).stream));                     \
     }                                                                    \
-    kernel<<<(grid), (block), (smem), (ex).stream>>>(__VA_ARGS__);       \
+    if ((ex).pdl)                                                        \
+      SVDAG_CUDA(::svdag::launch_pdl((ex).stream, kernel, dim3(grid),     \
+                                     dim3(block), (smem), __VA_ARGS__)); \
+    else                                                                 \
+      kernel<<<(grid), (block), (smem), (ex).stream>>>(__VA_ARGS__);     \
     if ((ex).launches) ++*(ex).launches;                                 \
     SVDAG_CUDA(cudaPeekAtLastError());                                   \
     if (p__) {                                                           \

@@ -136,6 +136,8 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(const __half* __restri
   using S = GemmShape<A_KM, B_NK, BM, BN, WGM>;
   constexpr int WM = S::WM, WN = S::WN, MI = S::MI, NI = S::NI, AC = S::AC, BC = S::BC;
   static_assert(MI >= 1 && NI >= 2 && NI % 2 == 0, "warp tile");
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __half* sA = reinterpret_cast<__half*>(smem_raw);
   __half* sB = sA + kStages * S::kA;
@@ -324,9 +326,14 @@ constexpr float kLossScale = 1024.f;
 
 // Siamese loss: rows [0, n) are side a, [n, 2n) side b of the embeddings.
 // pred = |e_a - e_b|^2, loss = mean (pred - t)^2; dE (x kLossScale, fp16)
-// written for both sides.
+// written for both sides.  `counter` (training graph): the step counter,
+// advanced here once the batch setup of this step has read it and before
+// Adam reads it.
 __global__ void k_pair_loss(const float* __restrict__ E, const float* __restrict__ t, int n, __half* __restrict__ dE,
-                            float* __restrict__ loss) {
+                            float* __restrict__ loss, unsigned long long* __restrict__ counter) {
+  pdl_wait();
+  pdl_trigger();
+  if (counter && blockIdx.x == 0 && threadIdx.x == 0) *counter += 1;
   for (int p = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); p < n; p += gridDim.x * (blockDim.x / 32)) {
     const int lane = threadIdx.x & 31;
     const float d0 = E[size_t(p) * kOut + lane] - E[size_t(p + n) * kOut + lane];
@@ -360,14 +367,17 @@ __global__ void k_adam(float* __restrict__ w, __half* __restrict__ wh, const flo
 }
 
 // Adam with the step number read from the device (training replays one
-// captured step graph): step = *counter + 1.
-__global__ void k_adam_dev(float* __restrict__ w, __half* __restrict__ wh, const float* __restrict__ g,
+// captured step graph; the loss kernel has already advanced the counter):
+// step = *counter.  The gradients are zeroed for the next step's
+// accumulation once read.
+__global__ void k_adam_dev(float* __restrict__ w, __half* __restrict__ wh, float* __restrict__ g,
                            float* __restrict__ m, float* __restrict__ v, size_t n, float lr, float b1, float b2,
                            const unsigned long long* __restrict__ counter) {
-  const float t = float(*counter + 1);
+  const float t = float(*counter);
   const float c1 = 1.f - powf(b1, t), c2 = 1.f - powf(b2, t);
   for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
     const float gi = g[i];
+    g[i] = 0.f;
     const float mi = b1 * m[i] + (1.f - b1) * gi;
     const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
     m[i] = mi;
@@ -407,18 +417,18 @@ __global__ void k_sample_pairs(const uint32_t* __restrict__ order, const uint32_
 }
 
 // Start of a replayed training step: batch (*counter mod batches) of the
-// epoch's rows and targets into the step's fixed buffers.
+// epoch's rows and targets into the step's fixed buffers, and the loss
+// accumulator zeroed.
 __global__ void k_batch_setup(const unsigned long long* __restrict__ counter, uint32_t batches, int B,
                               const uint32_t* __restrict__ rows_all, const float* __restrict__ t_all,
-                              uint32_t* __restrict__ rows, float* __restrict__ t) {
+                              uint32_t* __restrict__ rows, float* __restrict__ t, float* __restrict__ loss) {
   const uint64_t b = *counter % batches;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *loss = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * B; i += gridDim.x * blockDim.x) {
     rows[i] = rows_all[2 * b * B + i];
     if (i < B) t[i] = t_all[b * B + i];
   }
 }
-
-__global__ void k_step_advance(unsigned long long* counter) { *counter += 1; }
 
 // Candidate features: 512 cells, the fraction of set voxels in each cell's
 // Morton-aligned block (8 voxels per cell three levels above the leaves).
@@ -633,18 +643,28 @@ struct SideStream {
 // bias gradients are fused into the GEMMs that produce dH2 and dH1 (the
 // output bias's gradient is an exact zero: the two sides of every pair
 // contribute opposite terms), and the weight-gradient epilogues undo the
-// scale.  Every gradient is zeroed by one memset.  With `side`, the weight
-// gradients of layers 3 and 2 run on the side stream, beside dH2 and dH1.
+// scale.  Every gradient is zeroed by one memset -- or, inside the captured
+// training step (`counter` given), already zero (Adam zeroes them once read)
+// with the loss zeroed by the batch setup, and the loss kernel advances the
+// step counter.  With `side`, the weight gradients of layers 3 and 2 run on
+// the side stream, beside dH2 and dH1 (ordinary launches there: the
+// programmatic launches of ex.pdl chain kernels of one stream).
 void mlp_loss_grad(const Exec& ex, Mlp& net, MlpWork& W, const __half* X, const uint32_t* rowmap, int n,
-                   SideStream* side = nullptr) {
+                   SideStream* side = nullptr, unsigned long long* counter = nullptr) {
   const int rows = 2 * n;
   const float inv = 1.f / kLossScale;
   mlp_forward(ex, net, W, X, rowmap, rows);
-  SVDAG_CUDA(cudaMemsetAsync(W.loss.get(), 0, 4, ex.stream));
-  SVDAG_CUDA(cudaMemsetAsync(net.g.get(), 0, 4 * Mlp::total(), ex.stream));
-  SVDAG_LAUNCH(ex, k_pair_loss, grid_for(ex, n, 8), 256, 0, W.E.get(), W.t.get(), n, W.dE.get(), W.loss.get());
+  if (!counter) {
+    SVDAG_CUDA(cudaMemsetAsync(W.loss.get(), 0, 4, ex.stream));
+    SVDAG_CUDA(cudaMemsetAsync(net.g.get(), 0, 4 * Mlp::total(), ex.stream));
+  }
+  SVDAG_LAUNCH(ex, k_pair_loss, grid_for(ex, n, 8), 256, 0, W.E.get(), W.t.get(), n, W.dE.get(), W.loss.get(),
+               counter);
   Exec sx = ex;
-  if (side) sx.stream = side->stream;
+  if (side) {
+    sx.stream = side->stream;
+    sx.pdl = false;
+  }
   GemmOpts wg;  // weight gradients: split-K partial sums into the zeroed gradients, unscaled
   wg.alpha = inv;
   wg.zeroed = true;
@@ -779,9 +799,16 @@ struct LearnedProposer : LossyProposer {
     SVDAG_LAUNCH(ex, k_pair_target, grid_for(ex, np, 8, 16), 256, 0, S.bytes.get(), S.words, S.pop.get(), pairs.get(),
                  np, target.get());
     SVDAG_CUDA(cudaMemsetAsync(counter.get(), 0, 8, st));
+    SVDAG_CUDA(cudaMemsetAsync(net.g.get(), 0, 4 * Mlp::total(), st));  // then zeroed by Adam every step
     work.ensure(2 * B, st);
     Exec gx = ex;
     gx.prof = nullptr;  // no per-launch timing events inside a captured graph
+    // programmatic launches between the step's consecutive kernels on the
+    // stream (each waits for its predecessor with pdl_wait); the batch setup
+    // (the graph's first node) and Adam (after the side stream's join) launch
+    // ordinarily
+    Exec gp = gx;
+    gp.pdl = true;
     SideStream side;
     side.create();
     const uint64_t l0 = gx.launches ? *gx.launches : 0;
@@ -789,11 +816,10 @@ struct LearnedProposer : LossyProposer {
     SVDAG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     try {
       SVDAG_LAUNCH(gx, k_batch_setup, 32, 256, 0, counter.get(), uint32_t(batches), B, rows_all.get(), target.get(),
-                   rows.get(), work.t.get());
-      mlp_loss_grad(gx, net, work, X.get(), rows.get(), B, &side);
+                   rows.get(), work.t.get(), work.loss.get());
+      mlp_loss_grad(gp, net, work, X.get(), rows.get(), B, &side, counter.get());
       SVDAG_LAUNCH(gx, k_adam_dev, grid_for(gx, Mlp::total(), 256), 256, 0, net.w.get(), net.wh.get(), net.g.get(),
                    net.m.get(), net.v.get(), Mlp::total(), cfg.lr, 0.9f, 0.999f, counter.get());
-      SVDAG_LAUNCH(gx, k_step_advance, 1, 1, 0, counter.get());
     } catch (...) {
       cudaStreamEndCapture(st, &graph);
       if (graph) cudaGraphDestroy(graph);
