@@ -60,9 +60,9 @@ def parse():
     ap.add_argument("--pixel-tolerance", type=float, default=1.0)
     ap.add_argument("--top-k", type=int, default=384)
     ap.add_argument("--train-pairs", type=int, default=2000000)
-    ap.add_argument("--epochs", type=int, default=2)
-    ap.add_argument("--train-batch", type=int, default=4096)
-    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--epochs", type=int, default=1)
+    ap.add_argument("--train-batch", type=int, default=8192)
+    ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--chunks", type=int, default=256)
     ap.add_argument("--max-depth", type=int, default=11)
     ap.add_argument("--grid", type=int, default=None)

@@ -381,10 +381,10 @@ typedef struct svdag_lossy_params {
   uint32_t proposer;
   uint32_t top_k;            /* learned: proposals per candidate (0 = 16) */
   uint64_t train_pairs;      /* learned: training pairs (0 = 2,000,000) */
-  uint32_t train_epochs;     /* learned: passes over them (0 = 2) */
+  uint32_t train_epochs;     /* learned: passes over them (0 = 1) */
   uint64_t seed;
-  uint32_t train_batch;      /* learned: pairs per training step, a multiple of 64 in [256, 65536] (0 = 4096) */
-  float train_lr;            /* learned: Adam learning rate (0 = 1e-3) */
+  uint32_t train_batch;      /* learned: pairs per training step, a multiple of 64 in [256, 65536] (0 = 8192) */
+  float train_lr;            /* learned: Adam learning rate (0 = 2e-3) */
 } svdag_lossy_params;
 typedef struct svdag_lossy_stats {
   uint64_t nodes_before, nodes_after, candidates, pairs_evaluated, edges, merged;

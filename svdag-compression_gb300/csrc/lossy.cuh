@@ -11,10 +11,10 @@ struct LossyConfig {
   double max_error = 0.01;    // allowed voxel difference per replaced subtree (fraction of its cube's voxels)
   uint32_t top_k = 16;        // learned: proposals per candidate
   uint64_t train_pairs = 2000000;
-  uint32_t epochs = 2;
+  uint32_t epochs = 1;
   uint64_t seed = 1;
-  uint32_t train_batch = 4096;  // learned: pairs per training step
-  float lr = 1e-3f;             // learned: Adam learning rate
+  uint32_t train_batch = 8192;  // learned: pairs per training step
+  float lr = 2e-3f;             // learned: Adam learning rate
 };
 
 struct LossyResult {

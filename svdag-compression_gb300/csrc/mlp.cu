@@ -290,14 +290,18 @@ void launch_gemm(const Exec& ex, dim3 grid, const __half* A, const __half* B, Ou
 // Row-major A (M = batch rows, many tiles) uses 64-row tiles: twice the
 // blocks of 128-row ones, two of them resident per SM (the GEMMs are small
 // and latency-bound; ncu: one 8-warp block per SM left the tensor pipe busy
-// a quarter of the time).  K-major A (M = a layer width) keeps 128 rows and
+// a quarter of the time) -- unless 64-row tiles would need more than one
+// wave of two blocks per SM and 128-row ones would not (wide layers of
+// 16,384-row batches).  K-major A (M = a layer width) keeps 128 rows and
 // splits K instead.
 template <bool A_KM, bool B_NK, class OutT>
 void gemm_tc(const Exec& ex, const __half* A, const __half* B, OutT* C, int M, int N, int K,
              const GemmOpts& o = GemmOpts()) {
-  constexpr int BM = A_KM ? 128 : 64;
   const bool narrow = N <= 64;
   const int BN = narrow ? 64 : 128;
+  const int wave = 2 * ex.sm_count;
+  const bool tall = A_KM || (!narrow && (N / BN) * ((M + 63) / 64) > wave && (N / BN) * ((M + 127) / 128) <= wave);
+  const int BM = tall ? 128 : 64;
   // chunked dimensions (see k_gemm_tc) must be whole tiles
   if (N % BN || (A_KM && M % BM) || (!A_KM && K % kBK) || (B_NK && K % kBK))
     throw Error(SVDAG_ERR_INVALID_ARG, "gemm: unsupported shape");
@@ -314,6 +318,7 @@ void gemm_tc(const Exec& ex, const __half* A, const __half* B, OutT* C, int M, i
     else launch_gemm<A_KM, B_NK, 128, 128, 2, OutT>(ex, grid, A, B, C, M, N, K, k_per, o);
   } else {
     if (narrow) launch_gemm<A_KM, B_NK, 64, 64, 2, OutT>(ex, grid, A, B, C, M, N, K, k_per, o);
+    else if (tall) launch_gemm<A_KM, B_NK, 128, 128, 2, OutT>(ex, grid, A, B, C, M, N, K, k_per, o);
     else launch_gemm<A_KM, B_NK, 64, 128, 2, OutT>(ex, grid, A, B, C, M, N, K, k_per, o);
   }
 }
@@ -992,10 +997,10 @@ extern "C" int svdag_lossy_dag(svdag_ctx* h, const svdag_lossy_params* p, svdag_
     cfg.max_error = p->max_error;
     cfg.top_k = p->top_k ? p->top_k : 16;
     cfg.train_pairs = p->train_pairs ? p->train_pairs : 2000000;
-    cfg.epochs = p->train_epochs ? p->train_epochs : 2;
+    cfg.epochs = p->train_epochs ? p->train_epochs : 1;
     cfg.seed = p->seed;
-    cfg.train_batch = p->train_batch ? p->train_batch : 4096;
-    cfg.lr = p->train_lr > 0.f ? p->train_lr : 1e-3f;
+    cfg.train_batch = p->train_batch ? p->train_batch : 8192;
+    cfg.lr = p->train_lr > 0.f ? p->train_lr : 2e-3f;
     if (cfg.top_k > 512) throw svdag::Error(SVDAG_ERR_INVALID_ARG, "lossy: top_k above 512");
     if (cfg.train_batch % 64 || cfg.train_batch < 256 || cfg.train_batch > 65536)
       throw svdag::Error(SVDAG_ERR_INVALID_ARG, "lossy: train_batch must be a multiple of 64 in [256, 65536]");

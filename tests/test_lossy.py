@@ -40,13 +40,16 @@ def test_lossy_exact_matches_oracle(levels, grid, boxes):
     assert st["nodes_after"] == o.stats()["n_nodes"] < st["nodes_before"]
 
 
-def test_network_gradients_match_cpu_model():
+@pytest.mark.parametrize("pairs", [40, 8192])
+def test_network_gradients_match_cpu_model(pairs):
+    # 8192 pairs = 16,384 rows: the wide layers' row-major GEMMs take
+    # 128-row tiles (64-row ones would need more than one wave)
     m = sv.Mlp(seed=11)
     w = m.params()
     rng = np.random.default_rng(4)
-    xa = (rng.random((40, 512)) < 0.3).astype(np.float32)
-    xb = (rng.random((40, 512)) < 0.3).astype(np.float32)
-    t = rng.random(40).astype(np.float32)
+    xa = (rng.random((pairs, 512)) < 0.3).astype(np.float32)
+    xb = (rng.random((pairs, 512)) < 0.3).astype(np.float32)
+    t = rng.random(pairs).astype(np.float32)
     loss, g = m.loss_grad(xa, xb, t)
     rl, rg = mlp_ref.loss_grad(w, xa, xb, t)
     # tensor-core operands: fp16 (11-bit significands; the backward scaled
@@ -78,7 +81,8 @@ def test_training_beats_the_untrained_network():
     res = {}
     for kind in ("exact", "learned", "untrained"):
         o = base.clone()
-        res[kind] = o.lossy(kind, 3, 5, 0.01, top_k=8, train_pairs=200000, epochs=3, seed=2)
+        res[kind] = o.lossy(kind, 3, 5, 0.01, top_k=8, train_pairs=200000, epochs=3, seed=2, train_batch=4096,
+                             lr=1e-3)
     saved = {k: v["nodes_before"] - v["nodes_after"] for k, v in res.items()}
     assert saved["exact"] > 0
     # the same proposal budget per candidate (top_k): training finds more of
