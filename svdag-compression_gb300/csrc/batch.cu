@@ -317,6 +317,89 @@ __global__ void k_batch_insert(HeightView V, uint64_t total, unsigned long long*
   }
 }
 
+// Height 1 (cells of 8 bricks): within one entry (chunk), a brick's leaf DAG
+// id is a one-to-one function of its mask (the rank of the mask's first
+// occurrence), so two cells have equal keys exactly when they are cells of
+// the same entry with the same 8 brick bytes.  The key is therefore (entry,
+// 64-bit brick word): one load per cell, no rank lookups, and a probe that
+// meets a candidate confirms it with one load of the candidate's word.  The
+// representatives -- and so every id -- are the ones the general key gives.
+// The entry of a warp's cells is searched once per warp (lanes past its end
+// search for their own).
+__device__ __forceinline__ uint64_t brick_word(const HeightView& V, uint32_t e, uint64_t g) {
+  return reinterpret_cast<const uint64_t*>(V.bricks[e])[g - V.cells.base[e]];
+}
+
+__device__ __forceinline__ uint64_t h1_probe(const HeightView& V, uint64_t g, uint32_t e, uint64_t word, uint64_t hk,
+                                             unsigned long long* __restrict__ slots, uint64_t mask, uint64_t limit) {
+  const uint64_t tag = hk >> kGBits;
+  const unsigned long long mine = (tag << kGBits) | g;
+  const uint64_t lo = V.cells.base[e], hi = V.cells.base[e + 1];
+  uint64_t pos = hk & mask;
+  for (uint64_t probe = 0; probe <= limit; ++probe) {
+    unsigned long long cur = __ldcg(&slots[pos]);
+    if (cur == kEmpty64) {
+      const unsigned long long prev = atomicCAS(&slots[pos], kEmpty64, mine);
+      if (prev == kEmpty64) return pos;
+      cur = prev;
+    }
+    if ((cur >> kGBits) == tag) {
+      const uint64_t g2 = cur & kGMask;
+      // equal keys only within the entry: a candidate outside it differs
+      if (g2 >= lo && g2 < hi && brick_word(V, e, g2) == word) {
+        if (g < g2) atomicMin(&slots[pos], mine);
+        return pos;
+      }
+    }
+    pos = (pos + 1) & mask;
+  }
+  return ~0ull;
+}
+
+__global__ void k_batch_insert_h1(HeightView V, uint64_t total, unsigned long long* __restrict__ slots, uint64_t mask,
+                                  uint64_t limit, uint64_t* __restrict__ slot_of, int* err) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t warps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t w = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; (w << 5) < total; w += warps) {
+    if (limit < mask) {
+      // warp-uniform: every lane takes the flag lane 0 read
+      int stop = 0;
+      if (lane == 0) stop = *reinterpret_cast<volatile int*>(err);
+      if (__shfl_sync(0xFFFFFFFFu, stop, 0)) return;
+    }
+    const uint64_t g0 = w << 5, g = g0 + lane;
+    uint32_t e = 0;
+    if (lane == 0) e = chunk_of(V.cells, g0);
+    e = __shfl_sync(0xFFFFFFFFu, e, 0);
+    uint64_t word = 0;
+    bool part = false;
+    if (g < total) {
+      if (g >= V.cells.base[e + 1]) e = chunk_of(V.cells, g);
+      word = brick_word(V, e, g);
+      part = word != 0 || V.is_top[e];
+    }
+    const unsigned act = __ballot_sync(0xFFFFFFFFu, part);
+    if (!part) {
+      if (g < total) slot_of[g] = ~0ull;
+      continue;
+    }
+    const uint64_t hk = finish_hash(mix_word(mix_word(mix_word(0x3C6EF372FE94F82Bull, e), uint32_t(word)),
+                                             uint32_t(word >> 32)));
+    // lanes with the same (entry, word) probe once, through the lowest
+    const unsigned grp = __match_any_sync(act, hk);
+    const int lead = __ffs(int(grp)) - 1;
+    const uint32_t le = __shfl_sync(act, e, lead);  // both shuffles on every active lane
+    const uint64_t lw = __shfl_sync(act, word, lead);
+    const bool same = le == e && lw == word;
+    uint64_t pos = 0;
+    if (int(lane) == lead) pos = h1_probe(V, g, e, word, hk, slots, mask, limit);
+    const uint64_t lpos = __shfl_sync(act, pos, lead);
+    if (int(lane) != lead) pos = same ? lpos : h1_probe(V, g, e, word, hk, slots, mask, limit);
+    if (pos == ~0ull) atomicExch(err, 1);
+    slot_of[g] = pos;
+  }
+}
+
 // The representative (smallest index with the same key) of every non-empty
 // cell: the index its slot holds once every insert is done.  Nothing to do
 // when an insert into an estimated table gave up (retry non-null and set:
@@ -625,9 +708,14 @@ void build_wave(Batch& B, const std::vector<uint32_t>& sel) {
       const bool bounded = tsize < full;
       DBuf<unsigned long long> slots(tsize, st);
       SVDAG_CUDA(cudaMemsetAsync(slots.get(), 0xFF, 8 * tsize, st));
-      SVDAG_LAUNCH(ex, k_batch_insert, grid_for(ex, total, tb, 8), tb, 0, V, total, slots.get(), tsize - 1,
-                   bounded ? std::min<uint64_t>(kProbeLimit, tsize - 1) : tsize - 1, rep.get(),
-                   bounded ? d_retry.get() : d_err.get());
+      const uint64_t lim = bounded ? std::min<uint64_t>(kProbeLimit, tsize - 1) : tsize - 1;
+      int* flag = bounded ? d_retry.get() : d_err.get();
+      if (h == 1)
+        SVDAG_LAUNCH(ex, k_batch_insert_h1, grid_for(ex, total, tb, 8), tb, 0, V, total, slots.get(), tsize - 1, lim,
+                     rep.get(), flag);
+      else
+        SVDAG_LAUNCH(ex, k_batch_insert, grid_for(ex, total, tb, 8), tb, 0, V, total, slots.get(), tsize - 1, lim,
+                     rep.get(), flag);
       SVDAG_LAUNCH(ex, k_batch_rep, grid_for(ex, total, tb, 8), tb, 0, total, slots.get(), tsize - 1,
                    bounded ? d_retry.get() : nullptr, rep.get());
       slots.release();
