@@ -852,7 +852,12 @@ def run_batch(args, rank, local, world):
     t0 = time.perf_counter()
     stage = {"dag_ms": 0.0, "reduce_ms": 0.0}
     for _ in range(args.steps):
+        # an NVTX range per timed build, so that a profiler can be limited to
+        # it (ncu --nvtx --nvtx-include "batch_build/"; ranges are per host
+        # thread: the reduction workers' launches fall outside)
+        torch.cuda.nvtx.range_push("batch_build")
         B.build()
+        torch.cuda.nvtx.range_pop()
         st = B.stats()
         stage["dag_ms"] += st["dag_ms"]
         stage["reduce_ms"] += st["reduce_ms"]
