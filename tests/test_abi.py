@@ -1,8 +1,10 @@
 """The C-ABI library loads and exports every entry point include/svdag_gpu.h
-declares (no compute without a GPU)."""
+declares (no compute without a GPU), and the Python mirrors of its structs
+have the header's layout."""
 import ctypes
 import os
 import re
+import subprocess
 
 import svdag_gb300 as sv
 
@@ -67,3 +69,44 @@ def test_create_fails_loudly_without_device():
     h = ctypes.c_void_p()
     assert sv.load_gpu().svdag_create(ctypes.byref(h), 0, None) == 7  # SVDAG_ERR_NO_DEVICE
     assert not h.value
+
+
+# (header struct, its Python mirror) -- a mismatch would make the library
+# read or write past the Python object
+STRUCTS = [("svdag_stats", sv._Stats), ("svdag_lossy_params", sv.LossyParams),
+           ("svdag_lossy_stats", sv._LossyStats), ("svdag_batch_tuning", sv.BatchTuning),
+           ("svdag_batch_stats", sv._BatchStats), ("svdag_camera", sv._Camera)]
+
+
+def c_layouts(tmp_path):
+    """sizeof and every field's offsetof, as a C compiler lays the header's
+    structs out."""
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "svdag_gpu.h"', "int main(void) {"]
+    for name, py in STRUCTS:
+        lines.append('  printf("%s size %%zu\\n", sizeof(%s));' % (name, name))
+        for f, _ in py._fields_:
+            lines.append('  printf("%s %s %%zu\\n", offsetof(%s, %s));' % (name, f, name, f))
+    lines.append('  printf("svdag_ray_hit size %zu\\n", sizeof(svdag_ray_hit));')
+    for f in sv.HIT.names:
+        lines.append('  printf("svdag_ray_hit %s %%zu\\n", offsetof(svdag_ray_hit, %s));' % (f, f))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        s, f, v = line.split()
+        out[(s, f)] = int(v)
+    return out
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    c = c_layouts(tmp_path)
+    for name, py in STRUCTS:
+        assert c[(name, "size")] == ctypes.sizeof(py), name
+        for f, _ in py._fields_:
+            assert c[(name, f)] == getattr(py, f).offset, (name, f)
+    assert c[("svdag_ray_hit", "size")] == sv.HIT.itemsize
+    for f in sv.HIT.names:
+        assert c[("svdag_ray_hit", f)] == sv.HIT.fields[f][1], f
