@@ -379,7 +379,7 @@ typedef struct svdag_lossy_params {
   uint32_t levels_above_max; /* 5 */
   double max_error;          /* 0.01 */
   uint32_t proposer;
-  uint32_t top_k;            /* learned: proposals per candidate (0 = 16) */
+  uint32_t top_k;            /* learned: proposals per candidate, at most 512 (0 = 384) */
   uint64_t train_pairs;      /* learned: training pairs (0 = 2,000,000) */
   uint32_t train_epochs;     /* learned: passes over them (0 = 1) */
   uint64_t seed;

@@ -9,7 +9,7 @@ struct LossyConfig {
   uint32_t min_above = 3;     // candidate levels L-1-max_above .. L-1-min_above
   uint32_t max_above = 5;
   double max_error = 0.01;    // allowed voxel difference per replaced subtree (fraction of its cube's voxels)
-  uint32_t top_k = 16;        // learned: proposals per candidate
+  uint32_t top_k = 384;       // learned: proposals per candidate
   uint64_t train_pairs = 2000000;
   uint32_t epochs = 1;
   uint64_t seed = 1;

@@ -995,7 +995,7 @@ extern "C" int svdag_lossy_dag(svdag_ctx* h, const svdag_lossy_params* p, svdag_
     cfg.min_above = p->levels_above_min;
     cfg.max_above = p->levels_above_max;
     cfg.max_error = p->max_error;
-    cfg.top_k = p->top_k ? p->top_k : 16;
+    cfg.top_k = p->top_k ? p->top_k : 384;
     cfg.train_pairs = p->train_pairs ? p->train_pairs : 2000000;
     cfg.epochs = p->train_epochs ? p->train_epochs : 1;
     cfg.seed = p->seed;

@@ -426,7 +426,7 @@ class Octree:
 
     LOSSY = {"exact": 0, "learned": 1, "untrained": 2}
 
-    def lossy(self, proposer="exact", min_above=3, max_above=5, max_error=0.01, top_k=16, train_pairs=0,
+    def lossy(self, proposer="exact", min_above=3, max_above=5, max_error=0.01, top_k=0, train_pairs=0,
               epochs=0, seed=1, train_batch=0, lr=0.0):
         """Lossy LSVDAG on a DAG (svdag_lossy_dag); returns its statistics."""
         p = LossyParams(min_above, max_above, max_error, self.LOSSY[proposer], top_k, train_pairs, epochs, seed,
