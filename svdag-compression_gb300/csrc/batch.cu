@@ -401,41 +401,70 @@ __global__ void k_batch_insert_h1(HeightView V, uint64_t total, unsigned long lo
 }
 
 // The representative (smallest index with the same key) of every non-empty
-// cell: the index its slot holds once every insert is done.  Nothing to do
-// when an insert into an estimated table gave up (retry non-null and set:
-// slot_of is incomplete and the height is redone).
+// cell: the index its slot holds once every insert is done; and one bit per
+// cell, set for the representatives (bit g & 31 of word g >> 5, one word per
+// warp by ballot).  Nothing to do when an insert into an estimated table gave
+// up (retry non-null and set: slot_of is incomplete and the height is
+// redone).
 __global__ void k_batch_rep(uint64_t total, const unsigned long long* __restrict__ slots, uint64_t mask,
-                            const int* __restrict__ retry, uint64_t* __restrict__ rep) {
+                            const int* __restrict__ retry, uint64_t* __restrict__ rep, uint32_t* __restrict__ flags) {
   if (retry && *retry) return;
-  for (uint64_t g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; g < total; g += uint64_t(gridDim.x) * blockDim.x) {
-    const uint64_t p = rep[g];
-    rep[g] = p > mask ? ~0ull : (slots[p] & kGMask);
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t warps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t w = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; (w << 5) < total; w += warps) {
+    const uint64_t g = (w << 5) + lane;
+    bool own = false;
+    if (g < total) {
+      const uint64_t p = rep[g];
+      const uint64_t r = p > mask ? ~0ull : (slots[p] & kGMask);
+      rep[g] = r;
+      own = r == g;
+    }
+    const unsigned b = __ballot_sync(0xFFFFFFFFu, own);
+    if (lane == 0) flags[w] = b;
   }
 }
 
-struct RepIn {
-  const uint64_t* rep;
-  __device__ __forceinline__ uint32_t operator()(uint64_t g) const { return rep[g] == g ? 1u : 0u; }
+struct FlagPopc {
+  const uint32_t* w;
+  __device__ __forceinline__ uint32_t operator()(uint64_t i) const { return __popc(w[i]); }
 };
 struct U32Out {
   uint32_t* a;
   __device__ __forceinline__ void operator()(uint64_t i, uint32_t v) const { a[i] = v; }
 };
 
+// Number of representatives before cell g (woff: exclusive prefix of the
+// flag words' popcounts): a representative's node number in the wave.
+__device__ __forceinline__ uint32_t flag_rank(const uint32_t* __restrict__ flags, const uint32_t* __restrict__ woff,
+                                              uint64_t g) {
+  const uint64_t w = g >> 5;
+  return woff[w] + uint32_t(__popc(flags[w] & ((1u << (g & 31u)) - 1u)));
+}
+
+// Node number of each entry's first cell (the entry's DAG nodes are the
+// numbers from there to the next entry's), and the wave's total.
+__global__ void k_entry_bases(uint32_t n, const uint64_t* __restrict__ base, const uint32_t* __restrict__ flags,
+                              const uint32_t* __restrict__ woff, const uint32_t* __restrict__ d_total,
+                              uint32_t* __restrict__ out) {
+  for (uint32_t e = threadIdx.x; e <= n; e += blockDim.x) out[e] = e < n ? flag_rank(flags, woff, base[e]) : *d_total;
+}
+
 // DAG id (within the chunk) of every cell, and the DAG nodes of this height
 // (node numbers of a wave fit 32 bits: a wave has at most 2^30 cells).
 __global__ void k_batch_emit(HeightView V, uint64_t total, const uint64_t* __restrict__ rep,
-                             const uint32_t* __restrict__ newid, const uint64_t* __restrict__ rep_base,
-                             uint32_t* __restrict__ ids_out, uint32_t* __restrict__ hdr, uint32_t* __restrict__ ch) {
+                             const uint32_t* __restrict__ flags, const uint32_t* __restrict__ woff,
+                             const uint64_t* __restrict__ rep_base, uint32_t* __restrict__ ids_out,
+                             uint32_t* __restrict__ hdr, uint32_t* __restrict__ ch) {
   for (uint64_t g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; g < total; g += uint64_t(gridDim.x) * blockDim.x) {
     const uint64_t r = rep[g];
     if (r == ~0ull) { ids_out[g] = kNone; continue; }
     const uint32_t e = chunk_of(V.cells, g);
-    ids_out[g] = uint32_t(newid[r] - rep_base[e]);
+    const uint32_t id = flag_rank(flags, woff, r);
+    ids_out[g] = uint32_t(id - rep_base[e]);
     if (r == g) {
       uint32_t e2, ids[8];
       const uint32_t m = cell_key(V, g, e2, ids);
-      const uint64_t id = newid[g];
       hdr[id] = m;
       store_children(ch, id, ids);
     }
@@ -702,8 +731,9 @@ void build_wave(Batch& B, const std::vector<uint32_t>& sel) {
       size = std::min(full, next_pow2(uint64_t(keys * B.tuning.table_factor)));
     }
     DBuf<uint64_t> rep(total, st);
-    DBuf<uint32_t> newid(total, st);
-    DBuf<uint32_t> d_total(1, st);
+    const uint64_t words = (total + 31) / 32;
+    DBuf<uint32_t> flags(words, st), woff(words, st);
+    DBuf<uint32_t> d_total(1, st), d_bases(n + 1, st);
     auto dedup = [&](uint64_t tsize) {
       const bool bounded = tsize < full;
       DBuf<unsigned long long> slots(tsize, st);
@@ -717,19 +747,20 @@ void build_wave(Batch& B, const std::vector<uint32_t>& sel) {
         SVDAG_LAUNCH(ex, k_batch_insert, grid_for(ex, total, tb, 8), tb, 0, V, total, slots.get(), tsize - 1, lim,
                      rep.get(), flag);
       SVDAG_LAUNCH(ex, k_batch_rep, grid_for(ex, total, tb, 8), tb, 0, total, slots.get(), tsize - 1,
-                   bounded ? d_retry.get() : nullptr, rep.get());
+                   bounded ? d_retry.get() : nullptr, rep.get(), flags.get());
       slots.release();
-      device_exclusive_scan<uint32_t>(ex, RepIn{rep.get()}, total, U32Out{newid.get()}, d_total.get());
+      // node numbers: a scan over the flag words' popcounts (32 cells each)
+      device_exclusive_scan<uint32_t>(ex, FlagPopc{flags.get()}, words, U32Out{woff.get()}, d_total.get());
+      SVDAG_LAUNCH(ex, k_entry_bases, 1, 256, 0, n, d_base.get(), flags.get(), woff.get(), d_total.get(),
+                   d_bases.get());
     };
-    // DAG nodes of each entry: newid range [newid at its first cell, next
-    // entry's); read together with the retry flag (one synchronisation)
+    // DAG nodes of each entry: the node numbers from its first cell's to the
+    // next entry's; read together with the retry flag (one synchronisation)
     std::vector<uint64_t> rep_base(n + 1);
     auto read_bases = [&]() -> bool {
       std::vector<uint32_t> h_nid(n + 1);
       int retry = 0;
-      for (uint32_t e = 0; e < n; ++e)
-        SVDAG_CUDA(cudaMemcpyAsync(&h_nid[e], newid.get() + base[e], 4, cudaMemcpyDeviceToHost, st));
-      SVDAG_CUDA(cudaMemcpyAsync(&h_nid[n], d_total.get(), 4, cudaMemcpyDeviceToHost, st));
+      SVDAG_CUDA(cudaMemcpyAsync(h_nid.data(), d_bases.get(), 4ull * (n + 1), cudaMemcpyDeviceToHost, st));
       SVDAG_CUDA(cudaMemcpyAsync(&retry, d_retry.get(), 4, cudaMemcpyDeviceToHost, st));
       SVDAG_CUDA(cudaStreamSynchronize(st));
       for (uint32_t e = 0; e <= n; ++e) rep_base[e] = h_nid[e];
@@ -748,7 +779,7 @@ void build_wave(Batch& B, const std::vector<uint32_t>& sel) {
     SVDAG_CUDA(cudaMemcpyAsync(d_rep_base.get(), rep_base.data(), 8ull * n, cudaMemcpyHostToDevice, st));
     const uint64_t nodes = rep_base[n];
     DBuf<uint32_t> hdr(nodes ? nodes : 1, st), ch(8 * (nodes ? nodes : 1), st), ids(total, st);
-    SVDAG_LAUNCH(ex, k_batch_emit, grid_for(ex, total, tb, 8), tb, 0, V, total, rep.get(), newid.get(),
+    SVDAG_LAUNCH(ex, k_batch_emit, grid_for(ex, total, tb, 8), tb, 0, V, total, rep.get(), flags.get(), woff.get(),
                  d_rep_base.get(), ids.get(), hdr.get(), ch.get());
     // hand each entry its level
     for (uint32_t e = 0; e < n; ++e) {
