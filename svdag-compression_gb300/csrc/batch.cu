@@ -19,8 +19,13 @@
 // its key (mask, DAG ids of its 8 children) in one hash table shared by all
 // chunks, with the chunk id in the key; equal keys converge on the smallest
 // global cell index, i.e. the first occurrence within their chunk.  One
-// launch per step covers every chunk of a height.  The DAGs then go through
-// toSDAG and the cross-level merge per chunk, on several streams at once.
+// launch per step covers every chunk of a height.  One height above the
+// leaves the key is the equivalent (chunk, 8 brick bytes) (k_batch_insert_h1);
+// each height's table is sized from the share of distinct keys earlier waves
+// saw there, and rebuilt at full size when that proves too small; the
+// representatives are numbered from one flag bit per cell.  The DAGs then go
+// through toSDAG and the cross-level merge per chunk, on several streams at
+// once.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
