@@ -238,6 +238,9 @@ constexpr uint64_t kGMask = (1ull << kGBits) - 1;
 // Probes after which an insert into a table sized from an estimate gives up
 // (the table is then rebuilt at full size).
 constexpr uint64_t kProbeLimit = 512;
+// Largest table (slot positions and the kNone mark fit 32 bits; a height of
+// 2^30 cells -- a wave's largest -- still loads it at most half).
+constexpr uint64_t kMaxTableSlots = 1ull << 31;
 
 // Probe for the key of cell g; returns its slot (inserted, or found holding
 // an equal key, lowered to g when g is smaller), or ~0 when `limit` + 1 slots
@@ -281,7 +284,7 @@ __device__ __forceinline__ uint64_t batch_probe(const HeightView& V, uint64_t g,
 // A probe that gives up sets *err; with limit < mask (a table sized from an
 // estimate) the other warps then stop early, as the insert will be redone.
 __global__ void k_batch_insert(HeightView V, uint64_t total, unsigned long long* __restrict__ slots, uint64_t mask,
-                               uint64_t limit, uint64_t* __restrict__ slot_of, int* err) {
+                               uint64_t limit, uint32_t* __restrict__ slot_of, int* err) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint64_t warps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
   for (uint64_t w = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; (w << 5) < total; w += warps) {
@@ -300,7 +303,7 @@ __global__ void k_batch_insert(HeightView V, uint64_t total, unsigned long long*
     }
     const unsigned act = __ballot_sync(0xFFFFFFFFu, part);
     if (!part) {
-      if (g < total) slot_of[g] = ~0ull;
+      if (g < total) slot_of[g] = kNone;
       continue;
     }
     const uint32_t chunk = V.part[e];
@@ -318,7 +321,7 @@ __global__ void k_batch_insert(HeightView V, uint64_t total, unsigned long long*
     const uint64_t lpos = __shfl_sync(act, pos, lead);
     if (int(lane) != lead) pos = same ? lpos : batch_probe(V, g, chunk, m, ids, hk, slots, mask, limit);
     if (pos == ~0ull) atomicExch(err, 1);
-    slot_of[g] = pos;
+    slot_of[g] = pos == ~0ull ? kNone : uint32_t(pos);
   }
 }
 
@@ -362,7 +365,7 @@ __device__ __forceinline__ uint64_t h1_probe(const HeightView& V, uint64_t g, ui
 }
 
 __global__ void k_batch_insert_h1(HeightView V, uint64_t total, unsigned long long* __restrict__ slots, uint64_t mask,
-                                  uint64_t limit, uint64_t* __restrict__ slot_of, int* err) {
+                                  uint64_t limit, uint32_t* __restrict__ slot_of, int* err) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint64_t warps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
   for (uint64_t w = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; (w << 5) < total; w += warps) {
@@ -385,7 +388,7 @@ __global__ void k_batch_insert_h1(HeightView V, uint64_t total, unsigned long lo
     }
     const unsigned act = __ballot_sync(0xFFFFFFFFu, part);
     if (!part) {
-      if (g < total) slot_of[g] = ~0ull;
+      if (g < total) slot_of[g] = kNone;
       continue;
     }
     const uint64_t hk = finish_hash(mix_word(mix_word(mix_word(0x3C6EF372FE94F82Bull, e), uint32_t(word)),
@@ -401,7 +404,7 @@ __global__ void k_batch_insert_h1(HeightView V, uint64_t total, unsigned long lo
     const uint64_t lpos = __shfl_sync(act, pos, lead);
     if (int(lane) != lead) pos = same ? lpos : h1_probe(V, g, e, word, hk, slots, mask, limit);
     if (pos == ~0ull) atomicExch(err, 1);
-    slot_of[g] = pos;
+    slot_of[g] = pos == ~0ull ? kNone : uint32_t(pos);
   }
 }
 
@@ -412,7 +415,7 @@ __global__ void k_batch_insert_h1(HeightView V, uint64_t total, unsigned long lo
 // up (retry non-null and set: slot_of is incomplete and the height is
 // redone).
 __global__ void k_batch_rep(uint64_t total, const unsigned long long* __restrict__ slots, uint64_t mask,
-                            const int* __restrict__ retry, uint64_t* __restrict__ rep, uint32_t* __restrict__ flags) {
+                            const int* __restrict__ retry, uint32_t* __restrict__ rep, uint32_t* __restrict__ flags) {
   if (retry && *retry) return;
   const uint32_t lane = threadIdx.x & 31u;
   const uint64_t warps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
@@ -420,8 +423,8 @@ __global__ void k_batch_rep(uint64_t total, const unsigned long long* __restrict
     const uint64_t g = (w << 5) + lane;
     bool own = false;
     if (g < total) {
-      const uint64_t p = rep[g];
-      const uint64_t r = p > mask ? ~0ull : (slots[p] & kGMask);
+      const uint32_t p = rep[g];
+      const uint32_t r = p > mask ? kNone : uint32_t(slots[p] & kGMask);
       rep[g] = r;
       own = r == g;
     }
@@ -457,13 +460,13 @@ __global__ void k_entry_bases(uint32_t n, const uint64_t* __restrict__ base, con
 
 // DAG id (within the chunk) of every cell, and the DAG nodes of this height
 // (node numbers of a wave fit 32 bits: a wave has at most 2^30 cells).
-__global__ void k_batch_emit(HeightView V, uint64_t total, const uint64_t* __restrict__ rep,
+__global__ void k_batch_emit(HeightView V, uint64_t total, const uint32_t* __restrict__ rep,
                              const uint32_t* __restrict__ flags, const uint32_t* __restrict__ woff,
                              const uint64_t* __restrict__ rep_base, uint32_t* __restrict__ ids_out,
                              uint32_t* __restrict__ hdr, uint32_t* __restrict__ ch) {
   for (uint64_t g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; g < total; g += uint64_t(gridDim.x) * blockDim.x) {
-    const uint64_t r = rep[g];
-    if (r == ~0ull) { ids_out[g] = kNone; continue; }
+    const uint32_t r = rep[g];
+    if (r == kNone) { ids_out[g] = kNone; continue; }
     const uint32_t e = chunk_of(V.cells, g);
     const uint32_t id = flag_rank(flags, woff, r);
     ids_out[g] = uint32_t(id - rep_base[e]);
@@ -492,6 +495,14 @@ __global__ void k_batch_leaf_first(const uint8_t* const* __restrict__ bricks, co
     const uint64_t w = w8[i];
     if (!w) continue;
     s += __popcll(w);
+    const uint32_t m0 = uint32_t(w) & 0xFFu;
+    if (w == uint64_t(m0) * 0x0101010101010101ull) {
+      // 8 equal bricks (solid or repeated regions): only the first can be a
+      // first occurrence
+      const uint32_t at = uint32_t(8 * i);
+      if (sf[m0] > at) atomicMin(&sf[m0], at);
+      continue;
+    }
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       const uint32_t m = uint32_t(w >> (8 * k)) & 0xFFu;
@@ -728,14 +739,18 @@ void build_wave(Batch& B, const std::vector<uint32_t>& sel) {
     // redone with the full-size table.
     const unsigned tb = B.tuning.threads;
     if (total >= (1ull << 32)) throw Error(SVDAG_ERR_OVERFLOW, "batch: more than 2^32 cells on one height");
-    const uint64_t full = next_pow2(uint64_t(double(std::max<uint64_t>(total, 16)) * B.tuning.table_factor));
+    const uint64_t full = std::min<uint64_t>(
+        kMaxTableSlots, next_pow2(uint64_t(double(std::max<uint64_t>(total, 16)) * B.tuning.table_factor)));
     const double share = share_env > 0 ? share_env : (h < B.distinct_share.size() ? B.distinct_share[h] : 0.0);
     uint64_t size = full;
     if (share > 0) {
       const double keys = std::max(2.0 * share * double(total), 65536.0);
       size = std::min(full, next_pow2(uint64_t(keys * B.tuning.table_factor)));
     }
-    DBuf<uint64_t> rep(total, st);
+    // the slot of each cell's key, then its representative (kNone: empty
+    // cell), in 32 bits: cell indices of a height are below 2^32 (checked
+    // above) and tables are capped at 2^31 slots
+    DBuf<uint32_t> rep(total, st);
     const uint64_t words = (total + 31) / 32;
     DBuf<uint32_t> flags(words, st), woff(words, st);
     DBuf<uint32_t> d_total(1, st), d_bases(n + 1, st);
