@@ -458,23 +458,24 @@ __global__ void k_entry_bases(uint32_t n, const uint64_t* __restrict__ base, con
   for (uint32_t e = threadIdx.x; e <= n; e += blockDim.x) out[e] = e < n ? flag_rank(flags, woff, base[e]) : *d_total;
 }
 
-// DAG id (within the chunk) of every cell, and the DAG nodes of this height
+// DAG id (within the chunk) of every cell, and the DAG nodes of this height,
+// written straight into each entry's own level buffers (hdr_e[e], ch_e[e])
 // (node numbers of a wave fit 32 bits: a wave has at most 2^30 cells).
 __global__ void k_batch_emit(HeightView V, uint64_t total, const uint32_t* __restrict__ rep,
                              const uint32_t* __restrict__ flags, const uint32_t* __restrict__ woff,
                              const uint64_t* __restrict__ rep_base, uint32_t* __restrict__ ids_out,
-                             uint32_t* __restrict__ hdr, uint32_t* __restrict__ ch) {
+                             uint32_t* const* __restrict__ hdr_e, uint32_t* const* __restrict__ ch_e) {
   for (uint64_t g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; g < total; g += uint64_t(gridDim.x) * blockDim.x) {
     const uint32_t r = rep[g];
     if (r == kNone) { ids_out[g] = kNone; continue; }
     const uint32_t e = chunk_of(V.cells, g);
-    const uint32_t id = flag_rank(flags, woff, r);
-    ids_out[g] = uint32_t(id - rep_base[e]);
+    const uint32_t id = uint32_t(flag_rank(flags, woff, r) - rep_base[e]);
+    ids_out[g] = id;
     if (r == g) {
       uint32_t e2, ids[8];
       const uint32_t m = cell_key(V, g, e2, ids);
-      hdr[id] = m;
-      store_children(ch, id, ids);
+      hdr_e[e][id] = m;
+      store_children(ch_e[e], id, ids);
     }
   }
 }
@@ -797,11 +798,9 @@ void build_wave(Batch& B, const std::vector<uint32_t>& sel) {
     B.distinct_share[h] = std::max(B.distinct_share[h], double(rep_base[n]) / double(total));
     DBuf<uint64_t> d_rep_base(n, st);
     SVDAG_CUDA(cudaMemcpyAsync(d_rep_base.get(), rep_base.data(), 8ull * n, cudaMemcpyHostToDevice, st));
-    const uint64_t nodes = rep_base[n];
-    DBuf<uint32_t> hdr(nodes ? nodes : 1, st), ch(8 * (nodes ? nodes : 1), st), ids(total, st);
-    SVDAG_LAUNCH(ex, k_batch_emit, grid_for(ex, total, tb, 8), tb, 0, V, total, rep.get(), flags.get(), woff.get(),
-                 d_rep_base.get(), ids.get(), hdr.get(), ch.get());
-    // hand each entry its level
+    // each entry's level, sized now that its node count is known; the emit
+    // kernel fills them in place
+    std::vector<uint32_t*> h_hdr(n), h_ch(n);
     for (uint32_t e = 0; e < n; ++e) {
       const uint32_t c = part[e];
       Ctx& X = RES(c).dag->c;
@@ -809,11 +808,15 @@ void build_wave(Batch& B, const std::vector<uint32_t>& sel) {
       L.n = rep_base[e + 1] - rep_base[e];
       L.hdr.alloc(L.n ? L.n : 1, st);
       L.ch.alloc(8 * (L.n ? L.n : 1), st);
-      if (L.n) {
-        SVDAG_CUDA(cudaMemcpyAsync(L.hdr.get(), hdr.get() + rep_base[e], 4 * L.n, cudaMemcpyDeviceToDevice, st));
-        SVDAG_CUDA(cudaMemcpyAsync(L.ch.get(), ch.get() + 8 * rep_base[e], 32 * L.n, cudaMemcpyDeviceToDevice, st));
-      }
+      h_hdr[e] = L.hdr.get();
+      h_ch[e] = L.ch.get();
     }
+    DBuf<uint32_t*> d_hdr(n, st), d_ch(n, st);
+    SVDAG_CUDA(cudaMemcpyAsync(d_hdr.get(), h_hdr.data(), sizeof(uint32_t*) * n, cudaMemcpyHostToDevice, st));
+    SVDAG_CUDA(cudaMemcpyAsync(d_ch.get(), h_ch.data(), sizeof(uint32_t*) * n, cudaMemcpyHostToDevice, st));
+    DBuf<uint32_t> ids(total, st);
+    SVDAG_LAUNCH(ex, k_batch_emit, grid_for(ex, total, tb, 8), tb, 0, V, total, rep.get(), flags.get(), woff.get(),
+                 d_rep_base.get(), ids.get(), d_hdr.get(), d_ch.get());
     below_ids = std::move(ids);
     below_base_h.assign(base.begin(), base.end() - 1);
     below_part = part;
