@@ -830,16 +830,12 @@ def run_batch(args, rank, local, world):
               for i, (d, f) in enumerate(zip(depths, fills))]
     in_bytes = sum(b.numel() for b in bricks)
     B = sv.Batch(device=local)
-    # settings: autotuned on a sample of the chunks (every 8th), untimed
-    T = sv.Batch(device=local)
-    for i in range(0, args.chunks, 8):
-        T.add_chunk(int(depths[i]), bricks[i])
-    T.autotune(max_trials=10)
-    tune = T.tuning()
-    T.close()
-    B.set_tuning(**tune)
     for d, b in zip(depths, bricks):
         B.add_chunk(int(d), b)
+    # settings: autotuned on the batch itself (full builds, untimed; a sample
+    # of every 8th chunk picked 2 or 4 reduction streams from run to run)
+    B.autotune(max_trials=10)
+    tune = B.tuning()
     for _ in range(max(args.warmup, 0)):
         B.build()
     voxels = sum(B.result(i, "dag").stats()["n_total_voxels"] for i in range(args.chunks))
