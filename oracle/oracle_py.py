@@ -45,6 +45,7 @@ _SIGS = {
     "ora_get_outside": (_I, [_VP, _U32, _VP]),
     "ora_to_dag": (_I, [_VP]),
     "ora_to_sdag": (_I, [_VP]),
+    "ora_to_sdag_ex": (_I, [_VP, _I]),
     "ora_init_child_levels": (_I, [_VP]),
     "ora_merge_across_levels": (_I, [_VP]),
     "ora_level_count": (_U64, [_VP, _U32]),
@@ -161,8 +162,8 @@ class OracleOctree:
     def toDAG(self):
         assert self.L.ora_to_dag(self.h) == 0
 
-    def toSDAG(self):
-        assert self.L.ora_to_sdag(self.h) == 0
+    def toSDAG(self, skip_symmetry=False):
+        assert self.L.ora_to_sdag_ex(self.h, 1 if skip_symmetry else 0) == 0
 
     def initChildLevels(self):
         assert self.L.ora_init_child_levels(self.h) == 0

@@ -24,6 +24,11 @@
 //                     before it runs the external MCL program as
 //                     $HOME/local/bin/mcl (cluster.hpp:134-192), which the
 //                     caller provides
+//   --sdag-skip       <out_prefix>.sdagskip.pool: GeomOctree::toSDAG(true,
+//                     true) -- skipSymmetry, pointer compression only
+//                     (geom_octree.cpp:596-601); internalCall only silences
+//                     its log -- on a copy of the DAG, and a REFSKIP line
+//                     with its nNodesSDAG
 //   --traverse <pts>  <out_prefix>.trav: EncodedSSVDAG::traverse
 //                     (encoded_ssvdag.cpp:527-574) of the .ssvdag encoding
 //                     for every point of <pts> (u64 n, then n float[3]); one
@@ -145,7 +150,7 @@ int main(int argc, char** argv) {
   unsigned levels = (unsigned)std::atoi(argv[2]);
   std::string pre = argv[3];
   int step = 0;
-  bool soup = false, soup_only = false, flood = false, lossy = false;
+  bool soup = false, soup_only = false, flood = false, lossy = false, sdag_skip = false;
   float infl = 2.f, diff_factor = 1.f;
   int refs = 1;
   std::string trav_pts;
@@ -154,6 +159,7 @@ int main(int argc, char** argv) {
     if (o == "--soup") soup = true;
     else if (o == "--soup-only") soup = soup_only = true;
     else if (o == "--flood") flood = true;
+    else if (o == "--sdag-skip") sdag_skip = true;
     else if (o == "--traverse" && a + 1 < argc) trav_pts = argv[++a];
     else if (o == "--lossy" && a + 3 < argc) {
       lossy = true;
@@ -224,6 +230,13 @@ int main(int argc, char** argv) {
       levels, st_svo.nTotalVoxels, st_svo.nNodesSVO, st_svo.nNodesLastLevSVO, oct.getStats().nNodesDAG,
       sd.getStats().nNodesSDAG, cs.getNNodes(), merged, t_dag, t_sdag, t_csv);
   std::fflush(stdout);
+  if (sdag_skip) {
+    GeomOctree sk(oct);
+    sk.toSDAG(true, true);
+    dump_pool(sk, pre + ".sdagskip.pool");
+    std::printf("REFSKIP {\"nNodesSDAG\": %zu}\n", (size_t)sk.getStats().nNodesSDAG);
+    std::fflush(stdout);
+  }
   if (lossy) {
     GeomOctree lo(oct);
     lo.toLossyDag(infl, diff_factor, refs);

@@ -296,8 +296,11 @@ void invert_invs(const ora_octree* o, Node& n, uint32_t lev, bool x, bool y, boo
   }
 }
 
-// GeomOctree::toSDAG(false, false) (src/symvox/geom_octree.cpp:551-697)
-int to_sdag(ora_octree* o) {
+// GeomOctree::toSDAG(false, skip_symmetry) (src/symvox/geom_octree.cpp:551-697).
+// With skip_symmetry (:596-601, "pointer compression" only) every non-empty
+// node is kept in order with no invariance bits and no lookups; a pointer to
+// a dropped empty node keeps the default correspondence (id 0, no mirrors).
+int to_sdag(ora_octree* o, bool skip_symmetry = false) {
   if (o->state != 1 && o->state != 2) return -1;
   struct Corr { uint8_t m; uint32_t id; };
   std::map<Node, uint32_t, KeyLess> seen;
@@ -312,6 +315,11 @@ int to_sdag(ora_octree* o) {
     for (size_t i = 0; i < L.size(); ++i) {
       Node n = L[i];
       if (n.mask == 0) continue;
+      if (skip_symmetry) {
+        corr[i] = Corr{0, uint32_t(uniq.size())};
+        uniq.push_back(n);
+        continue;
+      }
       if (key_eq(n, mirror(n, true, false, false))) n.inv |= 1u;
       if (key_eq(n, mirror(n, false, true, false))) n.inv |= 2u;
       if (key_eq(n, mirror(n, false, false, true))) n.inv |= 4u;
@@ -1037,6 +1045,7 @@ int ora_ssvdag_traverse(const uint16_t* inner, uint64_t n_inner, const uint8_t* 
 
 int ora_to_dag(ora_octree* o) { return o ? to_dag(o) : -1; }
 int ora_to_sdag(ora_octree* o) { return o ? to_sdag(o) : -1; }
+int ora_to_sdag_ex(ora_octree* o, int skip_symmetry) { return o ? to_sdag(o, skip_symmetry != 0) : -1; }
 int ora_init_child_levels(ora_octree* o) {
   if (!o) return -1;
   init_child_levels(o);

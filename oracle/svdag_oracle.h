@@ -62,6 +62,7 @@ int ora_flood_fill(ora_octree* o, uint64_t* n_empty, uint64_t* n_surface);
 int ora_get_outside(const ora_octree* o, uint32_t level, uint8_t* out);
 int ora_to_dag(ora_octree* o);                 /* geom_octree.cpp:462-548 */
 int ora_to_sdag(ora_octree* o);                /* geom_octree.cpp:551-697 (greedy, symmetry on) */
+int ora_to_sdag_ex(ora_octree* o, int skip_symmetry); /* the same, skipSymmetry (:596-601) when non-zero */
 int ora_init_child_levels(ora_octree* o);      /* geom_octree_extension.cpp:21-30 */
 int ora_merge_across_levels(ora_octree* o);    /* geom_octree_extension.cpp:1192-1544 */
 

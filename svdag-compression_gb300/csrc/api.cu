@@ -299,6 +299,12 @@ int svdag_reduce_sdag(svdag_ctx* h) {
   return guarded(h, [&](Ctx& c) { c.st.sdag_ms = timed(c, [&] { svdag::phase_reduce_sdag(c); }); });
 }
 
+int svdag_reduce_sdag_ex(svdag_ctx* h, uint32_t flags) {
+  if (flags & ~uint32_t(SVDAG_SDAG_SKIP_SYMMETRY)) return fail(h, SVDAG_ERR_INVALID_ARG, "reduce_sdag_ex: unknown flags");
+  if (!(flags & SVDAG_SDAG_SKIP_SYMMETRY)) return svdag_reduce_sdag(h);
+  return guarded(h, [&](Ctx& c) { c.st.sdag_ms = timed(c, [&] { svdag::phase_reduce_sdag_skip_symmetry(c); }); });
+}
+
 int svdag_cross_level_merge(svdag_ctx* h) {
   return guarded(h, [&](Ctx& c) { c.st.csv_ms = timed(c, [&] { svdag::phase_cross_level_merge(c); }); });
 }

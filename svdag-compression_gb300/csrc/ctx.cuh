@@ -74,6 +74,8 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bbox[6], const uint32_
 void phase_build_dag(Ctx& c, uint32_t levels, uint32_t step_level, const double bbox[6]);
 void phase_reduce_dag(Ctx& c);
 void phase_reduce_sdag(Ctx& c);
+// toSDAG with skipSymmetry: pointer compression only (reduce.cu)
+void phase_reduce_sdag_skip_symmetry(Ctx& c);
 void phase_cross_level_merge(Ctx& c);
 // GeomOctree::hiddenGeometryFloodfill: outside masks of an SVO (floodfill.cu).
 void phase_flood_fill(Ctx& c, uint64_t* n_empty, uint64_t* n_surface);

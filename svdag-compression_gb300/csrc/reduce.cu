@@ -771,6 +771,91 @@ void phase_reduce_sdag(Ctx& c) {
 }
 
 // ---------------------------------------------------------------------------
+// toSDAG(internalCall, skipSymmetry = true) (src/symvox/geom_octree.cpp:
+// 596-601, "pointer compression" only): per level, bottom-up, every
+// non-empty node is kept in order with no invariance bits and no mirror
+// lookups; the parents' pointers follow the kept nodes, and a pointer to a
+// dropped empty node takes the reference's default correspondence (id 0, no
+// mirror bits).  A DAG made by toDAG has no empty nodes, so there the pools
+// stay as they are (one count per level, invariance bytes zeroed); imported
+// pools may have some, and are compacted.
+namespace {
+
+struct NonEmptyIn {
+  const uint32_t* hdr;
+  __device__ __forceinline__ uint32_t operator()(uint64_t i) const { return (hdr[i] & 0xFFu) ? 1u : 0u; }
+};
+
+__global__ void k_skip_compact(const uint32_t* __restrict__ hdr, const uint32_t* __restrict__ ch, uint64_t n,
+                               const uint32_t* __restrict__ newidx, uint32_t* __restrict__ ohdr,
+                               uint32_t* __restrict__ och) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    if (!(hdr[i] & 0xFFu)) continue;
+    const uint32_t id = newidx[i];
+    ohdr[id] = hdr[i];
+    if (ch) {
+      uint32_t c[8];
+      load_children(ch, i, c);
+      store_children(och, id, c);
+    }
+  }
+}
+
+// Parent pointers into a compacted level (child_hdr: its headers before).
+__global__ void k_skip_remap(uint32_t* __restrict__ pch, uint64_t pn, const uint32_t* __restrict__ child_hdr,
+                             const uint32_t* __restrict__ newidx) {
+  for (uint64_t p = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; p < pn; p += uint64_t(gridDim.x) * blockDim.x) {
+    uint32_t c[8];
+    load_children(pch, p, c);
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if (c[j] != kNull) c[j] = (child_hdr[c[j]] & 0xFFu) ? newidx[c[j]] : 0u;
+    store_children(pch, p, c);
+  }
+}
+
+}  // namespace
+
+void phase_reduce_sdag_skip_symmetry(Ctx& c) {
+  if (c.state != SVDAG_S_SVO && c.state != SVDAG_S_DAG)
+    throw Error(SVDAG_ERR_INVALID_STATE, "toSDAG: the octree is not a DAG");
+  if (c.state == SVDAG_S_SVO && c.levels >= 2) throw Error(SVDAG_ERR_INVALID_STATE, "toSDAG on an SVO: run toDAG first");
+  const Exec& ex = c.ex;
+  const cudaStream_t st = c.stream;
+  const uint32_t L = c.levels;
+  uint64_t nnodes = 0;
+  for (uint32_t l = L > 0 ? L - 1 : 0; l >= 1; --l) {
+    Level& V = c.lev[l];
+    const uint64_t n = V.n;
+    uint64_t kept = 0;
+    if (n) {
+      DBuf<uint32_t> newidx(n, st), d_cnt(1, st);
+      device_exclusive_scan<uint32_t>(ex, NonEmptyIn{V.hdr.get()}, n, U32Out{newidx.get()}, d_cnt.get());
+      kept = read_scalar(ex, d_cnt.get());
+      if (kept != n) {
+        const bool inner = l + 1 < L && V.ch.get();
+        DBuf<uint32_t> ohdr(kept ? kept : 1, st), och;
+        if (inner) och.alloc(8 * (kept ? kept : 1), st);
+        SVDAG_LAUNCH(ex, k_skip_compact, grid_for(ex, n, 256), 256, 0, V.hdr.get(), inner ? V.ch.get() : nullptr, n,
+                     newidx.get(), ohdr.get(), inner ? och.get() : nullptr);
+        const Level& P = c.lev[l - 1];
+        if (P.n && P.ch.get())
+          SVDAG_LAUNCH(ex, k_skip_remap, grid_for(ex, P.n, 256), 256, 0, P.ch.get(), P.n, V.hdr.get(), newidx.get());
+        V.hdr = std::move(ohdr);
+        if (inner) V.ch = std::move(och);
+        V.n = kept;
+      }
+    }
+    V.inv.alloc(kept ? kept : 1, st);
+    SVDAG_CUDA(cudaMemsetAsync(V.inv.get(), 0, kept ? kept : 1, st));
+    nnodes += kept;
+  }
+  c.st.n_nodes_sdag = nnodes;
+  c.st.n_nodes = nnodes;
+  c.state = SVDAG_S_SDAG;
+}
+
+// ---------------------------------------------------------------------------
 // toDAG on caller-provided device scratch: the same kernels and the same
 // result as phase_reduce_dag, with every temporary placed in `scratch` and
 // each reduced level copied back to the front of its own buffers (a level

@@ -52,8 +52,8 @@ void GeomOctree::toDAG() {
   invalidate();
 }
 
-void GeomOctree::toSDAG() {
-  check(svdag_reduce_sdag(ctx_));
+void GeomOctree::toSDAG(bool /*internalCall*/, bool skipSymmetry) {
+  check(svdag_reduce_sdag_ex(ctx_, skipSymmetry ? SVDAG_SDAG_SKIP_SYMMETRY : 0));
   invalidate();
 }
 

@@ -65,7 +65,9 @@ class GeomOctree {
   // build, same node order as the reference.
   void buildDAG(unsigned levels, unsigned stepLevel, const double bbox[6]);
   void toDAG();
-  void toSDAG();
+  // toSDAG(internalCall, skipSymmetry) (geom_octree.cpp:551-697); internalCall
+  // only silences the reference's log
+  void toSDAG(bool internalCall = false, bool skipSymmetry = false);
   unsigned mergeAcrossAllLevels();
   // toLossyDag(lossyInflation, allowedLossyDiffFactor, includedNodeRefCount)
   // (geom_octree_extension.cpp:797-1179).  The reference clusters its

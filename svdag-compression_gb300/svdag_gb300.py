@@ -72,6 +72,7 @@ GPU_SYMBOLS = {
     "svdag_tri_box_children": (_I, [_VP, _VP, _VP, _VP, _U64, _VP, ctypes.POINTER(_U64)]),
     "svdag_init_child_levels": (_I, [_VP]),
     "svdag_reduce_sdag": (_I, [_VP]),
+    "svdag_reduce_sdag_ex": (_I, [_VP, _U32]),
     "svdag_cross_level_merge": (_I, [_VP]),
     "svdag_level_count": (_I, [_VP, _U32, ctypes.POINTER(_U64)]),
     "svdag_download_level": (_I, [_VP, _U32, _VP, _VP, _VP, _VP]),
@@ -463,8 +464,9 @@ class Octree:
     def initChildLevels(self):
         self._check(self._lib.svdag_init_child_levels(self._h))
 
-    def toSDAG(self):
-        self._check(self._lib.svdag_reduce_sdag(self._h))
+    def toSDAG(self, skip_symmetry=False):
+        """GeomOctree::toSDAG(false, skipSymmetry)."""
+        self._check(self._lib.svdag_reduce_sdag_ex(self._h, 1 if skip_symmetry else 0))
 
     def mergeAcrossAllLevels(self):
         self._check(self._lib.svdag_cross_level_merge(self._h))

@@ -5,7 +5,8 @@ by oracle/Makefile) on seeded synthetic scenes.
     python tests/golden/make_golden.py
 
 Each case records the reference's counts and SHA-256 digests of its SVO,
-DAG, SDAG and CSVDAG node pools (48-byte records, oracle/ref_dump.cpp) and of
+DAG, SDAG and CSVDAG node pools (48-byte records, oracle/ref_dump.cpp), of
+the pool toSDAG leaves with skipSymmetry (pointer compression only), and of
 the encoded .svdag/.esvdag/.ussvdag/.ssvdag/.csv.svdag files; the FLOOD cases
 also the outside masks of the reference's hiddenGeometryFloodfill.  Small
 cases also keep their full DAG/SDAG/CSVDAG pools as .npz.  `--obj` writes
@@ -161,7 +162,7 @@ def run_case(name, make, levels, step, keep):
         obj = os.path.join(td, "scene.obj")
         sv.write_obj(obj, tris, True)
         pre = os.path.join(td, "out")
-        extra = ["--flood"] if name in FLOOD else []
+        extra = ["--sdag-skip"] + (["--flood"] if name in FLOOD else [])
         if name in TRAVERSE:
             pts = traverse_points(levels)
             with open(os.path.join(td, "pts.bin"), "wb") as f:
@@ -173,11 +174,13 @@ def run_case(name, make, levels, step, keep):
         line = [l for l in r.stdout.splitlines() if l.startswith("REFJSON ")][-1]
         info = json.loads(line[len("REFJSON "):])
         info["missing_correspondence_prints"] = r.stdout.count("Missing correspondence")
+        skip = [l for l in r.stdout.splitlines() if l.startswith("REFSKIP ")][-1]
+        info["nNodesSDAGSkipSymmetry"] = json.loads(skip[len("REFSKIP "):])["nNodesSDAG"]
         info["step_levels"] = step
         info["n_tris"] = int(tris.shape[0])
         info["tris_sha256"] = hashlib.sha256(np.ascontiguousarray(tris).tobytes()).hexdigest()
         pools = {}
-        for kind in ("svo", "dag", "sdag", "csv"):
+        for kind in ("svo", "dag", "sdag", "csv", "sdagskip"):
             p = pre + "." + kind + ".pool"
             if not os.path.exists(p):
                 continue

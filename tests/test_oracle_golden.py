@@ -41,6 +41,11 @@ def test_oracle_matches_reference_pools(name):
     s.toSDAG()
     assert oracle_py.pool_digest(s.pool()) == g["sdag"]["digest"]
     assert s.stats()["n_nodes_sdag"] == g["nNodesSDAG"]
+    # toSDAG with skipSymmetry (pointer compression only)
+    k = o.clone()
+    k.toSDAG(skip_symmetry=True)
+    assert oracle_py.pool_digest(k.pool()) == g["sdagskip"]["digest"]
+    assert k.stats()["n_nodes_sdag"] == g["nNodesSDAGSkipSymmetry"]
     c = o.clone()
     c.mergeAcrossAllLevels()
     assert oracle_py.pool_digest(c.pool()) == g["csv"]["digest"]
