@@ -103,6 +103,15 @@ int svdag_set_device_triangles(svdag_ctx* ctx, const float* device_tris, uint64_
 /* GeomOctree::buildSVO(levels, bbox) (src/symvox/geom_octree.cpp:171-280):
  * bbox = {minx, miny, minz, maxx, maxy, maxz} in double, 1 <= levels <= 21. */
 int svdag_voxelize(svdag_ctx* ctx, uint32_t levels, const double bbox[6]);
+/* The same; with SVDAG_VOXELIZE_LEAF_CENTERS the build keeps buildSVO's
+ * leavesCenters (geom_octree.cpp:245-246: the fp64 centre each leaf-level
+ * node was created with, in node order; none for levels == 1), read with
+ * svdag_download_leaf_centers until the next voxelization (count = the
+ * leaf level's node count; capacity in centres, 3 doubles each; a capacity
+ * below the count is SVDAG_ERR_OVERFLOW; NULL xyz only counts). */
+enum { SVDAG_VOXELIZE_LEAF_CENTERS = 1 };
+int svdag_voxelize_ex(svdag_ctx* ctx, uint32_t levels, const double bbox[6], uint32_t flags);
+int svdag_download_leaf_centers(svdag_ctx* ctx, double* xyz, uint64_t capacity, uint64_t* count);
 /* GeomOctree::buildDAG(levels, stepLevel, bbox) (src/symvox/geom_octree.cpp:289-435):
  * the chunked build svbuilder runs for numBuildSteps > 0
  * (src/svbuilder/main.cpp:158-175) -- a top SVO of stepLevel+1 levels, one

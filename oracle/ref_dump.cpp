@@ -24,6 +24,10 @@
 //                     before it runs the external MCL program as
 //                     $HOME/local/bin/mcl (cluster.hpp:134-192), which the
 //                     caller provides
+//   --leaf-centers    <out_prefix>.leafctr: the leavesCenters list of a
+//                     second GeomOctree::buildSVO(levels, bbox, true,
+//                     &centers) (geom_octree.cpp:245-246): u64 n, then n
+//                     double[3] (plain builds only)
 //   --sdag-skip       <out_prefix>.sdagskip.pool: GeomOctree::toSDAG(true,
 //                     true) -- skipSymmetry, pointer compression only
 //                     (geom_octree.cpp:596-601); internalCall only silences
@@ -150,7 +154,7 @@ int main(int argc, char** argv) {
   unsigned levels = (unsigned)std::atoi(argv[2]);
   std::string pre = argv[3];
   int step = 0;
-  bool soup = false, soup_only = false, flood = false, lossy = false, sdag_skip = false;
+  bool soup = false, soup_only = false, flood = false, lossy = false, sdag_skip = false, leaf_centers = false;
   float infl = 2.f, diff_factor = 1.f;
   int refs = 1;
   std::string trav_pts;
@@ -160,6 +164,7 @@ int main(int argc, char** argv) {
     else if (o == "--soup-only") soup = soup_only = true;
     else if (o == "--flood") flood = true;
     else if (o == "--sdag-skip") sdag_skip = true;
+    else if (o == "--leaf-centers") leaf_centers = true;
     else if (o == "--traverse" && a + 1 < argc) trav_pts = argv[++a];
     else if (o == "--lossy" && a + 3 < argc) {
       lossy = true;
@@ -176,6 +181,20 @@ int main(int argc, char** argv) {
   if (soup_only) return 0;
   auto minF = scene.getAABB()[0], maxF = scene.getAABB()[1];
   sl::aabox3d bb(sl::point3d(minF[0], minF[1], minF[2]), sl::point3d(maxF[0], maxF[1], maxF[2]));
+
+  if (leaf_centers && step == 0) {
+    GeomOctree lc(&scene);
+    std::vector<sl::point3d> centers;
+    lc.buildSVO(levels, bb, true, &centers, false);
+    FILE* f = std::fopen((pre + ".leafctr").c_str(), "wb");
+    const uint64_t n = centers.size();
+    std::fwrite(&n, 8, 1, f);
+    for (const auto& c : centers) {
+      const double v[3] = {c[0], c[1], c[2]};
+      std::fwrite(v, 8, 3, f);
+    }
+    std::fclose(f);
+  }
 
   GeomOctree oct(&scene);
   sl::real_time_clock ck;

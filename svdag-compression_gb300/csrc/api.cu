@@ -169,6 +169,7 @@ int svdag_destroy(svdag_ctx* h) {
   c.owned_tris.release();
   c.ss_inner.clear();
   c.ss_leaves.release();
+  c.leaf_ctr.release();
   cudaStreamSynchronize(c.stream);
   if (c.ev0) cudaEventDestroy(c.ev0);
   if (c.ev1) cudaEventDestroy(c.ev1);
@@ -236,6 +237,32 @@ int svdag_set_device_triangles(svdag_ctx* h, const float* device_tris, uint64_t 
 int svdag_voxelize(svdag_ctx* h, uint32_t levels, const double bbox[6]) {
   if (!bbox) return fail(h, SVDAG_ERR_INVALID_ARG, "voxelize: null bbox");
   return guarded(h, [&](Ctx& c) { c.st.svo_ms = timed(c, [&] { svdag::phase_voxelize(c, levels, bbox); }); });
+}
+
+int svdag_voxelize_ex(svdag_ctx* h, uint32_t levels, const double bbox[6], uint32_t flags) {
+  if (!bbox) return fail(h, SVDAG_ERR_INVALID_ARG, "voxelize: null bbox");
+  if (flags & ~uint32_t(SVDAG_VOXELIZE_LEAF_CENTERS)) return fail(h, SVDAG_ERR_INVALID_ARG, "voxelize_ex: unknown flags");
+  return guarded(h, [&](Ctx& c) {
+    c.keep_leaf_centers = (flags & SVDAG_VOXELIZE_LEAF_CENTERS) != 0;
+    try {
+      c.st.svo_ms = timed(c, [&] { svdag::phase_voxelize(c, levels, bbox); });
+    } catch (...) {
+      c.keep_leaf_centers = false;
+      throw;
+    }
+    c.keep_leaf_centers = false;
+  });
+}
+
+int svdag_download_leaf_centers(svdag_ctx* h, double* xyz, uint64_t capacity, uint64_t* count) {
+  return guarded(h, [&](Ctx& c) {
+    const uint64_t n = c.leaf_ctr.get() ? c.leaf_ctr_n : 0;
+    if (count) *count = n;
+    if (!xyz || !n) return;
+    if (capacity < n) throw svdag::Error(SVDAG_ERR_OVERFLOW, "download_leaf_centers: capacity below the count");
+    SVDAG_CUDA(cudaMemcpyAsync(xyz, c.leaf_ctr.get(), 24 * n, cudaMemcpyDeviceToHost, c.stream));
+    SVDAG_CUDA(cudaStreamSynchronize(c.stream));
+  });
 }
 
 int svdag_build_dag(svdag_ctx* h, uint32_t levels, uint32_t step_level, const double bbox[6]) {

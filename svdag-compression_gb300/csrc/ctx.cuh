@@ -50,6 +50,12 @@ struct Ctx {
   svdag_stats st{};
   std::string last_error;
 
+  // buildSVO's leavesCenters (geom_octree.cpp:245-246): the fp64 centre of
+  // every leaf-level node, in node order, kept by svdag_voxelize_ex on request
+  bool keep_leaf_centers = false;
+  DBuf<double> leaf_ctr;
+  uint64_t leaf_ctr_n = 0;
+
   // Outside masks taken off the levels by svdag_reduce_dag_noalloc, which
   // may not free device memory: released by a later call on the context
   // (every entry point that can allocate) or by svdag_destroy.

@@ -479,6 +479,8 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6], const uint32_t*
   c.lev.clear();
   c.lev.resize(levels);
   c.child_levels_init = false;
+  c.leaf_ctr.release();
+  c.leaf_ctr_n = 0;
 
   // level 0: the root
   c.lev[0].n = 1;
@@ -587,6 +589,12 @@ void phase_voxelize(Ctx& c, uint32_t levels, const double bb[6], const uint32_t*
     if (P_.n)
       SVDAG_LAUNCH(ex, k_clean_empty, grid_for(ex, P_.n, 256), 256, 0, P_.hdr.get(), P_.ch.get(), P_.n,
                    c.lev[lev].hdr.get());
+  }
+  // leavesCenters: the centres the leaf level's nodes were created with
+  // (none for a single level, whose root is the leaf)
+  if (c.keep_leaf_centers && levels >= 2) {
+    c.leaf_ctr = std::move(c.lev[levels - 1].ctr);
+    c.leaf_ctr_n = c.lev[levels - 1].n;
   }
   for (auto& L : c.lev) {
     L.ctr.release();

@@ -26,10 +26,17 @@ GeomOctree::~GeomOctree() {
   if (ctx_) svdag_destroy(ctx_);
 }
 
-void GeomOctree::buildSVO(unsigned levels, const double bb[6]) {
+void GeomOctree::buildSVO(unsigned levels, const double bb[6], bool /*internalCall*/,
+                          std::vector<std::array<double, 3>>* leavesCenters) {
   if (!scene_) throw std::runtime_error("GeomOctree::buildSVO: no scene");
   check(svdag_upload_triangles(ctx_, scene_->triangles().data(), scene_->nTriangles()));
-  check(svdag_voxelize(ctx_, levels, bb));
+  check(svdag_voxelize_ex(ctx_, levels, bb, leavesCenters ? SVDAG_VOXELIZE_LEAF_CENTERS : 0));
+  if (leavesCenters) {
+    uint64_t n = 0;
+    check(svdag_download_leaf_centers(ctx_, nullptr, 0, &n));
+    leavesCenters->resize(n);
+    if (n) check(svdag_download_leaf_centers(ctx_, leavesCenters->front().data(), n, &n));
+  }
   // Octree bbox and root side as resizeSceneBbox (octree.hpp:101-105)
   float b[6];
   for (int k = 0; k < 6; ++k) b[k] = float(bb[k]);

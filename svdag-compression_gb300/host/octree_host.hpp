@@ -11,6 +11,7 @@
 
 #include <stdint.h>
 
+#include <array>
 #include <string>
 #include <vector>
 
@@ -60,7 +61,11 @@ class GeomOctree {
 
   void setScene(Scene* s) { scene_ = s; }
   // buildSVO(levels, bbox) (geom_octree.cpp:171-280); bbox = {min xyz, max xyz}
-  void buildSVO(unsigned levels, const double bbox[6]);
+  // With leavesCenters, also the reference's list of leaf-node centres
+  // (geom_octree.cpp:245-246), in node order; internalCall only silences the
+  // reference's log.  putMaterialIdInLeaves is not supported.
+  void buildSVO(unsigned levels, const double bbox[6], bool internalCall = false,
+                std::vector<std::array<double, 3>>* leavesCenters = nullptr);
   // buildDAG(levels, stepLevel, bbox) (geom_octree.cpp:289-435): chunked
   // build, same node order as the reference.
   void buildDAG(unsigned levels, unsigned stepLevel, const double bbox[6]);

@@ -73,6 +73,8 @@ GPU_SYMBOLS = {
     "svdag_init_child_levels": (_I, [_VP]),
     "svdag_reduce_sdag": (_I, [_VP]),
     "svdag_reduce_sdag_ex": (_I, [_VP, _U32]),
+    "svdag_voxelize_ex": (_I, [_VP, _U32, _VP, _U32]),
+    "svdag_download_leaf_centers": (_I, [_VP, _VP, _U64, ctypes.POINTER(_U64)]),
     "svdag_cross_level_merge": (_I, [_VP]),
     "svdag_level_count": (_I, [_VP, _U32, ctypes.POINTER(_U64)]),
     "svdag_download_level": (_I, [_VP, _U32, _VP, _VP, _VP, _VP]),
@@ -336,9 +338,21 @@ class Octree:
         self._check(self._lib.svdag_set_device_triangles(self._h, ctypes.c_void_p(dev_ptr), n_tris))
 
     # GeomOctree surface
-    def buildSVO(self, levels, bbox=UNIT_BOX):
+    def buildSVO(self, levels, bbox=UNIT_BOX, leaves_centers=False):
+        """GeomOctree::buildSVO; with leaves_centers, returns its leavesCenters
+        list (the fp64 centre of every leaf-level node, in node order) as an
+        (n, 3) float64 array."""
         bb = (ctypes.c_double * 6)(*bbox)
-        self._check(self._lib.svdag_voxelize(self._h, levels, bb))
+        if not leaves_centers:
+            self._check(self._lib.svdag_voxelize(self._h, levels, bb))
+            return None
+        self._check(self._lib.svdag_voxelize_ex(self._h, levels, bb, 1))
+        n = _U64()
+        self._check(self._lib.svdag_download_leaf_centers(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros((n.value, 3), np.float64)
+        if n.value:
+            self._check(self._lib.svdag_download_leaf_centers(self._h, out.ctypes.data, n.value, ctypes.byref(n)))
+        return out
 
     def buildDAG(self, levels, step_level, bbox=UNIT_BOX):
         """GeomOctree::buildDAG: chunked build, DAG state, reference node order."""

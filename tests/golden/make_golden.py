@@ -6,7 +6,8 @@ by oracle/Makefile) on seeded synthetic scenes.
 
 Each case records the reference's counts and SHA-256 digests of its SVO,
 DAG, SDAG and CSVDAG node pools (48-byte records, oracle/ref_dump.cpp), of
-the pool toSDAG leaves with skipSymmetry (pointer compression only), and of
+the pool toSDAG leaves with skipSymmetry (pointer compression only), of the
+leavesCenters list buildSVO fills (plain builds), and of
 the encoded .svdag/.esvdag/.ussvdag/.ssvdag/.csv.svdag files; the FLOOD cases
 also the outside masks of the reference's hiddenGeometryFloodfill.  Small
 cases also keep their full DAG/SDAG/CSVDAG pools as .npz.  `--obj` writes
@@ -162,7 +163,7 @@ def run_case(name, make, levels, step, keep):
         obj = os.path.join(td, "scene.obj")
         sv.write_obj(obj, tris, True)
         pre = os.path.join(td, "out")
-        extra = ["--sdag-skip"] + (["--flood"] if name in FLOOD else [])
+        extra = ["--sdag-skip", "--leaf-centers"] + (["--flood"] if name in FLOOD else [])
         if name in TRAVERSE:
             pts = traverse_points(levels)
             with open(os.path.join(td, "pts.bin"), "wb") as f:
@@ -189,6 +190,10 @@ def run_case(name, make, levels, step, keep):
                           "nnodes": int(pool["nnodes"]), "nvoxels": int(pool["nvoxels"])}
             pools[kind] = pool["pool"]
         info["files"] = {ext: sha(pre + "." + ext) for ext in ("svdag", "esvdag", "ussvdag", "ssvdag", "csv.svdag")}
+        if os.path.exists(pre + ".leafctr"):
+            raw = open(pre + ".leafctr", "rb").read()
+            info["leaf_centers"] = {"count": int(np.frombuffer(raw[:8], np.uint64)[0]),
+                                    "sha256": hashlib.sha256(raw[8:]).hexdigest()}
         if name in TRAVERSE:
             res = np.fromfile(pre + ".trav", np.int32)
             np.savez_compressed(os.path.join(HERE, name + "_traverse.npz"), depth=res.astype(np.int8))
