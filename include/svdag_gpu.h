@@ -161,13 +161,17 @@ int svdag_lossy_candidates(svdag_ctx* ctx, uint32_t level, float diff_factor, in
                            uint64_t* count);
 /* GeomOctree::initChildLevels (src/symvox/geom_octree_extension.cpp:21-30) */
 int svdag_init_child_levels(svdag_ctx* ctx);
-/* GeomOctree::toSDAG(false, false) (src/symvox/geom_octree.cpp:551-697) */
+/* GeomOctree::toSDAG(false, false) (src/symvox/geom_octree.cpp:551-697).  On
+ * an SVO (the reference's direct "SVO -> SDAG", :554-556) the result is the
+ * one toDAG then toSDAG give -- the compiled reference's direct pass gives the
+ * same pools -- and nNodesDAG is left as it was. */
 int svdag_reduce_sdag(svdag_ctx* ctx);
 /* GeomOctree::toSDAG(false, skipSymmetry): flags 0 is svdag_reduce_sdag;
  * SVDAG_SDAG_SKIP_SYMMETRY is the reference's pointer-compression-only form
  * (geom_octree.cpp:596-601): every non-empty node kept in order, no
  * invariance bits, no mirror lookups (a DAG's pools stay as they are; empty
- * nodes of imported pools are dropped, a pointer to one becomes 0). */
+ * nodes of imported pools and of an SVO are dropped, a pointer to one becomes
+ * 0; an SVO's duplicates stay). */
 enum { SVDAG_SDAG_SKIP_SYMMETRY = 1 };
 int svdag_reduce_sdag_ex(svdag_ctx* ctx, uint32_t flags);
 /* GeomOctree::mergeAcrossAllLevels (src/symvox/geom_octree_extension.cpp:1192-1544) */

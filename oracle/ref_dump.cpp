@@ -28,6 +28,9 @@
 //                     second GeomOctree::buildSVO(levels, bbox, true,
 //                     &centers) (geom_octree.cpp:245-246): u64 n, then n
 //                     double[3] (plain builds only)
+//   --sdag-from-svo   <out_prefix>.sdagsvo.pool: GeomOctree::toSDAG straight
+//                     on a copy of the SVO ("SVO -> SDAG", geom_octree.cpp:
+//                     554-556), after initChildLevels (plain builds only)
 //   --sdag-skip       <out_prefix>.sdagskip.pool: GeomOctree::toSDAG(true,
 //                     true) -- skipSymmetry, pointer compression only
 //                     (geom_octree.cpp:596-601); internalCall only silences
@@ -154,7 +157,8 @@ int main(int argc, char** argv) {
   unsigned levels = (unsigned)std::atoi(argv[2]);
   std::string pre = argv[3];
   int step = 0;
-  bool soup = false, soup_only = false, flood = false, lossy = false, sdag_skip = false, leaf_centers = false;
+  bool soup = false, soup_only = false, flood = false, lossy = false, sdag_skip = false, leaf_centers = false,
+       sdag_from_svo = false;
   float infl = 2.f, diff_factor = 1.f;
   int refs = 1;
   std::string trav_pts;
@@ -165,6 +169,7 @@ int main(int argc, char** argv) {
     else if (o == "--flood") flood = true;
     else if (o == "--sdag-skip") sdag_skip = true;
     else if (o == "--leaf-centers") leaf_centers = true;
+    else if (o == "--sdag-from-svo") sdag_from_svo = true;
     else if (o == "--traverse" && a + 1 < argc) trav_pts = argv[++a];
     else if (o == "--lossy" && a + 3 < argc) {
       lossy = true;
@@ -203,6 +208,12 @@ int main(int argc, char** argv) {
   if (step == 0) {
     oct.buildSVO(levels, bb, false, NULL, false);
     dump_pool(oct, pre + ".svo.pool");
+    if (sdag_from_svo) {
+      GeomOctree s2(oct);
+      s2.initChildLevels();
+      s2.toSDAG(true, false);
+      dump_pool(s2, pre + ".sdagsvo.pool");
+    }
     if (flood) svo_copy = new GeomOctree(oct);
     oct.toDAG();
   } else {

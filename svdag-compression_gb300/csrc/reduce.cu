@@ -689,8 +689,17 @@ void phase_reduce_dag(Ctx& c) {
 void phase_reduce_sdag(Ctx& c) {
   if (c.state != SVDAG_S_SVO && c.state != SVDAG_S_DAG)
     throw Error(SVDAG_ERR_INVALID_STATE, "toSDAG: the octree is not a DAG");
-  // an SVO level may hold empty nodes; toSDAG skips them like toDAG
-  if (c.state == SVDAG_S_SVO && c.levels >= 2) throw Error(SVDAG_ERR_INVALID_STATE, "toSDAG on an SVO: run toDAG first");
+  if (c.state == SVDAG_S_SVO && c.levels >= 2) {
+    // The reference also reduces an SVO straight to an SDAG ("not best way",
+    // geom_octree.cpp:554-556); its symmetry classes appear in the same
+    // first-occurrence order whether or not toDAG ran first, so the result
+    // is the DAG's toSDAG.  Its toSDAG leaves nNodesDAG as it was; the
+    // SVO's outside masks go, as toDAG drops them.
+    const uint64_t dag_nodes = c.st.n_nodes_dag;
+    phase_reduce_dag(c);
+    for (auto& V : c.lev) V.outm.release();
+    c.st.n_nodes_dag = dag_nodes;
+  }
   const uint32_t L = c.levels;
   if (L > kMaxRedLevels) throw Error(SVDAG_ERR_INVALID_ARG, "toSDAG: too many levels");
   const Exec& ex = c.ex;
@@ -778,7 +787,8 @@ void phase_reduce_sdag(Ctx& c) {
 // dropped empty node takes the reference's default correspondence (id 0, no
 // mirror bits).  A DAG made by toDAG has no empty nodes, so there the pools
 // stay as they are (one count per level, invariance bytes zeroed); imported
-// pools may have some, and are compacted.
+// pools and SVOs may have some, and are compacted (an SVO keeps its
+// duplicates: the reference's skipSymmetry pass merges nothing).
 namespace {
 
 struct NonEmptyIn {
@@ -819,7 +829,9 @@ __global__ void k_skip_remap(uint32_t* __restrict__ pch, uint64_t pn, const uint
 void phase_reduce_sdag_skip_symmetry(Ctx& c) {
   if (c.state != SVDAG_S_SVO && c.state != SVDAG_S_DAG)
     throw Error(SVDAG_ERR_INVALID_STATE, "toSDAG: the octree is not a DAG");
-  if (c.state == SVDAG_S_SVO && c.levels >= 2) throw Error(SVDAG_ERR_INVALID_STATE, "toSDAG on an SVO: run toDAG first");
+  // on an SVO (empty nodes and duplicates) the same rule: only the empty
+  // nodes go; outside masks are numbered by the nodes before, and go too
+  for (auto& V : c.lev) V.outm.release();
   const Exec& ex = c.ex;
   const cudaStream_t st = c.stream;
   const uint32_t L = c.levels;

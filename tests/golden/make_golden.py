@@ -7,7 +7,8 @@ by oracle/Makefile) on seeded synthetic scenes.
 Each case records the reference's counts and SHA-256 digests of its SVO,
 DAG, SDAG and CSVDAG node pools (48-byte records, oracle/ref_dump.cpp), of
 the pool toSDAG leaves with skipSymmetry (pointer compression only), of the
-leavesCenters list buildSVO fills (plain builds), and of
+leavesCenters list buildSVO fills (plain builds), of the pool toSDAG leaves
+when run straight on the SVO (plain builds), and of
 the encoded .svdag/.esvdag/.ussvdag/.ssvdag/.csv.svdag files; the FLOOD cases
 also the outside masks of the reference's hiddenGeometryFloodfill.  Small
 cases also keep their full DAG/SDAG/CSVDAG pools as .npz.  `--obj` writes
@@ -163,7 +164,7 @@ def run_case(name, make, levels, step, keep):
         obj = os.path.join(td, "scene.obj")
         sv.write_obj(obj, tris, True)
         pre = os.path.join(td, "out")
-        extra = ["--sdag-skip", "--leaf-centers"] + (["--flood"] if name in FLOOD else [])
+        extra = ["--sdag-skip", "--leaf-centers", "--sdag-from-svo"] + (["--flood"] if name in FLOOD else [])
         if name in TRAVERSE:
             pts = traverse_points(levels)
             with open(os.path.join(td, "pts.bin"), "wb") as f:
@@ -181,7 +182,7 @@ def run_case(name, make, levels, step, keep):
         info["n_tris"] = int(tris.shape[0])
         info["tris_sha256"] = hashlib.sha256(np.ascontiguousarray(tris).tobytes()).hexdigest()
         pools = {}
-        for kind in ("svo", "dag", "sdag", "csv", "sdagskip"):
+        for kind in ("svo", "dag", "sdag", "csv", "sdagskip", "sdagsvo"):
             p = pre + "." + kind + ".pool"
             if not os.path.exists(p):
                 continue

@@ -41,6 +41,16 @@ def test_oracle_matches_reference_pools(name):
     s.toSDAG()
     assert oracle_py.pool_digest(s.pool()) == g["sdag"]["digest"]
     assert s.stats()["n_nodes_sdag"] == g["nNodesSDAG"]
+    if not g["step_levels"]:
+        # toSDAG straight on the SVO: the compiled reference's direct pass
+        # (oracle/ref_dump --sdag-from-svo) gives the same pools as toDAG
+        # then toSDAG, and so does the oracle's
+        assert g["sdagsvo"]["digest"] == g["sdag"]["digest"]
+        v = oracle_py.OracleOctree()
+        v.buildSVO(tris, g["levels"])
+        v.initChildLevels()
+        v.toSDAG()
+        assert oracle_py.pool_digest(v.pool()) == g["sdagsvo"]["digest"]
     # toSDAG with skipSymmetry (pointer compression only)
     k = o.clone()
     k.toSDAG(skip_symmetry=True)

@@ -2,7 +2,8 @@
 compression only (src/symvox/geom_octree.cpp:596-601) -- on the GPU: the
 reference's own pools (golden digests written by the compiled reference),
 and imported pools holding empty nodes, which it drops (a pointer to one
-takes the default correspondence, id 0)."""
+takes the default correspondence, id 0).  And toSDAG straight on an SVO
+(the reference's direct "SVO -> SDAG", :554-556), plain and skipSymmetry."""
 import numpy as np
 import pytest
 
@@ -79,3 +80,38 @@ def test_skip_symmetry_drops_empty_nodes():
         if l >= 1:
             assert not got[l]["inv"].any()
     assert d.stats()["n_nodes_sdag"] == sum(len(l) for l in want[1:])
+
+
+@pytest.mark.parametrize("name", ["ico3_L6", "terrain65_L8", "cavity_L7"])
+def test_sdag_straight_from_svo(name):
+    """The compiled reference's direct pass gives the golden SDAG pools (its
+    toSDAG on a copy of the SVO, oracle/ref_dump --sdag-from-svo); so does
+    the GPU's, and nNodesDAG stays as it was."""
+    g = G[name]
+    o = sv.Octree()
+    o.upload_triangles(SCENES[name]())
+    o.buildSVO(g["levels"])
+    o.initChildLevels()
+    dag_before = o.stats()["n_nodes_dag"]
+    o.toSDAG()
+    assert oracle_py.pool_digest(o.pool()) == g["sdagsvo"]["digest"]
+    assert o.stats()["n_nodes_sdag"] == g["nNodesSDAG"]
+    assert o.stats()["n_nodes_dag"] == dag_before
+
+
+@pytest.mark.parametrize("name", ["ico3_L6", "terrain65_L8"])
+def test_skip_symmetry_on_svo_matches_oracle(name):
+    """skipSymmetry on an SVO drops only its empty nodes (duplicates stay)."""
+    g = G[name]
+    tris = SCENES[name]()
+    o = sv.Octree()
+    o.upload_triangles(tris)
+    o.buildSVO(g["levels"])
+    o.initChildLevels()
+    o.toSDAG(skip_symmetry=True)
+    r = oracle_py.OracleOctree()
+    r.buildSVO(tris, g["levels"])
+    r.initChildLevels()
+    r.toSDAG(skip_symmetry=True)
+    assert oracle_py.pool_digest(o.pool()) == oracle_py.pool_digest(r.pool())
+    assert o.stats()["n_nodes_sdag"] == r.stats()["n_nodes_sdag"] > g["nNodesDAG"]
